@@ -1,0 +1,164 @@
+// Shared by every translation unit of libdiorama_gb300: the data layouts of the
+// reference's GPU structs, the context/buffer objects behind the C ABI, error
+// plumbing, and the device math the forward and backward passes share.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <string>
+#include <vector>
+
+#include "../../include/diorama_gb300.h"
+
+namespace dg {
+
+// ---------------------------------------------------------------- layouts
+// struct Gaussian (src/shaders/common.wgsl:11-17, src/gaussians.ts:38-46): position
+// xyz, opacity, scale xyz, pad, rotation (w,x,y,z), color rgb, pad.
+constexpr uint32_t FLOATS_PER_GAUSSIAN = 16;
+// struct Splat2D (src/shaders/common.wgsl:20-26): mean xy, depth, radius, conic
+// (a,b,c), pad, color rgb, opacity.
+constexpr uint32_t FLOATS_PER_SPLAT = 12;
+// Spherical-harmonic coefficients 1..15, rgb each, coefficient-major (src/gaussians.ts:34-36).
+constexpr uint32_t SH_REST_FLOATS = 45;
+// Adam moment slots per Gaussian, one vec2 each (src/trainer.ts:17).
+constexpr uint32_t MOMENT_SLOTS = FLOATS_PER_GAUSSIAN + SH_REST_FLOATS;
+// Gradients per splat from the blend's backward (src/shaders/rasterizeBackward.wgsl:124-126).
+constexpr uint32_t SPLAT_GRADS = 9;
+constexpr uint32_t TILE = 16;
+// At most 2^16 tiles, as the sort looks at 16 bits of the tile index (src/tileRasterizer.ts:10).
+constexpr uint32_t TILE_INDEX_BITS = 16;
+
+// The Camera uniform (src/shaders/common.wgsl:4-8): 144 bytes.
+struct Camera {
+  float view[16];  // column-major
+  float proj[16];
+  float viewport[2];
+  float pad[2];
+};
+static_assert(sizeof(Camera) == 144, "Camera is 144 bytes like the reference's uniform");
+
+// Bits of the device error word that bounded waits set instead of hanging.
+constexpr uint32_t DEVICE_ERROR_SCAN_WAIT = 1u << 0;
+constexpr uint32_t DEVICE_ERROR_SORT_WAIT = 1u << 1;
+// Iteration cap of every spin on another block's status (about a second at worst).
+constexpr uint32_t SPIN_LIMIT = 1u << 22;
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& message);
+dg_status fail(dg_status code, const std::string& message);
+dg_status cuda_fail(cudaError_t err, const char* what);
+
+#define DG_CUDA(call)                                             \
+  do {                                                            \
+    cudaError_t dg_err_ = (call);                                 \
+    if (dg_err_ != cudaSuccess) return ::dg::cuda_fail(dg_err_, #call); \
+  } while (0)
+
+#define DG_TRY(call)                         \
+  do {                                       \
+    dg_status dg_st_ = (call);               \
+    if (dg_st_ != DG_OK) return dg_st_;      \
+  } while (0)
+
+#define DG_REQUIRE(cond, msg)                                 \
+  do {                                                        \
+    if (!(cond)) return ::dg::fail(DG_ERROR_INVALID_ARGUMENT, msg); \
+  } while (0)
+
+// Kernel launches report their own configuration errors.
+#define DG_LAUNCHED(name) DG_CUDA(cudaGetLastError())
+
+inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace dg
+
+// ---------------------------------------------------------------- objects
+
+// A device allocation standing in for a GPUBuffer. Owned buffers are freed by
+// dg_buffer_destroy; wrapped ones only forget the pointer.
+struct dg_buffer {
+  dg_context* ctx;
+  void* ptr;
+  uint64_t bytes;
+  bool owned;
+};
+
+// The "device" and its "queue": one CUDA device and one stream, in order.
+struct dg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t* device_error = nullptr;  // set by bounded waits
+  int sm_count = 0;
+  // Pinned staging ring for queue.writeBuffer: each write is copied here at call
+  // time, so the caller's memory is free on return, as with WebGPU.
+  char* staging = nullptr;
+  size_t staging_bytes = 0;
+  size_t staging_head = 0;
+  struct Pending {
+    size_t begin, end;
+    cudaEvent_t done;
+  };
+  std::deque<Pending> pending;
+  std::vector<cudaEvent_t> free_events;
+  bool capturing = false;
+  // Kernels launched through this context (graph replays add their kernel count).
+  uint64_t launches = 0;
+};
+
+namespace dg {
+// Enqueue a host→device copy with writeBuffer semantics (the source is
+// snapshotted now). Not allowed while a graph is being captured.
+dg_status write_async(dg_context* ctx, void* dst, const void* src, size_t bytes);
+dg_status alloc_buffer(dg_context* ctx, uint64_t bytes, dg_buffer** out);
+void free_buffer(dg_buffer* b);
+inline void* ptr_of(dg_buffer* b) { return b ? b->ptr : nullptr; }
+template <typename T>
+inline T* typed(dg_buffer* b) {
+  return reinterpret_cast<T*>(b ? b->ptr : nullptr);
+}
+}  // namespace dg
+
+// ---------------------------------------------------------------- device math
+namespace dg {
+
+// e^x by Cody-Waite reduction x = n ln2 + r (|r| <= ln2/2), e^r from its Taylor
+// series to degree 7 by Horner's rule, and scaling by 2^n through the exponent
+// bits; results below the smallest normal float are 0. The blend's forward and
+// backward both use it, so their alpha tests agree exactly; its error is about
+// one ulp.
+__host__ __device__ __forceinline__ float exp_blend(float x) {
+  if (x < -87.0f) return 0.0f;
+  if (x > 88.0f) return INFINITY;
+  float n = rintf(x * 1.44269504088896341f);
+  float r = fmaf(n, -0.693145751953125f, x);
+  r = fmaf(n, -1.428606820309417232e-6f, r);
+  float p = 1.98412698412698413e-4f;
+  p = fmaf(p, r, 1.38888888888888889e-3f);
+  p = fmaf(p, r, 8.33333333333333333e-3f);
+  p = fmaf(p, r, 4.16666666666666667e-2f);
+  p = fmaf(p, r, 1.66666666666666667e-1f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  int32_t e = (int32_t)n + 127;
+#ifdef __CUDA_ARCH__
+  float scale = __int_as_float(e << 23);
+#else
+  float scale;
+  uint32_t bits = (uint32_t)e << 23;
+  std::memcpy(&scale, &bits, 4);
+#endif
+  return p * scale;
+}
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+
+constexpr float SH_C0 = 0.28209479177387814f;
+constexpr float SH_C1 = 0.4886025119029199f;
+
+}  // namespace dg

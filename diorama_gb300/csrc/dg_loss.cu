@@ -1,0 +1,377 @@
+// TrainingLoss (src/trainingLoss.ts:16-130, src/shaders/loss.wgsl:53-121):
+// 0.8 L1 + 0.2 (1 - SSIM) between a render and a photo, with an 11x11 Gaussian
+// window (sigma 1.5, zero padding), and its gradient with respect to every
+// rendered pixel.
+//
+// The reference makes 7 dispatches over 5-map and 3-map vec4 buffers (moments,
+// blur h, blur v, ssim, blur h, blur v, gradient: ~900 B/pixel of traffic). Here
+// it is 2 kernels. Each CTA owns a 16x16 block of pixels, loads its 26x26 halo
+// once, and does the separable blurs in shared memory:
+//   ssim_kernel:     moments -> blur h -> blur v -> SSIM and its three partials
+//   gradient_kernel: partials -> blur h -> blur v -> dL/dpixel and the pixel loss
+// Sums run over the taps -5..5 in order and skip taps past the image, as the
+// WGSL does, so the values are the reference's float32 values.
+//
+// The same ssim_kernel also measures held-out renders (PSNR and SSIM of the
+// 8-bit-quantized image, src/trainer.ts:371-386 and src/metrics.ts) on the GPU.
+#include "dg_common.cuh"
+#include "dg_loss.cuh"
+
+namespace dg {
+namespace {
+
+constexpr int LT = 16;             // pixels per side of a CTA's block
+constexpr int HALO = 5;
+constexpr int LS = LT + 2 * HALO;  // 26
+constexpr float LAMBDA = 0.2f;
+constexpr float C1 = 0.0001f;
+constexpr float C2 = 0.0009f;
+
+struct Window {
+  float w[6];
+};
+
+__device__ __forceinline__ float3 load_x(const float4* rendered, int w, int h, int x, int y, bool quantize) {
+  if (x < 0 || y < 0 || x >= w || y >= h) return make_float3(0.f, 0.f, 0.f);
+  float4 v = rendered[(size_t)y * w + x];
+  if (quantize) {
+    // src/trainer.ts:381: round(min(1, max(0, v)) * 255) / 255, in double as the
+    // TypeScript does, then stored as float32.
+    auto q = [](float c) {
+      double d = rint((double)fminf(1.0f, fmaxf(0.0f, c)) * 255.0);
+      return __double2float_rn(d / 255.0);
+    };
+    return make_float3(q(v.x), q(v.y), q(v.z));
+  }
+  return make_float3(v.x, v.y, v.z);
+}
+
+__device__ __forceinline__ float3 load_y(const uchar4* target, int w, int h, int x, int y, bool exact_quotient) {
+  if (x < 0 || y < 0 || x >= w || y >= h) return make_float3(0.f, 0.f, 0.f);
+  uchar4 t = target[(size_t)y * w + x];
+  if (exact_quotient)  // Float32Array.from(bytes, v => v / 255): the double quotient rounded to float
+    return make_float3(__double2float_rn(t.x / 255.0), __double2float_rn(t.y / 255.0), __double2float_rn(t.z / 255.0));
+  return make_float3((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f);
+}
+
+// Moments, both blurs and the SSIM partials for one 16x16 block. mode 0 (loss):
+// writes the three partials and S per channel to `partials` (12 floats per pixel:
+// dS/dmu_x rgb, dS/dE[x^2] rgb, dS/dE[xy] rgb, S rgb). mode 1 (metrics): the render
+// is quantized first, and each CTA adds its Σ S and Σ squared error to `sums`.
+__global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ rendered,
+                                                   const uchar4* const* __restrict__ target_slot, int w, int h,
+                                                   Window win, float* __restrict__ partials, int mode,
+                                                   double* __restrict__ sums) {
+  __shared__ float s_x[LS][LS][3];
+  __shared__ float s_y[LS][LS][3];
+  __shared__ float s_h[5][LS][LT][3];
+  __shared__ double s_red[2][8];
+  const uchar4* target = *target_slot;
+  const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
+  const bool metrics = mode == 1;
+  for (int k = threadIdx.x; k < LS * LS; k += 256) {
+    const int ly = k / LS, lx = k % LS;
+    float3 xv = load_x(rendered, w, h, x0 + lx, y0 + ly, metrics);
+    float3 yv = load_y(target, w, h, x0 + lx, y0 + ly, metrics);
+    s_x[ly][lx][0] = xv.x; s_x[ly][lx][1] = xv.y; s_x[ly][lx][2] = xv.z;
+    s_y[ly][lx][0] = yv.x; s_y[ly][lx][1] = yv.y; s_y[ly][lx][2] = yv.z;
+  }
+  __syncthreads();
+  // Horizontal pass over every halo row, for the 16 output columns.
+  for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
+    const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
+    const int gy = y0 + row;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f;
+    if (gy >= 0 && gy < h) {
+      for (int t = -HALO; t <= HALO; t++) {
+        const int gx = blockIdx.x * LT + col + t;
+        if (gx < 0 || gx >= w) continue;
+        const float wt = win.w[t < 0 ? -t : t];
+        const float xv = s_x[row][col + HALO + t][ch], yv = s_y[row][col + HALO + t][ch];
+        a0 = a0 + wt * xv;
+        a1 = a1 + wt * yv;
+        a2 = a2 + wt * (xv * xv);
+        a3 = a3 + wt * (yv * yv);
+        a4 = a4 + wt * (xv * yv);
+      }
+    }
+    s_h[0][row][col][ch] = a0;
+    s_h[1][row][col][ch] = a1;
+    s_h[2][row][col][ch] = a2;
+    s_h[3][row][col][ch] = a3;
+    s_h[4][row][col][ch] = a4;
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
+  const int gx = blockIdx.x * LT + lx, gy = blockIdx.y * LT + ly;
+  const bool inside = gx < w && gy < h;
+  double s_sum = 0.0, se_sum = 0.0;
+  if (inside) {
+    float out[12];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+      float m[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int t = -HALO; t <= HALO; t++) {
+        const int yy = gy + t;
+        if (yy < 0 || yy >= h) continue;
+        const float wt = win.w[t < 0 ? -t : t];
+#pragma unroll
+        for (int q = 0; q < 5; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
+      }
+      const float mx = m[0], my = m[1];
+      const float vx = m[2] - mx * mx, vy = m[3] - my * my, cxy = m[4] - mx * my;
+      const float a1 = 2.0f * mx * my + C1, a2 = 2.0f * cxy + C2;
+      const float b1 = mx * mx + my * my + C1, b2 = vx + vy + C2;
+      const float s = a1 * a2 / (b1 * b2);
+      out[ch] = s * (2.0f * my / a1 - 2.0f * my / a2 - 2.0f * mx / b1 + 2.0f * mx / b2);
+      out[3 + ch] = -s / b2;
+      out[6 + ch] = 2.0f * s / a2;
+      out[9 + ch] = s;
+      if (metrics) {
+        s_sum += (double)s;
+        const float xv = s_x[ly + HALO][lx + HALO][ch], yv = s_y[ly + HALO][lx + HALO][ch];
+        const double d = (double)xv - (double)yv;
+        se_sum += d * d;
+      }
+    }
+    if (!metrics) {
+      float4* dst = reinterpret_cast<float4*>(partials + ((size_t)gy * w + gx) * 12);
+      dst[0] = make_float4(out[0], out[1], out[2], out[3]);
+      dst[1] = make_float4(out[4], out[5], out[6], out[7]);
+      dst[2] = make_float4(out[8], out[9], out[10], out[11]);
+    }
+  }
+  if (metrics) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      s_sum += __shfl_xor_sync(0xffffffffu, s_sum, d);
+      se_sum += __shfl_xor_sync(0xffffffffu, se_sum, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      s_red[0][threadIdx.x >> 5] = s_sum;
+      s_red[1][threadIdx.x >> 5] = se_sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0, b = 0;
+      for (int k = 0; k < 8; k++) {
+        a += s_red[0][k];
+        b += s_red[1][k];
+      }
+      atomicAdd(&sums[0], a);
+      atomicAdd(&sums[1], b);
+    }
+  }
+}
+
+// Blurs the three partials and forms dL/dpixel and the pixel loss
+// (src/shaders/loss.wgsl:108-121).
+__global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict__ rendered,
+                                                       const uchar4* const* __restrict__ target_slot, int w, int h,
+                                                       Window win, const float* __restrict__ partials,
+                                                       float4* __restrict__ pixel_grads, float* __restrict__ pixel_loss) {
+  __shared__ float s_p[3][LS][LS][3];
+  __shared__ float s_h[3][LS][LT][3];
+  const uchar4* target = *target_slot;
+  const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
+  for (int k = threadIdx.x; k < LS * LS; k += 256) {
+    const int ly = k / LS, lx = k % LS;
+    const int gx = x0 + lx, gy = y0 + ly;
+    const bool in = gx >= 0 && gy >= 0 && gx < w && gy < h;
+    const float* src = partials + ((size_t)gy * w + gx) * 12;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) s_p[q][ly][lx][ch] = in ? src[q * 3 + ch] : 0.0f;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
+    const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
+    const int gy = y0 + row;
+    float a[3] = {0.f, 0.f, 0.f};
+    if (gy >= 0 && gy < h) {
+      for (int t = -HALO; t <= HALO; t++) {
+        const int gx = blockIdx.x * LT + col + t;
+        if (gx < 0 || gx >= w) continue;
+        const float wt = win.w[t < 0 ? -t : t];
+#pragma unroll
+        for (int q = 0; q < 3; q++) a[q] = a[q] + wt * s_p[q][row][col + HALO + t][ch];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) s_h[q][row][col][ch] = a[q];
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
+  const int gx = blockIdx.x * LT + lx, gy = blockIdx.y * LT + ly;
+  if (gx >= w || gy >= h) return;
+  const size_t p = (size_t)gy * w + gx;
+  const float scale = 1.0f / (float)(3u * (uint32_t)(w * h));
+  const float4 xv4 = rendered[p];
+  const uchar4 t4 = target[p];
+  const float xs[3] = {xv4.x, xv4.y, xv4.z};
+  const float ys[3] = {(float)t4.x / 255.0f, (float)t4.y / 255.0f, (float)t4.z / 255.0f};
+  const float* own = partials + p * 12;
+  float grad[3];
+  float lsum = 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    float m[3] = {0.f, 0.f, 0.f};
+    for (int t = -HALO; t <= HALO; t++) {
+      const int yy = gy + t;
+      if (yy < 0 || yy >= h) continue;
+      const float wt = win.w[t < 0 ? -t : t];
+#pragma unroll
+      for (int q = 0; q < 3; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
+    }
+    const float x = xs[ch], y = ys[ch];
+    const float sg = m[0] + 2.0f * x * m[1] + y * m[2];
+    const float diff = x - y;
+    const float sign = diff > 0.0f ? 1.0f : (diff < 0.0f ? -1.0f : 0.0f);
+    grad[ch] = ((1.0f - LAMBDA) * sign - LAMBDA * sg) * scale;
+    lsum = lsum + ((1.0f - LAMBDA) * fabsf(diff) - LAMBDA * own[9 + ch]);
+  }
+  pixel_grads[p] = make_float4(grad[0], grad[1], grad[2], 0.0f);
+  pixel_loss[p] = lsum * scale;
+}
+
+// Σ pixel_loss in double, in a fixed order (per-CTA partial sums, then one CTA).
+__global__ void __launch_bounds__(256) loss_sum_kernel(const float* __restrict__ pixel_loss, uint32_t n,
+                                                       double* __restrict__ partial, uint32_t per_block) {
+  __shared__ double s[8];
+  const uint32_t begin = blockIdx.x * per_block, end = min(n, begin + per_block);
+  double acc = 0.0;
+  for (uint32_t i = begin + threadIdx.x; i < end; i += 256) acc += (double)pixel_loss[i];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < 8; k++) t += s[k];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void loss_total_kernel(const double* __restrict__ partial, uint32_t blocks, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0;
+    for (uint32_t k = 0; k < blocks; k++) t += partial[k];
+    out[0] = t + (double)LAMBDA;
+  }
+}
+
+Window window_weights() {
+  double raw[6], total;
+  for (int k = 0; k < 6; k++) raw[k] = std::exp(-(double)(k * k) / (2 * 1.5 * 1.5));
+  total = raw[0] + 2 * (raw[1] + raw[2] + raw[3] + raw[4] + raw[5]);
+  Window win;
+  for (int k = 0; k < 6; k++) win.w[k] = (float)(raw[k] / total);
+  return win;
+}
+
+}  // namespace
+
+dg_status loss_launch(dg_training_loss* l, dg_buffer* rendered) {
+  dg_context* ctx = l->ctx;
+  const Window win = window_weights();
+  dim3 grid(ceil_div(l->width, LT), ceil_div(l->height, LT));
+  ssim_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(l->target_slot),
+                                             (int)l->width, (int)l->height, win, typed<float>(l->partials), 0,
+                                             nullptr);
+  ctx->launches++;
+  DG_LAUNCHED("ssim_kernel");
+  gradient_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(l->target_slot),
+                                                 (int)l->width, (int)l->height, win, typed<float>(l->partials),
+                                                 typed<float4>(l->pixel_grads), typed<float>(l->pixel_loss));
+  ctx->launches++;
+  DG_LAUNCHED("gradient_kernel");
+  return DG_OK;
+}
+
+dg_status loss_sum_launch(dg_training_loss* l) {
+  dg_context* ctx = l->ctx;
+  const uint32_t n = l->width * l->height;
+  const uint32_t per_block = 4096;
+  const uint32_t blocks = std::max(1u, ceil_div(n, per_block));
+  loss_sum_kernel<<<blocks, 256, 0, ctx->stream>>>(typed<float>(l->pixel_loss), n, typed<double>(l->sum_scratch),
+                                                   per_block);
+  loss_total_kernel<<<1, 32, 0, ctx->stream>>>(typed<double>(l->sum_scratch), blocks,
+                                                typed<double>(l->sum_scratch) + l->sum_blocks);
+  ctx->launches += 2;
+  DG_LAUNCHED("loss_sum");
+  return DG_OK;
+}
+
+dg_status metrics_launch(dg_context* ctx, dg_buffer* rendered, dg_buffer* target_slot, uint32_t width, uint32_t height,
+                         double* sums_device) {
+  const Window win = window_weights();
+  dim3 grid(ceil_div(width, LT), ceil_div(height, LT));
+  ssim_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(target_slot),
+                                             (int)width, (int)height, win, nullptr, 1, sums_device);
+  ctx->launches++;
+  DG_LAUNCHED("ssim_kernel(metrics)");
+  return DG_OK;
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+extern "C" {
+
+dg_status dg_training_loss_create(dg_context* ctx, uint32_t width, uint32_t height, dg_training_loss** out) {
+  DG_REQUIRE(ctx && out, "NULL argument");
+  DG_REQUIRE(width > 0 && height > 0, "empty image");
+  auto* l = new dg_training_loss();
+  l->ctx = ctx;
+  l->width = width;
+  l->height = height;
+  const size_t pixels = (size_t)width * height;
+  l->sum_blocks = std::max(1u, ceil_div(pixels, 4096));
+  dg_status st = alloc_buffer(ctx, pixels * 16, &l->pixel_grads);
+  if (st == DG_OK) st = alloc_buffer(ctx, pixels * 4, &l->pixel_loss);
+  if (st == DG_OK) st = alloc_buffer(ctx, pixels * 12 * 4, &l->partials);
+  if (st == DG_OK) st = alloc_buffer(ctx, 8, &l->target_slot);
+  if (st == DG_OK) st = alloc_buffer(ctx, (l->sum_blocks + 1) * 8, &l->sum_scratch);
+  if (st != DG_OK) {
+    dg_training_loss_destroy(l);
+    return st;
+  }
+  *out = l;
+  return DG_OK;
+}
+
+dg_status dg_training_loss_encode(dg_training_loss* l, dg_buffer* rendered, dg_buffer* target) {
+  DG_REQUIRE(l && rendered && target, "NULL argument");
+  const uint64_t pixels = (uint64_t)l->width * l->height;
+  DG_REQUIRE(rendered->bytes >= pixels * 16, "rendered buffer smaller than the image");
+  DG_REQUIRE(target->bytes >= pixels * 4, "target smaller than the image");
+  const void* ptr = target->ptr;
+  DG_TRY(write_async(l->ctx, l->target_slot->ptr, &ptr, sizeof(ptr)));
+  return loss_launch(l, rendered);
+}
+
+dg_buffer* dg_training_loss_pixel_grads(dg_training_loss* l) { return l ? l->pixel_grads : nullptr; }
+dg_buffer* dg_training_loss_pixel_loss(dg_training_loss* l) { return l ? l->pixel_loss : nullptr; }
+
+dg_status dg_training_loss_read(dg_training_loss* l, double* out) {
+  DG_REQUIRE(l && out, "NULL argument");
+  const size_t pixels = (size_t)l->width * l->height;
+  std::vector<float> shares(pixels);
+  DG_CUDA(cudaMemcpyAsync(shares.data(), l->pixel_loss->ptr, pixels * 4, cudaMemcpyDeviceToHost, l->ctx->stream));
+  DG_CUDA(cudaStreamSynchronize(l->ctx->stream));
+  double sum = 0;
+  for (float s : shares) sum += s;
+  *out = sum + (double)LAMBDA;
+  return DG_OK;
+}
+
+dg_status dg_training_loss_destroy(dg_training_loss* l) {
+  if (!l) return DG_OK;
+  for (dg_buffer* b : {l->pixel_grads, l->pixel_loss, l->partials, l->target_slot, l->sum_scratch}) free_buffer(b);
+  delete l;
+  return DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1099 @@
+// The renderer: preprocess (src/shaders/preprocess.wgsl), the tile stage
+// (src/shaders/tiles.wgsl), the forward blend (src/shaders/rasterize.wgsl) and
+// both backward passes (src/shaders/rasterizeBackward.wgsl,
+// src/shaders/preprocessBackward.wgsl), behind the TileRasterizer and
+// GaussianRenderer objects of src/tileRasterizer.ts and src/gaussianRenderer.ts.
+//
+// Compiled with --fmad=false (see dg_render_kernels.cuh).
+#include "dg_render.cuh"
+#include "dg_render_kernels.cuh"
+
+#include <algorithm>
+
+namespace dg {
+namespace {
+
+constexpr int PRE_THREADS = 128;
+constexpr int DUP_THREADS = 256;
+constexpr int RANGE_THREADS = 256;
+constexpr int BLEND_BATCH = 256;
+constexpr int BWD_BATCH = 256;
+
+__device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
+  const float* s = reinterpret_cast<const float*>(src);
+  float* d = reinterpret_cast<float*>(&dst);
+  for (int k = threadIdx.x; k < 36; k += blockDim.x) d[k] = s[k];
+}
+
+// ------------------------------------------------------------------ preprocess
+// One thread per Gaussian: src/shaders/preprocess.wgsl:21-88. The CTA's SH
+// coefficients are staged through shared memory with coalesced loads (45 floats
+// per Gaussian; the odd stride makes the per-thread reads conflict-free). When
+// tile_counts is given, the tiles each splat touches are written too
+// (src/shaders/tiles.wgsl:24-35, fused).
+__global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* __restrict__ camera,
+                                                                 const float* __restrict__ gaussians,
+                                                                 const float* __restrict__ sh, uint32_t count,
+                                                                 const uint32_t* __restrict__ scene_params,
+                                                                 float* __restrict__ splats,
+                                                                 uint32_t* __restrict__ tile_counts) {
+  __shared__ Camera s_cam;
+  __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
+  load_camera(s_cam, camera);
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  const uint32_t block_start = blockIdx.x * PRE_THREADS;
+  const uint32_t here = min((uint32_t)PRE_THREADS, count - block_start);
+  if (basis_count > 0) {
+    const float* src = sh + (size_t)block_start * SH_REST_FLOATS;
+    const uint32_t floats = here * SH_REST_FLOATS;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      const uint32_t vecs = floats / 4;
+      for (uint32_t k = threadIdx.x; k < vecs; k += PRE_THREADS)
+        reinterpret_cast<float4*>(s_sh)[k] = reinterpret_cast<const float4*>(src)[k];
+      for (uint32_t k = vecs * 4 + threadIdx.x; k < floats; k += PRE_THREADS) s_sh[k] = src[k];
+    } else {
+      for (uint32_t k = threadIdx.x; k < floats; k += PRE_THREADS) s_sh[k] = src[k];
+    }
+  }
+  __syncthreads();
+  const uint32_t i = block_start + threadIdx.x;
+  if (i >= count) return;
+  const Camera& cam = s_cam;
+  float g[16];
+  {
+    const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      float4 q = gp[k];
+      g[4 * k] = q.x; g[4 * k + 1] = q.y; g[4 * k + 2] = q.z; g[4 * k + 3] = q.w;
+    }
+  }
+  float4* out = reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT);
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto culled = [&]() {
+    out[0] = zero;
+    out[1] = zero;
+    out[2] = zero;
+    if (tile_counts) tile_counts[i] = 0;
+  };
+  if (-view_z(cam, g) <= 0.2f) return culled();
+  Projection p;
+  project(cam, g, p);
+  if (p.det <= 0.0f) return culled();
+  const float mid = 0.5f * (p.a + p.c);
+  const float lambda = mid + sqrtf(fmaxf(0.1f, mid * mid - p.det));
+  const float radius = ceilf(3.0f * sqrtf(lambda));
+  float clip[4];
+#pragma unroll
+  for (int row = 0; row < 4; row++) {
+    float v = cam.proj[0 * 4 + row] * p.t[0];
+    v = v + cam.proj[1 * 4 + row] * p.t[1];
+    v = v + cam.proj[2 * 4 + row] * p.t[2];
+    v = v + cam.proj[3 * 4 + row] * 1.0f;
+    clip[row] = v;
+  }
+  const float vpx = cam.viewport[0], vpy = cam.viewport[1];
+  const float mx = (clip[0] / clip[3] * 0.5f + 0.5f) * vpx;
+  const float my = (clip[1] / clip[3] * -0.5f + 0.5f) * vpy;
+  if (mx + radius < 0.0f || my + radius < 0.0f || mx - radius > vpx || my - radius > vpy) return culled();
+  float color[3] = {g[12], g[13], g[14]};
+  if (basis_count > 0) {
+    float campos[3], off[3], dir[3], basis[15];
+    camera_position(cam, campos);
+    off[0] = g[0] - campos[0];
+    off[1] = g[1] - campos[1];
+    off[2] = g[2] - campos[2];
+    normalize3(off, dir);
+    sh_basis(dir, basis);
+    const float* c = s_sh + threadIdx.x * SH_REST_FLOATS;
+    for (uint32_t k = 0; k < basis_count; k++) {
+      color[0] = color[0] + basis[k] * c[k * 3 + 0];
+      color[1] = color[1] + basis[k] * c[k * 3 + 1];
+      color[2] = color[2] + basis[k] * c[k * 3 + 2];
+    }
+  }
+  out[0] = make_float4(mx, my, p.depth, radius);
+  out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, 0.0f);
+  out[2] = make_float4(fmaxf(color[0], 0.0f), fmaxf(color[1], 0.0f), fmaxf(color[2], 0.0f), g[3]);
+  if (tile_counts) {
+    uint4 rect = tile_rect(mx, my, radius, tile_grid(cam));
+    tile_counts[i] = (rect.z - rect.x) * (rect.w - rect.y);
+  }
+}
+
+// src/shaders/tiles.wgsl:24-35 (for splats the renderer did not preprocess).
+__global__ void count_tiles_kernel(const Camera* __restrict__ camera, const float* __restrict__ splats, uint32_t count,
+                                   uint32_t* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const Camera& cam = *camera;
+  const float4 s = reinterpret_cast<const float4*>(splats + (size_t)i * FLOATS_PER_SPLAT)[0];
+  uint32_t touched = 0;
+  if (s.w > 0.0f) {
+    uint4 rect = tile_rect(s.x, s.y, s.w, tile_grid(cam));
+    touched = (rect.z - rect.x) * (rect.w - rect.y);
+  }
+  out[i] = touched;
+}
+
+// src/shaders/tiles.wgsl:37-60. Each warp writes the pairs of its 32 splats
+// together: those occupy one contiguous run of slots (the scan put them there),
+// so every lane writes the next slot of the run and the stores coalesce. A pair
+// is (key = tile << 32 | depth bits, value = splat index), dropped past capacity.
+__global__ void __launch_bounds__(DUP_THREADS) duplicate_kernel(const Camera* __restrict__ camera,
+                                                                const float* __restrict__ splats,
+                                                                const uint32_t* __restrict__ offsets, uint32_t count,
+                                                                uint32_t capacity, uint64_t* __restrict__ keys,
+                                                                uint32_t* __restrict__ values) {
+  __shared__ uint32_t s_excl[DUP_THREADS];
+  __shared__ uint32_t s_x0[DUP_THREADS];
+  __shared__ uint32_t s_y0[DUP_THREADS];
+  __shared__ uint32_t s_w[DUP_THREADS];
+  __shared__ uint32_t s_depth[DUP_THREADS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t i = blockIdx.x * DUP_THREADS + threadIdx.x;
+  const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
+  if (first >= count) return;  // warp-uniform
+  const Camera& cam = *camera;
+  const uint2 tiles = tile_grid(cam);
+  uint32_t n = 0;
+  uint4 rect = make_uint4(0, 0, 0, 0);
+  uint32_t depth_bits = 0;
+  if (i < count) {
+    const float4 s = reinterpret_cast<const float4*>(splats + (size_t)i * FLOATS_PER_SPLAT)[0];
+    if (s.w != 0.0f) {
+      rect = tile_rect(s.x, s.y, s.w, tiles);
+      n = (rect.z - rect.x) * (rect.w - rect.y);
+      depth_bits = __float_as_uint(s.z);
+    }
+  }
+  uint32_t incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  const uint32_t slot0 = offsets[first];
+  uint32_t* excl = s_excl + warp * 32;
+  excl[lane] = incl - n;
+  s_x0[threadIdx.x] = rect.x;
+  s_y0[threadIdx.x] = rect.y;
+  s_w[threadIdx.x] = rect.z - rect.x;
+  s_depth[threadIdx.x] = depth_bits;
+  __syncwarp();
+  for (uint32_t k = lane; k < total; k += 32) {
+    // The last lane whose run starts at or before k owns pair k.
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+      if (excl[lo + step] <= k) lo += step;
+    const int src = warp * 32 + lo;
+    const uint32_t local = k - excl[lo];
+    const uint32_t w = s_w[src];
+    const uint32_t y = s_y0[src] + local / w;
+    const uint32_t x = s_x0[src] + local % w;
+    const uint32_t slot = slot0 + k;
+    if (slot < capacity) {
+      keys[slot] = ((uint64_t)(y * tiles.x + x) << 32) | s_depth[src];
+      values[slot] = first + lo;
+    }
+  }
+}
+
+// src/shaders/tiles.wgsl:65-84
+__global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32_t* __restrict__ key_words,
+                                                                    const uint32_t* __restrict__ pair_total,
+                                                                    uint32_t capacity, uint2* __restrict__ ranges) {
+  const uint32_t n = min(pair_total[0], capacity);
+  const uint32_t i = blockIdx.x * RANGE_THREADS + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t tile = key_words[2 * (size_t)i + 1];
+  if (i == 0) {
+    ranges[tile].x = 0;
+  } else {
+    const uint32_t prev = key_words[2 * (size_t)i - 1];
+    if (tile != prev) {
+      ranges[prev].y = i;
+      ranges[tile].x = i;
+    }
+  }
+  if (i == n - 1) ranges[tile].y = n;
+}
+
+__device__ __forceinline__ unsigned char to_unorm8(float v) {
+  return (unsigned char)__float2uint_rn(clampf(v, 0.0f, 1.0f) * 255.0f);
+}
+
+// src/shaders/rasterize.wgsl:32-100: one CTA per 16x16 tile, one thread per pixel.
+// The tile's splats are staged 256 at a time through shared memory; a pixel stops
+// before the splat that would take its transmittance below 1e-4, and the CTA stops
+// loading once every pixel has stopped.
+__global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict__ camera,
+                                                        const float4* __restrict__ raster_params,
+                                                        const float* __restrict__ splats,
+                                                        const uint32_t* __restrict__ pair_splats,
+                                                        const uint2* __restrict__ ranges, uchar4* __restrict__ target,
+                                                        float4* __restrict__ pixel_color,
+                                                        uint32_t* __restrict__ pixel_last) {
+  __shared__ float2 s_mean[BLEND_BATCH];
+  __shared__ float4 s_conic[BLEND_BATCH];  // a, b, c, opacity
+  __shared__ float4 s_color[BLEND_BATCH];
+  const uint32_t tid = threadIdx.x;
+  const float vpx = camera->viewport[0], vpy = camera->viewport[1];
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
+  const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
+  const uint32_t px = blockIdx.x * TILE + (tid % TILE), py = blockIdx.y * TILE + (tid / TILE);
+  const bool inside = (float)px < vpx && (float)py < vpy;
+  const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+  const uint2 run = ranges[tile];
+  float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
+  bool done = !inside;
+  uint32_t visited = 0, last = 0;
+  for (uint32_t start = run.x; start < run.y; start += BLEND_BATCH) {
+    if (__syncthreads_count(done) == BLEND_BATCH) break;
+    const uint32_t k = start + tid;
+    if (k < run.y) {
+      const float4* s = reinterpret_cast<const float4*>(splats + (size_t)pair_splats[k] * FLOATS_PER_SPLAT);
+      const float4 s0 = s[0], s1 = s[1], s2 = s[2];
+      s_mean[tid] = make_float2(s0.x, s0.y);
+      s_conic[tid] = make_float4(s1.x, s1.y, s1.z, s2.w);
+      s_color[tid] = s2;
+    }
+    __syncthreads();
+    const uint32_t batch = min((uint32_t)BLEND_BATCH, run.y - start);
+    for (uint32_t j = 0; j < batch && !done; j++) {
+      visited++;
+      const float2 m = s_mean[j];
+      const float4 con = s_conic[j];
+      const float dx = cx - m.x, dy = cy - m.y;
+      const float power = -0.5f * (con.x * dx * dx + con.z * dy * dy) - con.y * dx * dy;
+      if (power > 0.0f) continue;
+      const float alpha = fminf(0.99f, con.w * exp_blend(power));
+      if (alpha < 1.0f / 255.0f) continue;
+      const float remaining = T * (1.0f - alpha);
+      if (remaining < 0.0001f) {
+        done = true;
+        continue;
+      }
+      const float4 c = s_color[j];
+      r = r + c.x * alpha * T;
+      g = g + c.y * alpha * T;
+      b = b + c.z * alpha * T;
+      T = remaining;
+      last = visited;
+    }
+  }
+  if (inside) {
+    const float4 bg = raster_params[0];
+    const float fr = r + T * bg.x, fg = g + T * bg.y, fb = b + T * bg.z;
+    const uint32_t p = py * (uint32_t)vpx + px;
+    pixel_color[p] = make_float4(fr, fg, fb, T);
+    pixel_last[p] = last;
+    if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
+  }
+}
+
+// Sums 16 values over the warp. Afterwards lanes 2s and 2s+1 both hold the total
+// of value s: each halving step swaps half of the values with the partner lane,
+// so 8 + 4 + 2 + 1 + 1 shuffles move everything instead of 5 per value.
+__device__ __forceinline__ float warp_transpose_reduce16(float v[16], int lane) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const bool upper = lane & 16;
+    float send = upper ? v[k] : v[k + 8];
+    float keep = upper ? v[k + 8] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const bool upper = lane & 8;
+    float send = upper ? v[k] : v[k + 4];
+    float keep = upper ? v[k + 4] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const bool upper = lane & 4;
+    float send = upper ? v[k] : v[k + 2];
+    float keep = upper ? v[k + 2] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    const bool upper = lane & 2;
+    float send = upper ? v[0] : v[1];
+    float keep = upper ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+// src/shaders/rasterizeBackward.wgsl:50-163. Each pixel walks its tile's list back
+// to front from its last blended splat, recovering the transmittance in front of
+// each splat by dividing the final one by (1 - alpha). A splat's 9 gradient shares
+// are summed over each warp's 32 pixels with shuffles, the 8 warps' sums meet in
+// shared memory, and each batch's per-splat totals go to global memory with one
+// atomic add per nonzero value. Splats past the tile's largest `last` cannot
+// contribute and are skipped.
+__global__ void __launch_bounds__(256) rasterize_backward_kernel(
+    const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
+    const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const float4* __restrict__ pixel_color,
+    const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads) {
+  __shared__ float2 s_mean[BWD_BATCH];
+  __shared__ float4 s_conic[BWD_BATCH];
+  __shared__ float4 s_color[BWD_BATCH];
+  __shared__ uint32_t s_index[BWD_BATCH];
+  __shared__ float s_acc[BWD_BATCH * SPLAT_GRADS];
+  __shared__ uint32_t s_max_last;
+  const uint32_t tid = threadIdx.x;
+  const int lane = tid & 31;
+  const float vpx = camera->viewport[0], vpy = camera->viewport[1];
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
+  const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
+  const uint32_t px = blockIdx.x * TILE + (tid % TILE), py = blockIdx.y * TILE + (tid / TILE);
+  const bool inside = (float)px < vpx && (float)py < vpy;
+  const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+  const uint2 run = ranges[tile];
+  float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
+  uint32_t last = 0;
+  if (inside) {
+    const uint32_t p = py * (uint32_t)vpx + px;
+    Tf = pixel_color[p].w;
+    last = pixel_last[p];
+    const float4 pg = pixel_grads[p];
+    pgx = pg.x;
+    pgy = pg.y;
+    pgz = pg.z;
+  }
+  if (tid == 0) s_max_last = 0;
+  for (uint32_t k = tid; k < BWD_BATCH * SPLAT_GRADS; k += 256) s_acc[k] = 0.0f;
+  __syncthreads();
+  if (last) atomicMax(&s_max_last, last);
+  __syncthreads();
+  const float4 bg = raster_params[0];
+  float bg_grad = bg.x * pgx;
+  bg_grad = bg_grad + bg.y * pgy;
+  bg_grad = bg_grad + bg.z * pgz;
+  float T = Tf;
+  float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
+  float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
+  const uint32_t end = run.x + s_max_last;
+  for (uint32_t batch_end = end; batch_end > run.x;) {
+    const uint32_t batch_start = batch_end - run.x > BWD_BATCH ? batch_end - BWD_BATCH : run.x;
+    const uint32_t n = batch_end - batch_start;
+    if (tid < n) {
+      const uint32_t index = pair_splats[batch_start + tid];
+      const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
+      const float4 s0 = s[0], s1 = s[1], s2 = s[2];
+      s_mean[tid] = make_float2(s0.x, s0.y);
+      s_conic[tid] = make_float4(s1.x, s1.y, s1.z, s2.w);
+      s_color[tid] = s2;
+      s_index[tid] = index;
+    }
+    __syncthreads();
+    for (uint32_t slot = n; slot > 0; slot--) {
+      const uint32_t j = slot - 1;
+      float v[16];
+#pragma unroll
+      for (int q = 0; q < 16; q++) v[q] = 0.0f;
+      bool contributes = false;
+      if (inside && batch_start + j - run.x < last) {
+        const float2 m = s_mean[j];
+        const float4 con = s_conic[j];
+        const float dx = cx - m.x, dy = cy - m.y;
+        const float power = -0.5f * (con.x * dx * dx + con.z * dy * dy) - con.y * dx * dy;
+        if (power <= 0.0f) {
+          const float G = exp_blend(power);
+          const float alpha = fminf(0.99f, con.w * G);
+          if (alpha >= 1.0f / 255.0f) {
+            contributes = true;
+            const float4 c = s_color[j];
+            T = T / (1.0f - alpha);
+            bhx = na * ncx + (1.0f - na) * bhx;
+            bhy = na * ncy + (1.0f - na) * bhy;
+            bhz = na * ncz + (1.0f - na) * bhz;
+            na = alpha;
+            ncx = c.x;
+            ncy = c.y;
+            ncz = c.z;
+            float dotv = (c.x - bhx) * pgx;
+            dotv = dotv + (c.y - bhy) * pgy;
+            dotv = dotv + (c.z - bhz) * pgz;
+            const float alpha_grad = T * dotv - Tf / (1.0f - alpha) * bg_grad;
+            const float power_grad = alpha_grad * con.w * G;
+            v[0] = power_grad * (con.x * dx + con.y * dy);
+            v[1] = power_grad * (con.y * dx + con.z * dy);
+            v[2] = power_grad * (-0.5f * dx * dx);
+            v[3] = power_grad * (-dx * dy);
+            v[4] = power_grad * (-0.5f * dy * dy);
+            v[5] = alpha_grad * G;
+            v[6] = alpha * T * pgx;
+            v[7] = alpha * T * pgy;
+            v[8] = alpha * T * pgz;
+          }
+        }
+      }
+      if (__any_sync(0xffffffffu, contributes)) {
+        const float total = warp_transpose_reduce16(v, lane);
+        const int which = lane >> 1;
+        if ((lane & 1) == 0 && which < (int)SPLAT_GRADS && total != 0.0f)
+          atomicAdd(&s_acc[j * SPLAT_GRADS + which], total);
+      }
+    }
+    __syncthreads();
+    for (uint32_t k = tid; k < n * SPLAT_GRADS; k += 256) {
+      const float total = s_acc[k];
+      if (total != 0.0f) {
+        atomicAdd(&splat_grads[(size_t)s_index[k / SPLAT_GRADS] * SPLAT_GRADS + k % SPLAT_GRADS], total);
+        s_acc[k] = 0.0f;
+      }
+    }
+    __syncthreads();
+    batch_end = batch_start;
+  }
+}
+
+// src/shaders/preprocessBackward.wgsl:28-181: one thread per Gaussian. Writes the
+// 16-float Gaussian gradient (slots 7 and 15 zero) and the 45 SH gradients.
+__global__ void __launch_bounds__(128) preprocess_backward_kernel(
+    const Camera* __restrict__ camera, const float* __restrict__ gaussians, const float* __restrict__ sh,
+    uint32_t count, const uint32_t* __restrict__ scene_params, const float* __restrict__ splats,
+    const float* __restrict__ splat_grads, float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
+  __shared__ Camera s_cam;
+  load_camera(s_cam, camera);
+  __syncthreads();
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const Camera& cam = s_cam;
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  float* gg = gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN;
+  float* sg = sh_grads + (size_t)i * SH_REST_FLOATS;
+  float out[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) out[k] = 0.0f;
+  bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
+  if (!visible) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) reinterpret_cast<float4*>(gg)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint32_t k = 0; k < SH_REST_FLOATS; k++) sg[k] = 0.0f;
+    return;
+  }
+  float grad[9];
+#pragma unroll
+  for (int k = 0; k < 9; k++) grad[k] = splat_grads[(size_t)i * SPLAT_GRADS + k];
+  float g[16];
+  {
+    const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      float4 q = gp[k];
+      g[4 * k] = q.x; g[4 * k + 1] = q.y; g[4 * k + 2] = q.z; g[4 * k + 3] = q.w;
+    }
+  }
+  Projection p;
+  project(cam, g, p);
+  const float depth = p.depth;
+  const float ratio0 = p.t[0] / depth, ratio1 = p.t[1] / depth;
+  const float free0 = fabsf(ratio0) > p.limit[0] ? 0.0f : 1.0f;
+  const float free1 = fabsf(ratio1) > p.limit[1] ? 0.0f : 1.0f;
+  const float depth2 = depth * depth, depth3 = depth2 * depth;
+  const float a = p.a, b = p.b, c = p.c, det = p.det;
+  // 1. conic -> 2D covariance
+  const float det2 = det * det;
+  const float a_grad = (-c * c * grad[2] + b * c * grad[3] - b * b * grad[4]) / det2;
+  const float b_grad = (2.0f * b * c * grad[2] - (det + 2.0f * b * b) * grad[3] + 2.0f * a * b * grad[4]) / det2;
+  const float c_grad = (-b * b * grad[2] + a * b * grad[3] - a * a * grad[4]) / det2;
+  const float G2[2][2] = {{a_grad, 0.5f * b_grad}, {0.5f * b_grad, c_grad}};
+  // 2. Σ' = T Σ Tᵀ with T = J W
+  float Gjw[3][2];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = G2[0][row] * p.jw[col][0];
+      v = v + G2[1][row] * p.jw[col][1];
+      Gjw[col][row] = v;
+    }
+  float cov3d_grad[3][3];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      float v = p.jw[row][0] * Gjw[col][0];
+      v = v + p.jw[row][1] * Gjw[col][1];
+      cov3d_grad[col][row] = v;
+    }
+  float t3[3][2];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = (2.0f * Gjw[0][row]) * p.cov3d[col][0];
+      v = v + (2.0f * Gjw[1][row]) * p.cov3d[col][1];
+      v = v + (2.0f * Gjw[2][row]) * p.cov3d[col][2];
+      t3[col][row] = v;
+    }
+  float jg[3][2];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = t3[0][row] * p.w[0][col];
+      v = v + t3[1][row] * p.w[1][col];
+      v = v + t3[2][row] * p.w[2][col];
+      jg[col][row] = v;
+    }
+  // 3. J moves with t
+  float tg[3];
+  tg[0] = jg[2][0] * free0 * p.focal[0] / depth2;
+  tg[1] = jg[2][1] * free1 * -p.focal[1] / depth2;
+  tg[2] = 0.0f;
+  const float depth_grad = jg[0][0] * (-p.focal[0] / depth2) + jg[1][1] * (p.focal[1] / depth2) +
+                           jg[2][0] * (-(1.0f + free0) * p.focal[0] * p.tx / depth3) +
+                           jg[2][1] * ((1.0f + free1) * p.focal[1] * p.ty / depth3);
+  tg[2] = tg[2] - depth_grad;
+  // 4. the 2D center
+  float clip[4];
+#pragma unroll
+  for (int row = 0; row < 4; row++) {
+    float v = cam.proj[0 * 4 + row] * p.t[0];
+    v = v + cam.proj[1 * 4 + row] * p.t[1];
+    v = v + cam.proj[2 * 4 + row] * p.t[2];
+    v = v + cam.proj[3 * 4 + row] * 1.0f;
+    clip[row] = v;
+  }
+  const float ng0 = grad[0] * 0.5f * cam.viewport[0], ng1 = grad[1] * -0.5f * cam.viewport[1];
+  float ndc_dot = ng0 * clip[0];
+  ndc_dot = ndc_dot + ng1 * clip[1];
+  const float clip_grad[4] = {ng0 / clip[3], ng1 / clip[3], 0.0f, -ndc_dot / (clip[3] * clip[3])};
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+    float v = cam.proj[col * 4 + 0] * clip_grad[0];
+    v = v + cam.proj[col * 4 + 1] * clip_grad[1];
+    v = v + cam.proj[col * 4 + 2] * clip_grad[2];
+    v = v + cam.proj[col * 4 + 3] * clip_grad[3];
+    tg[col] = tg[col] + v;
+  }
+  // 5. colour
+  float campos[3], off[3], dir[3], basis[15];
+  camera_position(cam, campos);
+  off[0] = g[0] - campos[0];
+  off[1] = g[1] - campos[1];
+  off[2] = g[2] - campos[2];
+  const float dist = normalize3(off, dir);
+  sh_basis(dir, basis);
+  const float* coef = sh + (size_t)i * SH_REST_FLOATS;
+  float raw_color[3] = {g[12], g[13], g[14]};
+  for (uint32_t k = 0; k < basis_count; k++)
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) raw_color[ch] = raw_color[ch] + basis[k] * coef[k * 3 + ch];
+  float raw_grad[3];
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) raw_grad[ch] = raw_color[ch] < 0.0f ? 0.0f : grad[6 + ch];
+  float dgrad[3] = {0.0f, 0.0f, 0.0f};
+  {
+    float bgrad[15][3];
+    sh_basis_gradient(dir, bgrad);
+    for (uint32_t k = 0; k < SH_REST_FLOATS / 3; k++) {
+      if (k < basis_count) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = basis[k] * raw_grad[ch];
+        float d = coef[k * 3] * raw_grad[0];
+        d = d + coef[k * 3 + 1] * raw_grad[1];
+        d = d + coef[k * 3 + 2] * raw_grad[2];
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) dgrad[ax] = dgrad[ax] + bgrad[k][ax] * d;
+      } else {
+#pragma unroll
+        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = 0.0f;
+      }
+    }
+  }
+  float dd = dir[0] * dgrad[0];
+  dd = dd + dir[1] * dgrad[1];
+  dd = dd + dir[2] * dgrad[2];
+  // 6. position
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+    float v = p.w[col][0] * tg[0];
+    v = v + p.w[col][1] * tg[1];
+    v = v + p.w[col][2] * tg[2];
+    out[col] = v + (dgrad[col] - dir[col] * dd) / dist;
+  }
+  // 7. scale and rotation
+  float mg[3][3];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      float v = 2.0f * cov3d_grad[0][row] * p.m[col][0];
+      v = v + 2.0f * cov3d_grad[1][row] * p.m[col][1];
+      v = v + 2.0f * cov3d_grad[2][row] * p.m[col][2];
+      mg[col][row] = v;
+    }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float v = mg[k][0] * p.r[k][0];
+    v = v + mg[k][1] * p.r[k][1];
+    v = v + mg[k][2] * p.r[k][2];
+    out[4 + k] = v;
+  }
+  float rg[3][3];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) rg[col][row] = mg[col][row] * g[4 + col];
+  const float qw = p.q[0], qx = p.q[1], qy = p.q[2], qz = p.q[3];
+  const float g00 = rg[0][0], g01 = rg[1][0], g02 = rg[2][0];
+  const float g10 = rg[0][1], g11 = rg[1][1], g12 = rg[2][1];
+  const float g20 = rg[0][2], g21 = rg[1][2], g22 = rg[2][2];
+  float qg[4];
+  qg[0] = 2.0f * (-qz * g01 + qy * g02 + qz * g10 - qx * g12 - qy * g20 + qx * g21);
+  qg[1] = 2.0f * (qy * g01 + qz * g02 + qy * g10 - 2.0f * qx * g11 - qw * g12 + qz * g20 + qw * g21 - 2.0f * qx * g22);
+  qg[2] = 2.0f * (-2.0f * qy * g00 + qx * g01 + qw * g02 + qx * g10 + qz * g12 - qw * g20 + qz * g21 - 2.0f * qy * g22);
+  qg[3] = 2.0f * (-2.0f * qz * g00 - qw * g01 + qx * g02 + qw * g10 - 2.0f * qz * g11 + qy * g12 + qx * g20 + qy * g21);
+  float qd = p.q[0] * qg[0];
+  qd = qd + p.q[1] * qg[1];
+  qd = qd + p.q[2] * qg[2];
+  qd = qd + p.q[3] * qg[3];
+  out[3] = grad[5];
+#pragma unroll
+  for (int k = 0; k < 4; k++) out[8 + k] = (qg[k] - p.q[k] * qd) / p.qlen;
+  out[12] = raw_grad[0];
+  out[13] = raw_grad[1];
+  out[14] = raw_grad[2];
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    reinterpret_cast<float4*>(gg)[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+}
+
+// The empty-scene render pass: clear the target to the background (src/gaussianRenderer.ts:178-184).
+__global__ void clear_target_kernel(uchar4* __restrict__ target, uint32_t pixels, float r, float g, float b) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < pixels) target[i] = make_uchar4(to_unorm8(r), to_unorm8(g), to_unorm8(b), 255);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ TileRasterizer
+
+static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
+  dg_context* ctx = tr->ctx;
+  free_buffer(tr->keys);
+  free_buffer(tr->values);
+  free_buffer(tr->keys_alt);
+  free_buffer(tr->values_alt);
+  free_buffer(tr->sort_scratch);
+  tr->keys = tr->values = tr->keys_alt = tr->values_alt = tr->sort_scratch = nullptr;
+  tr->plan = sort_plan(capacity, TILE_INDEX_BITS);
+  tr->pair_capacity = capacity;
+  DG_TRY(alloc_buffer(ctx, (size_t)capacity * 8, &tr->keys));
+  DG_TRY(alloc_buffer(ctx, (size_t)capacity * 4, &tr->values));
+  DG_TRY(alloc_buffer(ctx, (size_t)capacity * 8, &tr->keys_alt));
+  DG_TRY(alloc_buffer(ctx, (size_t)capacity * 4, &tr->values_alt));
+  DG_TRY(alloc_buffer(ctx, sort_scratch_bytes(tr->plan), &tr->sort_scratch));
+  return DG_OK;
+}
+
+dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity) { return make_pairs(tr, capacity); }
+
+dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
+                            uint32_t initial_pair_capacity, dg_tile_rasterizer** out) {
+  auto* tr = new dg_tile_rasterizer();
+  tr->ctx = ctx;
+  tr->camera = camera;
+  tr->splats = splats;
+  tr->count = count;
+  dg_status st = alloc_buffer(ctx, (size_t)std::max(count, 1u) * 4, &tr->tile_offsets);
+  if (st == DG_OK) st = alloc_buffer(ctx, 4, &tr->scan_total);
+  if (st == DG_OK) st = alloc_buffer(ctx, scan_scratch_bytes(std::max(count, 1u)), &tr->scan_scratch);
+  if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->raster_params);
+  if (st == DG_OK && cudaMallocHost(&tr->pinned_total, 4) != cudaSuccess) st = fail(DG_ERROR_OUT_OF_MEMORY, "pinned");
+  if (st == DG_OK && cudaEventCreateWithFlags(&tr->readback_event, cudaEventDisableTiming) != cudaSuccess)
+    st = fail(DG_ERROR_CUDA, "event");
+  uint32_t capacity = initial_pair_capacity ? initial_pair_capacity : std::max(1u << 16, count * 8u);
+  if (st == DG_OK) st = make_pairs(tr, capacity);
+  if (st != DG_OK) {
+    dg_tile_rasterizer_destroy(tr);
+    return st;
+  }
+  *out = tr;
+  return DG_OK;
+}
+
+dg_status rasterizer_prepare(dg_tile_rasterizer* tr, const float viewport[2], const float background[3]) {
+  const uint32_t tiles_x = ceil_div((uint32_t)viewport[0], TILE), tiles_y = ceil_div((uint32_t)viewport[1], TILE);
+  if ((uint64_t)tiles_x * tiles_y > (1u << TILE_INDEX_BITS))
+    return fail(DG_ERROR_INVALID_ARGUMENT, "A " + std::to_string((int)viewport[0]) + "x" +
+                                               std::to_string((int)viewport[1]) +
+                                               " viewport has more tiles than the sort can tell apart.");
+  tr->tiles_x = tiles_x;
+  tr->tiles_y = tiles_y;
+  tr->viewport[0] = viewport[0];
+  tr->viewport[1] = viewport[1];
+  const uint32_t tiles = tiles_x * tiles_y;
+  if (!tr->ranges || tr->ranges_tiles < tiles) {
+    free_buffer(tr->ranges);
+    tr->ranges = nullptr;
+    DG_TRY(alloc_buffer(tr->ctx, (size_t)std::max(tiles, 1u) * 8, &tr->ranges));
+    tr->ranges_tiles = tiles;
+  }
+  const uint32_t pixels = (uint32_t)viewport[0] * (uint32_t)viewport[1];
+  if (!tr->pixel_color || tr->pixel_count < pixels) {
+    free_buffer(tr->pixel_color);
+    free_buffer(tr->pixel_last);
+    tr->pixel_color = tr->pixel_last = nullptr;
+    DG_TRY(alloc_buffer(tr->ctx, (size_t)std::max(pixels, 1u) * 16, &tr->pixel_color));
+    DG_TRY(alloc_buffer(tr->ctx, (size_t)std::max(pixels, 1u) * 4, &tr->pixel_last));
+    tr->pixel_count = pixels;
+  }
+  const float params[4] = {background[0], background[1], background[2], 1.0f};
+  return write_async(tr->ctx, tr->raster_params->ptr, params, sizeof(params));
+}
+
+dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool counts_ready) {
+  dg_context* ctx = tr->ctx;
+  cudaStream_t st = ctx->stream;
+  const uint32_t count = tr->count;
+  const auto* cam = typed<const Camera>(tr->camera);
+  DG_CUDA(cudaMemsetAsync(tr->ranges->ptr, 0, (size_t)tr->tiles_x * tr->tiles_y * 8, st));
+  if (count > 0) {
+    if (!counts_ready) {
+      count_tiles_kernel<<<ceil_div(count, 256), 256, 0, st>>>(cam, typed<float>(tr->splats), count,
+                                                              typed<uint32_t>(tr->tile_offsets));
+      ctx->launches++;
+      DG_LAUNCHED("count_tiles");
+    }
+  }
+  DG_TRY(scan_launch(ctx, typed<uint32_t>(tr->tile_offsets), count, nullptr, typed<uint32_t>(tr->scan_total),
+                     tr->scan_scratch->ptr));
+  if (count > 0) {
+    duplicate_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
+        cam, typed<float>(tr->splats), typed<uint32_t>(tr->tile_offsets), count, tr->pair_capacity,
+        typed<uint64_t>(tr->keys), typed<uint32_t>(tr->values));
+    ctx->launches++;
+    DG_LAUNCHED("duplicate");
+  }
+  DG_TRY(sort_launch(ctx, tr->plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
+                     typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
+  find_ranges_kernel<<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0, st>>>(
+      typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total), tr->pair_capacity, typed<uint2>(tr->ranges));
+  ctx->launches++;
+  DG_LAUNCHED("find_ranges");
+  rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, st>>>(
+      cam, typed<float4>(tr->raster_params), typed<float>(tr->splats), typed<uint32_t>(tr->values),
+      typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
+      typed<uint32_t>(tr->pixel_last));
+  ctx->launches++;
+  DG_LAUNCHED("rasterize");
+  return DG_OK;
+}
+
+dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr) {
+  if (tr->readback_state != 0) return DG_OK;
+  DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, tr->ctx->stream));
+  DG_CUDA(cudaEventRecord(tr->readback_event, tr->ctx->stream));
+  tr->readback_state = 1;
+  return DG_OK;
+}
+
+dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads) {
+  dg_context* ctx = tr->ctx;
+  DG_CUDA(cudaMemsetAsync(splat_grads->ptr, 0, (size_t)tr->count * SPLAT_GRADS * 4, ctx->stream));
+  rasterize_backward_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
+      typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
+      typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
+      typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads));
+  ctx->launches++;
+  DG_LAUNCHED("rasterize_backward");
+  return DG_OK;
+}
+
+// ------------------------------------------------------------ GaussianRenderer
+
+static void destroy_scene(dg_renderer* r) {
+  free_buffer(r->gaussians);
+  free_buffer(r->splats);
+  free_buffer(r->sh);
+  free_buffer(r->scene_params);
+  free_buffer(r->grad_splats);
+  free_buffer(r->grad_gaussians);
+  free_buffer(r->grad_sh);
+  if (r->rasterizer) dg_tile_rasterizer_destroy(r->rasterizer);
+  r->gaussians = r->splats = r->sh = r->scene_params = nullptr;
+  r->grad_splats = r->grad_gaussians = r->grad_sh = nullptr;
+  r->rasterizer = nullptr;
+  r->has_scene = false;
+  r->count = 0;
+}
+
+static dg_status create_scene(dg_renderer* r, uint32_t count, dg_buffer* gaussians, dg_buffer* sh, uint32_t degree,
+                              uint32_t pair_capacity) {
+  r->has_scene = true;
+  r->count = count;
+  r->gaussians = gaussians;
+  r->sh = sh;
+  DG_TRY(alloc_buffer(r->ctx, 16, &r->scene_params));
+  const uint32_t params[4] = {degree, 0, 0, 0};
+  DG_TRY(write_async(r->ctx, r->scene_params->ptr, params, sizeof(params)));
+  DG_TRY(alloc_buffer(r->ctx, (size_t)count * FLOATS_PER_SPLAT * 4, &r->splats));
+  DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, &r->rasterizer));
+  return DG_OK;
+}
+
+dg_status renderer_write_camera(dg_renderer* r, const dg_camera* camera) {
+  Camera c{};
+  std::memcpy(c.view, camera->view, 64);
+  std::memcpy(c.proj, camera->proj, 64);
+  c.viewport[0] = camera->viewport[0];
+  c.viewport[1] = camera->viewport[1];
+  r->last_viewport[0] = camera->viewport[0];
+  r->last_viewport[1] = camera->viewport[1];
+  return write_async(r->ctx, r->camera->ptr, &c, sizeof(c));
+}
+
+dg_status renderer_prepare(dg_renderer* r, const dg_camera* camera, const float background[3]) {
+  DG_TRY(renderer_write_camera(r, camera));
+  if (!r->has_scene) return DG_OK;
+  return rasterizer_prepare(r->rasterizer, camera->viewport, background);
+}
+
+dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target) {
+  dg_context* ctx = r->ctx;
+  if (r->count > 0) {
+    preprocess_kernel<<<ceil_div(r->count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
+        typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
+        typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<uint32_t>(r->rasterizer->tile_offsets));
+    ctx->launches++;
+    DG_LAUNCHED("preprocess");
+  }
+  return rasterizer_launch(r->rasterizer, target, true);
+}
+
+dg_status renderer_ensure_gradients(dg_renderer* r) {
+  if (r->grad_splats) return DG_OK;
+  DG_TRY(alloc_buffer(r->ctx, (size_t)r->count * SPLAT_GRADS * 4, &r->grad_splats));
+  DG_TRY(alloc_buffer(r->ctx, (size_t)r->count * FLOATS_PER_GAUSSIAN * 4, &r->grad_gaussians));
+  DG_TRY(alloc_buffer(r->ctx, (size_t)r->count * SH_REST_FLOATS * 4, &r->grad_sh));
+  return DG_OK;
+}
+
+dg_status renderer_launch_backward(dg_renderer* r, dg_buffer* pixel_grads, bool write_gaussian_grads) {
+  DG_TRY(rasterizer_launch_backward(r->rasterizer, pixel_grads, r->grad_splats));
+  if (!write_gaussian_grads || r->count == 0) return DG_OK;
+  preprocess_backward_kernel<<<ceil_div(r->count, 128), 128, 0, r->ctx->stream>>>(
+      typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
+      typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats),
+      typed<float>(r->grad_gaussians), typed<float>(r->grad_sh));
+  r->ctx->launches++;
+  DG_LAUNCHED("preprocess_backward");
+  return DG_OK;
+}
+
+const Camera* renderer_camera(dg_renderer* r) { return typed<const Camera>(r->camera); }
+
+}  // namespace dg
+
+using namespace dg;
+
+extern "C" {
+
+dg_status dg_tile_rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
+                                    uint32_t initial_pair_capacity, dg_tile_rasterizer** out) {
+  DG_REQUIRE(ctx && camera && splats && out, "NULL argument");
+  DG_REQUIRE(camera->bytes >= sizeof(Camera), "camera buffer is smaller than the 144-byte Camera uniform");
+  DG_REQUIRE(splats->bytes >= (uint64_t)count * FLOATS_PER_SPLAT * 4, "splat buffer too small for count");
+  return rasterizer_create(ctx, camera, splats, count, initial_pair_capacity, out);
+}
+
+dg_status dg_tile_rasterizer_encode(dg_tile_rasterizer* tr, dg_buffer* target, const float viewport[2],
+                                    const float background[3]) {
+  DG_REQUIRE(tr && viewport && background, "NULL argument");
+  if (target)
+    DG_REQUIRE(target->bytes >= (uint64_t)(uint32_t)viewport[0] * (uint32_t)viewport[1] * 4,
+               "target is smaller than the viewport");
+  DG_TRY(rasterizer_prepare(tr, viewport, background));
+  DG_TRY(rasterizer_launch(tr, target, false));
+  return rasterizer_queue_readback(tr);
+}
+
+dg_status dg_tile_rasterizer_encode_backward(dg_tile_rasterizer* tr, const float viewport[2], dg_buffer* pixel_grads,
+                                             dg_buffer* splat_grads) {
+  DG_REQUIRE(tr && viewport && pixel_grads && splat_grads, "NULL argument");
+  if (!tr->pixel_color || !tr->ranges) return fail(DG_ERROR_STATE, "Encode a frame before its backward pass.");
+  DG_REQUIRE(splat_grads->bytes >= (uint64_t)tr->count * SPLAT_GRADS * 4, "splat gradient buffer too small");
+  DG_REQUIRE(pixel_grads->bytes >= (uint64_t)tr->pixel_count * 16, "pixel gradient buffer too small");
+  return rasterizer_launch_backward(tr, pixel_grads, splat_grads);
+}
+
+dg_status dg_tile_rasterizer_after_submit(dg_tile_rasterizer* tr, int32_t wait) {
+  DG_REQUIRE(tr, "NULL argument");
+  if (tr->readback_state != 1) return DG_OK;
+  if (!wait && cudaEventQuery(tr->readback_event) == cudaErrorNotReady) return DG_OK;
+  DG_CUDA(cudaEventSynchronize(tr->readback_event));
+  tr->last_pair_count = *tr->pinned_total;
+  tr->readback_state = 0;
+  if (tr->last_pair_count > tr->pair_capacity) {
+    double want = std::ceil(std::log2((double)tr->last_pair_count * 1.25));
+    DG_REQUIRE(want < 30, "the frame needs more pairs than the sort can hold");
+    DG_TRY(make_pairs(tr, 1u << (uint32_t)want));
+  }
+  return DG_OK;
+}
+
+uint32_t dg_tile_rasterizer_last_pair_count(const dg_tile_rasterizer* tr) { return tr ? tr->last_pair_count : 0; }
+uint32_t dg_tile_rasterizer_pair_capacity(const dg_tile_rasterizer* tr) { return tr ? tr->pair_capacity : 0; }
+dg_buffer* dg_tile_rasterizer_pair_splats(dg_tile_rasterizer* tr) { return tr ? tr->values : nullptr; }
+dg_buffer* dg_tile_rasterizer_ranges(dg_tile_rasterizer* tr) { return tr ? tr->ranges : nullptr; }
+dg_buffer* dg_tile_rasterizer_pair_keys(dg_tile_rasterizer* tr) { return tr ? tr->keys : nullptr; }
+dg_buffer* dg_tile_rasterizer_pixel_color(dg_tile_rasterizer* tr) { return tr ? tr->pixel_color : nullptr; }
+dg_buffer* dg_tile_rasterizer_pixel_last(dg_tile_rasterizer* tr) { return tr ? tr->pixel_last : nullptr; }
+dg_buffer* dg_tile_rasterizer_tile_offsets(dg_tile_rasterizer* tr) { return tr ? tr->tile_offsets : nullptr; }
+dg_buffer* dg_tile_rasterizer_pair_total(dg_tile_rasterizer* tr) { return tr ? tr->scan_total : nullptr; }
+
+dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
+  if (!tr) return DG_OK;
+  for (dg_buffer* b : {tr->tile_offsets, tr->scan_total, tr->scan_scratch, tr->raster_params, tr->keys, tr->values,
+                       tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last})
+    free_buffer(b);
+  if (tr->readback_event) {
+    cudaEventSynchronize(tr->readback_event);
+    cudaEventDestroy(tr->readback_event);
+  }
+  if (tr->pinned_total) cudaFreeHost(tr->pinned_total);
+  delete tr;
+  return DG_OK;
+}
+
+dg_status dg_renderer_create(dg_context* ctx, uint32_t initial_pair_capacity, dg_renderer** out) {
+  DG_REQUIRE(ctx && out, "NULL argument");
+  auto* r = new dg_renderer();
+  r->ctx = ctx;
+  r->initial_pair_capacity = initial_pair_capacity;
+  dg_status st = alloc_buffer(ctx, sizeof(Camera), &r->camera);
+  if (st != DG_OK) {
+    delete r;
+    return st;
+  }
+  *out = r;
+  return DG_OK;
+}
+
+dg_status dg_renderer_set_gaussians(dg_renderer* r, const float* data, uint32_t count, const float* sh_rest,
+                                    uint64_t sh_floats, uint32_t degree) {
+  DG_REQUIRE(r, "NULL argument");
+  if (count == 0) {
+    destroy_scene(r);
+    return DG_OK;
+  }
+  DG_REQUIRE(data, "NULL Gaussian data");
+  if (sh_rest && sh_floats != (uint64_t)count * SH_REST_FLOATS)
+    return fail(DG_ERROR_INVALID_ARGUMENT, "Expected " + std::to_string((uint64_t)count * SH_REST_FLOATS) +
+                                               " spherical-harmonic floats, got " + std::to_string(sh_floats) + ".");
+  DG_REQUIRE(degree <= 3, "SH degree is at most 3");
+  dg_buffer *g = nullptr, *s = nullptr;
+  DG_TRY(alloc_buffer(r->ctx, (size_t)count * FLOATS_PER_GAUSSIAN * 4, &g));
+  DG_TRY(write_async(r->ctx, g->ptr, data, (size_t)count * FLOATS_PER_GAUSSIAN * 4));
+  // Without SH the buffer is still sized for count Gaussians, so training can
+  // raise the degree later; its coefficients are zero.
+  DG_TRY(alloc_buffer(r->ctx, (size_t)count * SH_REST_FLOATS * 4, &s));
+  if (sh_rest) DG_TRY(write_async(r->ctx, s->ptr, sh_rest, (size_t)count * SH_REST_FLOATS * 4));
+  destroy_scene(r);
+  return create_scene(r, count, g, s, sh_rest ? degree : 0, r->initial_pair_capacity);
+}
+
+dg_status dg_renderer_adopt_gaussians(dg_renderer* r, uint32_t count, dg_buffer* gaussians, dg_buffer* sh,
+                                      uint32_t degree) {
+  DG_REQUIRE(r && gaussians && sh, "NULL argument");
+  DG_REQUIRE(gaussians->bytes >= (uint64_t)count * FLOATS_PER_GAUSSIAN * 4, "Gaussian buffer too small");
+  DG_REQUIRE(sh->bytes >= (uint64_t)count * SH_REST_FLOATS * 4, "SH buffer too small");
+  uint32_t capacity = r->rasterizer ? r->rasterizer->pair_capacity : r->initial_pair_capacity;
+  destroy_scene(r);
+  return create_scene(r, count, gaussians, sh, degree, capacity);
+}
+
+dg_status dg_renderer_set_sh_degree(dg_renderer* r, uint32_t degree) {
+  DG_REQUIRE(r, "NULL argument");
+  DG_REQUIRE(degree <= 3, "SH degree is at most 3");
+  if (!r->has_scene) return DG_OK;
+  const uint32_t params[4] = {degree, 0, 0, 0};
+  return write_async(r->ctx, r->scene_params->ptr, params, sizeof(params));
+}
+
+dg_status dg_renderer_encode(dg_renderer* r, dg_buffer* target, const dg_camera* camera, const float background[3]) {
+  DG_REQUIRE(r && camera && background, "NULL argument");
+  const uint32_t pixels = (uint32_t)camera->viewport[0] * (uint32_t)camera->viewport[1];
+  if (target) DG_REQUIRE(target->bytes >= (uint64_t)pixels * 4, "target is smaller than the viewport");
+  DG_TRY(renderer_prepare(r, camera, background));
+  if (!r->has_scene) {
+    if (target && pixels) {
+      clear_target_kernel<<<ceil_div(pixels, 256), 256, 0, r->ctx->stream>>>(typed<uchar4>(target), pixels,
+                                                                            background[0], background[1],
+                                                                            background[2]);
+      r->ctx->launches++;
+      DG_LAUNCHED("clear_target");
+    }
+    return DG_OK;
+  }
+  DG_TRY(renderer_launch_forward(r, target));
+  return rasterizer_queue_readback(r->rasterizer);
+}
+
+dg_status dg_renderer_encode_draw(dg_renderer* r, dg_buffer* target, dg_buffer* splats, uint32_t count,
+                                  const float viewport[2], const float background[3]) {
+  DG_REQUIRE(r && splats && viewport && background, "NULL argument");
+  dg_camera cam{};
+  for (int k = 0; k < 16; k++) cam.view[k] = cam.proj[k] = (k % 5 == 0) ? 1.0f : 0.0f;
+  cam.viewport[0] = viewport[0];
+  cam.viewport[1] = viewport[1];
+  DG_TRY(renderer_write_camera(r, &cam));
+  if (r->draw_rasterizer) dg_tile_rasterizer_destroy(r->draw_rasterizer);
+  r->draw_rasterizer = nullptr;
+  DG_TRY(dg_tile_rasterizer_create(r->ctx, r->camera, splats, count, r->initial_pair_capacity, &r->draw_rasterizer));
+  return dg_tile_rasterizer_encode(r->draw_rasterizer, target, viewport, background);
+}
+
+dg_status dg_renderer_encode_backward(dg_renderer* r, dg_buffer* pixel_grads) {
+  DG_REQUIRE(r && pixel_grads, "NULL argument");
+  if (!r->has_scene) return DG_OK;
+  if (!r->rasterizer->pixel_color || !r->rasterizer->ranges)
+    return fail(DG_ERROR_STATE, "Encode a frame before its backward pass.");
+  DG_REQUIRE(pixel_grads->bytes >= (uint64_t)r->rasterizer->pixel_count * 16, "pixel gradient buffer too small");
+  DG_TRY(renderer_ensure_gradients(r));
+  return renderer_launch_backward(r, pixel_grads, true);
+}
+
+dg_status dg_renderer_after_submit(dg_renderer* r, int32_t wait) {
+  DG_REQUIRE(r, "NULL argument");
+  if (!r->rasterizer) return DG_OK;
+  return dg_tile_rasterizer_after_submit(r->rasterizer, wait);
+}
+
+uint32_t dg_renderer_count(const dg_renderer* r) { return r ? r->count : 0; }
+dg_buffer* dg_renderer_splat_buffer(dg_renderer* r) { return r ? r->splats : nullptr; }
+dg_buffer* dg_renderer_gaussian_buffer(dg_renderer* r) { return r ? r->gaussians : nullptr; }
+dg_buffer* dg_renderer_sh_buffer(dg_renderer* r) { return r ? r->sh : nullptr; }
+dg_buffer* dg_renderer_pixel_buffer(dg_renderer* r) {
+  return r && r->rasterizer ? r->rasterizer->pixel_color : nullptr;
+}
+dg_buffer* dg_renderer_pixel_last_buffer(dg_renderer* r) {
+  return r && r->rasterizer ? r->rasterizer->pixel_last : nullptr;
+}
+dg_buffer* dg_renderer_gradient_gaussians(dg_renderer* r) { return r ? r->grad_gaussians : nullptr; }
+dg_buffer* dg_renderer_gradient_sh(dg_renderer* r) { return r ? r->grad_sh : nullptr; }
+dg_buffer* dg_renderer_gradient_splats(dg_renderer* r) { return r ? r->grad_splats : nullptr; }
+dg_tile_rasterizer* dg_renderer_tiles(dg_renderer* r) { return r ? r->rasterizer : nullptr; }
+dg_tile_rasterizer* dg_renderer_draw_tiles(dg_renderer* r) { return r ? r->draw_rasterizer : nullptr; }
+
+dg_status dg_renderer_destroy(dg_renderer* r) {
+  if (!r) return DG_OK;
+  destroy_scene(r);
+  if (r->draw_rasterizer) dg_tile_rasterizer_destroy(r->draw_rasterizer);
+  free_buffer(r->camera);
+  delete r;
+  return DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,79 @@
+// Internal view of the renderer's objects, shared with the trainer.
+#pragma once
+#include "dg_common.cuh"
+#include "dg_scan.cuh"
+
+// TileRasterizer (src/tileRasterizer.ts:29-317).
+struct dg_tile_rasterizer {
+  dg_context* ctx;
+  dg_buffer* camera;  // borrowed: the 144-byte Camera uniform
+  dg_buffer* splats;  // borrowed
+  uint32_t count;
+  dg_buffer* tile_offsets;   // per splat: tiles touched, then its first pair slot
+  dg_buffer* scan_total;     // PrefixSum.total: pairs this frame needs
+  dg_buffer* scan_scratch;
+  dg_buffer* raster_params;  // background (rgb, 1)
+  // Pairs (createPairs, src/tileRasterizer.ts:276-293)
+  uint32_t pair_capacity;
+  dg::SortPlan plan;
+  dg_buffer* keys;
+  dg_buffer* values;
+  dg_buffer* keys_alt;
+  dg_buffer* values_alt;
+  dg_buffer* sort_scratch;
+  dg_buffer* ranges;
+  uint32_t ranges_tiles;
+  dg_buffer* pixel_color;
+  dg_buffer* pixel_last;
+  uint32_t pixel_count;
+  // Pair-count readback (src/tileRasterizer.ts:187-191, 229-244)
+  uint32_t* pinned_total;
+  cudaEvent_t readback_event;
+  int readback_state;  // 0 idle, 1 queued
+  uint32_t last_pair_count;
+  uint32_t tiles_x, tiles_y;
+  float viewport[2];
+};
+
+namespace dg {
+// Host-side preparation of a frame: buffer sizes and the background uniform.
+dg_status rasterizer_prepare(dg_tile_rasterizer* tr, const float viewport[2], const float background[3]);
+// The frame's kernels. counts_ready: tile_offsets already hold the per-splat
+// tile counts (the renderer's preprocess writes them), so count_tiles is skipped.
+dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool counts_ready);
+dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr);
+dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
+dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
+                            uint32_t initial_pair_capacity, dg_tile_rasterizer** out);
+dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity);
+}  // namespace dg
+
+// GaussianRenderer (src/gaussianRenderer.ts:55-311).
+struct dg_renderer {
+  dg_context* ctx;
+  uint32_t initial_pair_capacity;
+  dg_buffer* camera;
+  float last_viewport[2];
+  // The scene (src/gaussianRenderer.ts:38-48)
+  bool has_scene;
+  uint32_t count;
+  dg_buffer* gaussians;
+  dg_buffer* splats;
+  dg_buffer* sh;
+  dg_buffer* scene_params;  // element 0: SH degree
+  dg_tile_rasterizer* rasterizer;
+  dg_buffer* grad_splats;
+  dg_buffer* grad_gaussians;
+  dg_buffer* grad_sh;
+  dg_tile_rasterizer* draw_rasterizer;
+};
+
+namespace dg {
+dg_status renderer_write_camera(dg_renderer* r, const dg_camera* camera);
+dg_status renderer_prepare(dg_renderer* r, const dg_camera* camera, const float background[3]);
+dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target);
+dg_status renderer_ensure_gradients(dg_renderer* r);
+dg_status renderer_launch_backward(dg_renderer* r, dg_buffer* pixel_grads, bool write_gaussian_grads);
+// The preprocess backward alone, for callers that fuse the Adam step into it.
+const Camera* renderer_camera(dg_renderer* r);
+}  // namespace dg

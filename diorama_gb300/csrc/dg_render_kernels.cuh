@@ -1,0 +1,217 @@
+// Device code of the renderer's forward and backward passes. This header is
+// compiled into dg_render.cu with --fmad=false, so every product is rounded
+// before it is added exactly as written; fused multiply-adds appear only where
+// fmaf is spelled out. The CPU oracle (oracle/oracle.c) evaluates the same
+// expressions in the same order, so forward splats and images agree bit for bit.
+#pragma once
+#include "dg_common.cuh"
+
+namespace dg {
+
+// The projection shared by preprocess and its backward: the view-space center
+// and the 2D covariance (src/shaders/preprocess.wgsl:27-57). Matrices are held
+// as columns m[col][row]; every sum runs from index 0 upwards.
+struct Projection {
+  float t[3], depth;
+  float r[3][3], q[4], qlen;
+  float m[3][3], cov3d[3][3];
+  float focal[2], limit[2], tx, ty;
+  float jw[3][2];
+  float w[3][3];
+  float a, b, c, det;
+};
+
+// The view-space z of a Gaussian's center, computed exactly as project() does.
+__device__ __forceinline__ float view_z(const Camera& cam, const float* g) {
+  float z = cam.view[0 * 4 + 2] * g[0];
+  z = z + cam.view[1 * 4 + 2] * g[1];
+  z = z + cam.view[2 * 4 + 2] * g[2];
+  z = z + cam.view[3 * 4 + 2] * 1.0f;
+  return z;
+}
+
+__device__ __forceinline__ void rotation_matrix(const float raw[4], float r[3][3], float q[4], float& len_out) {
+  float dot = raw[0] * raw[0];
+  dot = dot + raw[1] * raw[1];
+  dot = dot + raw[2] * raw[2];
+  dot = dot + raw[3] * raw[3];
+  float len = sqrtf(dot);
+  float qw = raw[0] / len, qx = raw[1] / len, qy = raw[2] / len, qz = raw[3] / len;
+  r[0][0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+  r[0][1] = 2.0f * (qx * qy + qw * qz);
+  r[0][2] = 2.0f * (qx * qz - qw * qy);
+  r[1][0] = 2.0f * (qx * qy - qw * qz);
+  r[1][1] = 1.0f - 2.0f * (qx * qx + qz * qz);
+  r[1][2] = 2.0f * (qy * qz + qw * qx);
+  r[2][0] = 2.0f * (qx * qz + qw * qy);
+  r[2][1] = 2.0f * (qy * qz - qw * qx);
+  r[2][2] = 1.0f - 2.0f * (qx * qx + qy * qy);
+  q[0] = qw;
+  q[1] = qx;
+  q[2] = qy;
+  q[3] = qz;
+  len_out = len;
+}
+
+__device__ __forceinline__ void project(const Camera& cam, const float* g, Projection& p) {
+  for (int row = 0; row < 3; row++) {
+    float v = cam.view[0 * 4 + row] * g[0];
+    v = v + cam.view[1 * 4 + row] * g[1];
+    v = v + cam.view[2 * 4 + row] * g[2];
+    v = v + cam.view[3 * 4 + row] * 1.0f;
+    p.t[row] = v;
+  }
+  p.depth = -p.t[2];
+  rotation_matrix(g + 8, p.r, p.q, p.qlen);
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) p.m[col][row] = p.r[col][row] * g[4 + col];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      float v = p.m[0][row] * p.m[0][col];
+      v = v + p.m[1][row] * p.m[1][col];
+      v = v + p.m[2][row] * p.m[2][col];
+      p.cov3d[col][row] = v;
+    }
+  p.focal[0] = cam.proj[0] * cam.viewport[0] * 0.5f;
+  p.focal[1] = cam.proj[5] * cam.viewport[1] * 0.5f;
+  p.limit[0] = 1.3f * cam.viewport[0] * 0.5f / p.focal[0];
+  p.limit[1] = 1.3f * cam.viewport[1] * 0.5f / p.focal[1];
+  const float depth = p.depth;
+  p.tx = clampf(p.t[0] / depth, -p.limit[0], p.limit[0]) * depth;
+  p.ty = clampf(p.t[1] / depth, -p.limit[1], p.limit[1]) * depth;
+  float j[3][2];
+  j[0][0] = p.focal[0] / depth;
+  j[0][1] = 0.0f;
+  j[1][0] = 0.0f;
+  j[1][1] = -p.focal[1] / depth;
+  j[2][0] = p.focal[0] * p.tx / (depth * depth);
+  j[2][1] = -p.focal[1] * p.ty / (depth * depth);
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 3; row++) p.w[col][row] = cam.view[col * 4 + row];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = j[0][row] * p.w[col][0];
+      v = v + j[1][row] * p.w[col][1];
+      v = v + j[2][row] * p.w[col][2];
+      p.jw[col][row] = v;
+    }
+  float t1[3][2];
+#pragma unroll
+  for (int col = 0; col < 3; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = p.jw[0][row] * p.cov3d[col][0];
+      v = v + p.jw[1][row] * p.cov3d[col][1];
+      v = v + p.jw[2][row] * p.cov3d[col][2];
+      t1[col][row] = v;
+    }
+  float cov[2][2];
+#pragma unroll
+  for (int col = 0; col < 2; col++)
+#pragma unroll
+    for (int row = 0; row < 2; row++) {
+      float v = t1[0][row] * p.jw[0][col];
+      v = v + t1[1][row] * p.jw[1][col];
+      v = v + t1[2][row] * p.jw[2][col];
+      cov[col][row] = v;
+    }
+  p.a = cov[0][0] + 0.3f;
+  p.b = cov[0][1];
+  p.c = cov[1][1] + 0.3f;
+  p.det = p.a * p.c - p.b * p.b;
+}
+
+__device__ __forceinline__ void camera_position(const Camera& cam, float out[3]) {
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+    float v = cam.view[col * 4 + 0] * cam.view[12];
+    v = v + cam.view[col * 4 + 1] * cam.view[13];
+    v = v + cam.view[col * 4 + 2] * cam.view[14];
+    out[col] = -v;
+  }
+}
+
+__device__ __forceinline__ float normalize3(const float v[3], float out[3]) {
+  float dot = v[0] * v[0];
+  dot = dot + v[1] * v[1];
+  dot = dot + v[2] * v[2];
+  float len = sqrtf(dot);
+  out[0] = v[0] / len;
+  out[1] = v[1] / len;
+  out[2] = v[2] / len;
+  return len;
+}
+
+// src/shaders/gaussianMath.wgsl:30-44
+__device__ __forceinline__ void sh_basis(const float d[3], float b[15]) {
+  const float C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+                       0.5462742152789498f};
+  const float C3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f, 0.3731763325901154f,
+                       -0.4570457994644658f, 1.445305721320277f, -0.5900435899266435f};
+  float x = d[0], y = d[1], z = d[2];
+  float xx = x * x, yy = y * y, zz = z * z;
+  b[0] = -SH_C1 * y;
+  b[1] = SH_C1 * z;
+  b[2] = -SH_C1 * x;
+  b[3] = C2[0] * x * y;
+  b[4] = C2[1] * y * z;
+  b[5] = C2[2] * (2.0f * zz - xx - yy);
+  b[6] = C2[3] * x * z;
+  b[7] = C2[4] * (xx - yy);
+  b[8] = C3[0] * y * (3.0f * xx - yy);
+  b[9] = C3[1] * x * y * z;
+  b[10] = C3[2] * y * (4.0f * zz - xx - yy);
+  b[11] = C3[3] * z * (2.0f * zz - 3.0f * xx - 3.0f * yy);
+  b[12] = C3[4] * x * (4.0f * zz - xx - yy);
+  b[13] = C3[5] * z * (xx - yy);
+  b[14] = C3[6] * x * (xx - 3.0f * yy);
+}
+
+// src/shaders/gaussianMath.wgsl:47-71, as g[k][axis].
+__device__ __forceinline__ void sh_basis_gradient(const float d[3], float g[15][3]) {
+  const float C2[5] = {1.0925484305920792f, -1.0925484305920792f, 0.31539156525252005f, -1.0925484305920792f,
+                       0.5462742152789498f};
+  const float C3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570457994644658f, 0.3731763325901154f,
+                       -0.4570457994644658f, 1.445305721320277f, -0.5900435899266435f};
+  float x = d[0], y = d[1], z = d[2];
+  float xx = x * x, yy = y * y, zz = z * z;
+  g[0][0] = 0.0f; g[0][1] = -SH_C1; g[0][2] = 0.0f;
+  g[1][0] = 0.0f; g[1][1] = 0.0f; g[1][2] = SH_C1;
+  g[2][0] = -SH_C1; g[2][1] = 0.0f; g[2][2] = 0.0f;
+  g[3][0] = C2[0] * y; g[3][1] = C2[0] * x; g[3][2] = C2[0] * 0.0f;
+  g[4][0] = C2[1] * 0.0f; g[4][1] = C2[1] * z; g[4][2] = C2[1] * y;
+  g[5][0] = C2[2] * (-2.0f * x); g[5][1] = C2[2] * (-2.0f * y); g[5][2] = C2[2] * (4.0f * z);
+  g[6][0] = C2[3] * z; g[6][1] = C2[3] * 0.0f; g[6][2] = C2[3] * x;
+  g[7][0] = C2[4] * (2.0f * x); g[7][1] = C2[4] * (-2.0f * y); g[7][2] = C2[4] * 0.0f;
+  g[8][0] = C3[0] * (6.0f * x * y); g[8][1] = C3[0] * (3.0f * xx - 3.0f * yy); g[8][2] = C3[0] * 0.0f;
+  g[9][0] = C3[1] * (y * z); g[9][1] = C3[1] * (x * z); g[9][2] = C3[1] * (x * y);
+  g[10][0] = C3[2] * (-2.0f * x * y); g[10][1] = C3[2] * (4.0f * zz - xx - 3.0f * yy); g[10][2] = C3[2] * (8.0f * y * z);
+  g[11][0] = C3[3] * (-6.0f * x * z); g[11][1] = C3[3] * (-6.0f * y * z);
+  g[11][2] = C3[3] * (6.0f * zz - 3.0f * xx - 3.0f * yy);
+  g[12][0] = C3[4] * (4.0f * zz - 3.0f * xx - yy); g[12][1] = C3[4] * (-2.0f * x * y); g[12][2] = C3[4] * (8.0f * x * z);
+  g[13][0] = C3[5] * (2.0f * x * z); g[13][1] = C3[5] * (-2.0f * y * z); g[13][2] = C3[5] * (xx - yy);
+  g[14][0] = C3[6] * (3.0f * xx - 3.0f * yy); g[14][1] = C3[6] * (-6.0f * x * y); g[14][2] = C3[6] * 0.0f;
+}
+
+// tile_count / tile_rect (src/shaders/common.wgsl:31-42).
+__device__ __forceinline__ uint2 tile_grid(const Camera& cam) {
+  return make_uint2(((uint32_t)cam.viewport[0] + TILE - 1u) / TILE, ((uint32_t)cam.viewport[1] + TILE - 1u) / TILE);
+}
+
+__device__ __forceinline__ uint4 tile_rect(float mx, float my, float radius, uint2 tiles) {
+  float lox = clampf(floorf((mx - radius) / 16.0f), 0.0f, (float)tiles.x);
+  float loy = clampf(floorf((my - radius) / 16.0f), 0.0f, (float)tiles.y);
+  float hix = clampf(floorf((mx + radius) / 16.0f) + 1.0f, 0.0f, (float)tiles.x);
+  float hiy = clampf(floorf((my + radius) / 16.0f) + 1.0f, 0.0f, (float)tiles.y);
+  return make_uint4((uint32_t)lox, (uint32_t)loy, (uint32_t)hix, (uint32_t)hiy);
+}
+
+}  // namespace dg

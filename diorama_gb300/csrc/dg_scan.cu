@@ -1,0 +1,214 @@
+// PrefixSum (src/prefixSum.ts:10-103, src/shaders/prefixSum.wgsl:31-91): an
+// exclusive scan of u32 values in place, whose length can come from a device
+// buffer, writing the grand total to `total[0]`.
+//
+// The reference runs a 512-value Blelloch scan per workgroup, recursively, with
+// 2·levels + 1 dispatches. Here it is ONE launch: a single-pass scan with
+// decoupled look-back (Merrill & Garland 2016). Each CTA takes the next tile of
+// 4096 values by an atomic ticket (so the tiles before it are already running),
+// scans it with warp shuffles, publishes its aggregate, and looks back over its
+// predecessors' published values a warp at a time. Every wait is bounded: after
+// SPIN_LIMIT polls it sets DEVICE_ERROR_SCAN_WAIT and stops waiting.
+#include "dg_common.cuh"
+#include "dg_scan.cuh"
+
+#include <cuda/atomic>
+
+namespace dg {
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096
+constexpr uint64_t FLAG_AGGREGATE = 1ull << 62;
+constexpr uint64_t FLAG_PREFIX = 2ull << 62;
+constexpr uint64_t FLAG_MASK = 3ull << 62;
+
+__device__ __forceinline__ uint64_t load_status(uint64_t* p) {
+  cuda::atomic_ref<uint64_t, cuda::thread_scope_device> ref(*p);
+  return ref.load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void store_status(uint64_t* p, uint64_t v) {
+  cuda::atomic_ref<uint64_t, cuda::thread_scope_device> ref(*p);
+  ref.store(v, cuda::memory_order_relaxed);
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive(uint32_t v, int lane) {
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t n = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += n;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict__ data, uint32_t capacity,
+                                                          const uint32_t* __restrict__ count_ptr,
+                                                          uint32_t* __restrict__ total, uint64_t* __restrict__ status,
+                                                          uint32_t* __restrict__ ticket, uint32_t* __restrict__ error) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_prefix;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  uint32_t n = count_ptr ? min(*count_ptr, capacity) : capacity;
+  uint32_t tiles = max(1u, (n + SCAN_TILE - 1) / SCAN_TILE);
+  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= tiles) return;
+
+  // Each thread owns SCAN_ITEMS consecutive values.
+  const uint64_t base = (uint64_t)tile * SCAN_TILE + (uint64_t)tid * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  const bool full = base + SCAN_ITEMS <= n && (reinterpret_cast<uintptr_t>(data) & 15) == 0;
+  if (full) {
+    const uint4* p = reinterpret_cast<const uint4*>(data + base);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; k++) {
+      uint4 q = p[k];
+      v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = base + k < n ? data[base + k] : 0u;
+  }
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) sum += v[k];
+  uint32_t incl = warp_inclusive(sum, lane);
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0u;
+    uint32_t wi = warp_inclusive(w, lane);
+    if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive per warp
+    uint32_t aggregate = __shfl_sync(0xffffffffu, wi, 31);
+    // Publish and look back.
+    uint32_t exclusive = 0;
+    if (tile == 0) {
+      if (lane == 0) store_status(&status[0], FLAG_PREFIX | aggregate);
+    } else {
+      if (lane == 0) store_status(&status[tile], FLAG_AGGREGATE | aggregate);
+      int64_t look = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      while (true) {
+        int64_t idx = look - lane;
+        uint64_t s = idx >= 0 ? load_status(&status[idx]) : (FLAG_PREFIX | 0ull);
+        while (!__all_sync(0xffffffffu, (s & FLAG_MASK) != 0)) {
+          if (++spins > SPIN_LIMIT) {
+            if (lane == 0) atomicOr(error, DEVICE_ERROR_SCAN_WAIT);
+            s = FLAG_PREFIX;  // give up: the values are wrong, but nothing hangs
+            break;
+          }
+          if ((s & FLAG_MASK) == 0) s = load_status(&status[idx]);
+        }
+        if ((s & FLAG_MASK) == 0) s = FLAG_PREFIX;
+        uint32_t prefix_lanes = __ballot_sync(0xffffffffu, (s & FLAG_MASK) == FLAG_PREFIX);
+        uint32_t value = (uint32_t)(s & 0xffffffffull);
+        if (prefix_lanes) {
+          int first = __ffs(prefix_lanes) - 1;  // the nearest predecessor with a full prefix
+          uint32_t part = lane <= first ? value : 0u;
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(0xffffffffu, part, d);
+          exclusive += part;
+          break;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) value += __shfl_xor_sync(0xffffffffu, value, d);
+        exclusive += value;
+        look -= 32;
+      }
+      if (lane == 0) store_status(&status[tile], FLAG_PREFIX | (uint64_t)(uint32_t)(exclusive + aggregate));
+    }
+    if (lane == 0) {
+      s_prefix = exclusive;
+      if (tile == tiles - 1) *total = exclusive + aggregate;
+    }
+  }
+  __syncthreads();
+  uint32_t running = s_prefix + s_warp[warp] + incl - sum;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    uint32_t x = v[k];
+    v[k] = running;
+    running += x;
+  }
+  if (full) {
+    uint4* p = reinterpret_cast<uint4*>(data + base);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS / 4; k++) p[k] = make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++)
+      if (base + k < n) data[base + k] = v[k];
+  }
+}
+
+}  // namespace
+
+size_t scan_scratch_bytes(uint32_t capacity) {
+  uint32_t tiles = std::max(1u, ceil_div(capacity, SCAN_TILE));
+  return 256 + (size_t)tiles * sizeof(uint64_t);
+}
+
+dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const uint32_t* count, uint32_t* total,
+                      void* scratch) {
+  uint32_t tiles = std::max(1u, ceil_div(capacity, SCAN_TILE));
+  auto* ticket = static_cast<uint32_t*>(scratch);
+  auto* status = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + 256);
+  DG_CUDA(cudaMemsetAsync(scratch, 0, scan_scratch_bytes(capacity), ctx->stream));
+  scan_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, total, status, ticket, ctx->device_error);
+  ctx->launches++;
+  DG_LAUNCHED("scan_kernel");
+  return DG_OK;
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+struct dg_prefix_sum {
+  dg_context* ctx;
+  dg_buffer* data;
+  dg_buffer* count;  // borrowed, may be NULL
+  uint32_t capacity;
+  dg_buffer* total;
+  dg_buffer* scratch;
+};
+
+extern "C" {
+
+dg_status dg_prefix_sum_create(dg_context* ctx, dg_buffer* data, uint32_t capacity, dg_buffer* count,
+                               dg_prefix_sum** out) {
+  DG_REQUIRE(ctx && data && out, "NULL argument");
+  DG_REQUIRE((uint64_t)capacity * 4 <= data->bytes, "capacity exceeds the data buffer");
+  DG_REQUIRE(!count || count->bytes >= 4, "count buffer too small");
+  auto* s = new dg_prefix_sum{ctx, data, count, capacity, nullptr, nullptr};
+  dg_status st = alloc_buffer(ctx, 4, &s->total);
+  if (st == DG_OK) st = alloc_buffer(ctx, scan_scratch_bytes(capacity), &s->scratch);
+  if (st != DG_OK) {
+    dg_prefix_sum_destroy(s);
+    return st;
+  }
+  *out = s;
+  return DG_OK;
+}
+
+dg_status dg_prefix_sum_encode(dg_prefix_sum* s) {
+  DG_REQUIRE(s, "NULL argument");
+  return scan_launch(s->ctx, typed<uint32_t>(s->data), s->capacity, s->count ? typed<uint32_t>(s->count) : nullptr,
+                     typed<uint32_t>(s->total), s->scratch->ptr);
+}
+
+dg_buffer* dg_prefix_sum_total(dg_prefix_sum* s) { return s ? s->total : nullptr; }
+
+dg_status dg_prefix_sum_destroy(dg_prefix_sum* s) {
+  if (!s) return DG_OK;
+  free_buffer(s->total);
+  free_buffer(s->scratch);
+  delete s;
+  return DG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,31 @@
+// Internal entry points of the scan and the sort, shared by the tile stage and
+// densification.
+#pragma once
+#include "dg_common.cuh"
+
+namespace dg {
+
+// Exclusive scan of min(*count, capacity) values of data in place (count may be
+// NULL: all capacity values); total[0] gets the sum. scratch holds
+// scan_scratch_bytes(capacity) bytes and is cleared by each launch.
+size_t scan_scratch_bytes(uint32_t capacity);
+dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const uint32_t* count, uint32_t* total,
+                      void* scratch);
+
+// Stable LSD radix sort with the reference's pass plan, in place in keys/values
+// (the scratch pair holds the odd passes). key_words = 1 for u32 keys, 2 for u64
+// keys stored (low, high) whose high word contributes high_bits bits.
+struct SortPlan {
+  uint32_t capacity;
+  uint32_t key_words;
+  uint32_t high_bits;
+  uint32_t passes;
+};
+SortPlan sort_plan(uint32_t capacity, uint32_t high_bits);
+// Per-device kernel attributes; called once when a context is created.
+dg_status sort_init();
+size_t sort_scratch_bytes(const SortPlan& plan);
+dg_status sort_launch(dg_context* ctx, const SortPlan& plan, void* keys, uint32_t* values, void* keys_alt,
+                      uint32_t* values_alt, const uint32_t* count, void* scratch);
+
+}  // namespace dg

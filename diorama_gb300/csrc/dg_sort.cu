@@ -1,0 +1,370 @@
+// RadixSort (src/radixSort.ts:27-142, src/shaders/radixSort.wgsl:45-120): a
+// stable LSD radix sort of u32 keys, or u64 keys stored as (low, high) of which
+// the high word contributes `high_bits` bits, each key carrying a u32 value.
+//
+// The pass plan is the reference's: 8-bit digits, four passes over the low word,
+// then 2·ceil(high_bits/16) over the high word, ping-ponging so the result lands
+// back in keys/values. Any stable LSD sort over the same digits yields the same
+// permutation, so the result is bit-identical to the reference's.
+//
+// The reference runs count_digits, a multi-level scan and scatter per pass (three
+// or more dispatches and four barriers per 256-key chunk). Here it is onesweep
+// (Adinets & Merrill 2022): one upfront kernel reads every key once and builds
+// the digit histograms of all passes, then each pass is ONE kernel. A CTA takes
+// the next tile of 3840 keys by ticket, ranks each key within its warp with
+// ballots (stable: warp-striped loads are ranked round by round), publishes its
+// per-digit counts, looks back over earlier tiles' counts (bounded waits), and
+// scatters through shared memory so each digit's run is written contiguously.
+#include "dg_common.cuh"
+#include "dg_scan.cuh"
+
+#include <cuda/atomic>
+
+namespace dg {
+
+namespace {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int SORT_ITEMS = 15;
+constexpr uint32_t WARP_ITEMS = 32 * SORT_ITEMS;             // 480
+constexpr uint32_t SORT_TILE = SORT_THREADS * SORT_ITEMS;    // 3840
+constexpr uint32_t RADIX = 256;
+constexpr uint32_t FLAG_AGGREGATE = 1u << 30;
+constexpr uint32_t FLAG_PREFIX = 2u << 30;
+constexpr uint32_t FLAG_MASK = 3u << 30;
+constexpr uint32_t VALUE_MASK = (1u << 30) - 1;
+constexpr int HIST_THREADS = 256;
+constexpr int MAX_PASSES = 8;
+
+template <int KW>
+struct KeyOf;
+template <>
+struct KeyOf<1> {
+  using type = uint32_t;
+};
+template <>
+struct KeyOf<2> {
+  using type = uint64_t;
+};
+
+__device__ __forceinline__ uint32_t load_status(uint32_t* p) {
+  cuda::atomic_ref<uint32_t, cuda::thread_scope_device> ref(*p);
+  return ref.load(cuda::memory_order_relaxed);
+}
+__device__ __forceinline__ void store_status(uint32_t* p, uint32_t v) {
+  cuda::atomic_ref<uint32_t, cuda::thread_scope_device> ref(*p);
+  ref.store(v, cuda::memory_order_relaxed);
+}
+
+struct PassShifts {
+  uint32_t shift[MAX_PASSES];
+};
+
+// Digit histograms of every pass from one read of the keys.
+template <int KW>
+__global__ void __launch_bounds__(HIST_THREADS) sort_histogram_kernel(const typename KeyOf<KW>::type* __restrict__ keys,
+                                                                      uint32_t capacity, const uint32_t* __restrict__ count,
+                                                                      uint32_t passes, PassShifts shifts,
+                                                                      uint32_t* __restrict__ hist) {
+  __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
+  for (uint32_t i = threadIdx.x; i < passes * RADIX; i += HIST_THREADS) s_hist[i / RADIX][i % RADIX] = 0;
+  __syncthreads();
+  const uint32_t n = count ? min(*count, capacity) : capacity;
+  for (uint32_t i = blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += gridDim.x * HIST_THREADS) {
+    uint64_t key = keys[i];
+    for (uint32_t p = 0; p < passes; p++) atomicAdd(&s_hist[p][(key >> shifts.shift[p]) & 0xff], 1u);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < passes * RADIX; i += HIST_THREADS) {
+    uint32_t c = s_hist[i / RADIX][i % RADIX];
+    if (c) atomicAdd(&hist[i], c);
+  }
+}
+
+// Exclusive scan of one value per thread over the CTA's 256 threads.
+__device__ __forceinline__ uint32_t block_exclusive_256(uint32_t v, uint32_t* s_tmp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t n = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += n;
+  }
+  if (lane == 31) s_tmp[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0;
+#pragma unroll
+  for (int w = 0; w < SORT_WARPS; w++) before += w < warp ? s_tmp[w] : 0u;
+  __syncthreads();
+  return before + incl - v;
+}
+
+template <int KW>
+__global__ void __launch_bounds__(SORT_THREADS, 2)
+    sort_pass_kernel(const typename KeyOf<KW>::type* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                     typename KeyOf<KW>::type* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                     uint32_t capacity, const uint32_t* __restrict__ count, uint32_t shift,
+                     const uint32_t* __restrict__ pass_hist, uint32_t* __restrict__ status,
+                     uint32_t* __restrict__ ticket, uint32_t* __restrict__ error) {
+  using K = typename KeyOf<KW>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  K* s_keys = reinterpret_cast<K*>(smem);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + SORT_TILE);
+  uint32_t* s_whist = s_vals + SORT_TILE;          // [warp][digit]
+  uint32_t* s_block_start = s_whist + SORT_WARPS * RADIX;
+  uint32_t* s_base = s_block_start + RADIX;
+  uint32_t* s_tmp = s_base + RADIX;
+  __shared__ uint32_t s_tile;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t n = count ? min(*count, capacity) : capacity;
+  const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+  if (tid == 0) s_tile = atomicAdd(ticket, 1u);
+  for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) s_whist[i] = 0;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= tiles) return;
+
+  // Load, warp-striped: warp w owns keys [w*480, w*480+480) of the tile, round j
+  // reads 32 consecutive ones, so order within the tile is (warp, round, lane).
+  const uint32_t base = tile * SORT_TILE + warp * WARP_ITEMS + lane;
+  K key[SORT_ITEMS];
+  uint32_t val[SORT_ITEMS];
+  uint32_t rank[SORT_ITEMS];
+#pragma unroll
+  for (int j = 0; j < SORT_ITEMS; j++) {
+    uint32_t idx = base + j * 32;
+    bool valid = idx < n;
+    key[j] = valid ? keys_in[idx] : K(0);
+    val[j] = valid ? vals_in[idx] : 0u;
+  }
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t* my_hist = s_whist + warp * RADIX;
+#pragma unroll
+  for (int j = 0; j < SORT_ITEMS; j++) {
+    bool valid = base + j * 32 < n;
+    uint32_t d = (uint32_t)(key[j] >> shift) & 0xffu;
+    uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+      uint32_t bit = (d >> b) & 1u;
+      uint32_t vote = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? vote : ~vote;
+    }
+    int leader = valid ? __ffs(peers) - 1 : lane;
+    uint32_t old = 0;
+    if (valid && lane == leader) {
+      old = my_hist[d];
+      my_hist[d] = old + __popc(peers);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rank[j] = old + __popc(peers & lt_mask);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // Per digit (thread = digit): offsets of each warp's run, and the tile's count.
+  const uint32_t d = tid;
+  uint32_t running = 0;
+#pragma unroll
+  for (int w = 0; w < SORT_WARPS; w++) {
+    uint32_t c = s_whist[w * RADIX + d];
+    s_whist[w * RADIX + d] = running;
+    running += c;
+  }
+  const uint32_t tile_count = running;
+  store_status(&status[tile * RADIX + d], (tile == 0 ? FLAG_PREFIX : FLAG_AGGREGATE) | tile_count);
+  const uint32_t block_start = block_exclusive_256(tile_count, s_tmp);
+  const uint32_t global_start = block_exclusive_256(pass_hist[d], s_tmp);
+  s_block_start[d] = block_start;
+
+  // Decoupled look-back over earlier tiles, for this thread's digit.
+  uint32_t prefix = 0;
+  if (tile > 0) {
+    int32_t look = (int32_t)tile - 1;
+    uint32_t spins = 0;
+    while (look >= 0) {
+      uint32_t s = load_status(&status[look * RADIX + d]);
+      while ((s & FLAG_MASK) == 0) {
+        if (++spins > SPIN_LIMIT) {
+          atomicOr(error, DEVICE_ERROR_SORT_WAIT);
+          s = FLAG_PREFIX;  // give up: the order is wrong, but nothing hangs
+          break;
+        }
+        s = load_status(&status[look * RADIX + d]);
+      }
+      prefix += s & VALUE_MASK;
+      if ((s & FLAG_MASK) == FLAG_PREFIX) break;
+      look--;
+    }
+    store_status(&status[tile * RADIX + d], FLAG_PREFIX | ((prefix + tile_count) & VALUE_MASK));
+  }
+  s_base[d] = global_start + prefix - block_start;
+  __syncthreads();
+
+  // Place each key at its rank within the tile, grouped by digit.
+#pragma unroll
+  for (int j = 0; j < SORT_ITEMS; j++) {
+    if (base + j * 32 < n) {
+      uint32_t dj = (uint32_t)(key[j] >> shift) & 0xffu;
+      uint32_t pos = s_block_start[dj] + s_whist[warp * RADIX + dj] + rank[j];
+      s_keys[pos] = key[j];
+      s_vals[pos] = val[j];
+    }
+  }
+  __syncthreads();
+  const uint32_t here = min(SORT_TILE, n - tile * SORT_TILE);
+  for (uint32_t k = tid; k < here; k += SORT_THREADS) {
+    K kk = s_keys[k];
+    uint32_t dk = (uint32_t)(kk >> shift) & 0xffu;
+    uint32_t out = s_base[dk] + k;
+    keys_out[out] = kk;
+    vals_out[out] = s_vals[k];
+  }
+}
+
+template <int KW>
+size_t pass_smem_bytes() {
+  return SORT_TILE * (sizeof(typename KeyOf<KW>::type) + 4) + (SORT_WARPS * RADIX + 2 * RADIX + 32) * 4;
+}
+
+struct ScratchLayout {
+  size_t tickets, hist, status, total;
+  uint32_t max_tiles;
+};
+
+ScratchLayout layout_of(const SortPlan& plan) {
+  ScratchLayout l;
+  l.max_tiles = std::max(1u, ceil_div(plan.capacity, SORT_TILE));
+  l.tickets = 0;
+  l.hist = 256;
+  l.status = l.hist + (size_t)plan.passes * RADIX * 4;
+  l.total = l.status + (size_t)plan.passes * l.max_tiles * RADIX * 4;
+  return l;
+}
+
+template <int KW>
+dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32_t* values, void* keys_alt,
+                       uint32_t* values_alt, const uint32_t* count, void* scratch) {
+  using K = typename KeyOf<KW>::type;
+  ScratchLayout l = layout_of(plan);
+  char* s = static_cast<char*>(scratch);
+  auto* tickets = reinterpret_cast<uint32_t*>(s + l.tickets);
+  auto* hist = reinterpret_cast<uint32_t*>(s + l.hist);
+  auto* status = reinterpret_cast<uint32_t*>(s + l.status);
+  DG_CUDA(cudaMemsetAsync(scratch, 0, l.total, ctx->stream));
+  PassShifts shifts{};
+  for (uint32_t p = 0; p < plan.passes; p++) shifts.shift[p] = p < 4 ? p * 8 : 32 + (p - 4) * 8;
+  uint32_t hist_blocks = std::min<uint32_t>(ceil_div(plan.capacity, HIST_THREADS * 16), (uint32_t)ctx->sm_count * 4);
+  hist_blocks = std::max(1u, hist_blocks);
+  sort_histogram_kernel<KW><<<hist_blocks, HIST_THREADS, 0, ctx->stream>>>(static_cast<const K*>(keys), plan.capacity,
+                                                                           count, plan.passes, shifts, hist);
+  ctx->launches++;
+  DG_LAUNCHED("sort_histogram_kernel");
+  size_t smem = pass_smem_bytes<KW>();
+  K* in_k = static_cast<K*>(keys);
+  uint32_t* in_v = values;
+  K* out_k = static_cast<K*>(keys_alt);
+  uint32_t* out_v = values_alt;
+  for (uint32_t p = 0; p < plan.passes; p++) {
+    sort_pass_kernel<KW><<<l.max_tiles, SORT_THREADS, smem, ctx->stream>>>(
+        in_k, in_v, out_k, out_v, plan.capacity, count, shifts.shift[p], hist + p * RADIX,
+        status + (size_t)p * l.max_tiles * RADIX, tickets + p, ctx->device_error);
+    ctx->launches++;
+    DG_LAUNCHED("sort_pass_kernel");
+    std::swap(in_k, out_k);
+    std::swap(in_v, out_v);
+  }
+  return DG_OK;
+}
+
+}  // namespace
+
+dg_status sort_init() {
+  // The pass kernels use more than the default 48 KB of dynamic shared memory.
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pass_smem_bytes<1>()));
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pass_smem_bytes<2>()));
+  return DG_OK;
+}
+
+SortPlan sort_plan(uint32_t capacity, uint32_t high_bits) {
+  SortPlan p;
+  p.capacity = capacity;
+  p.key_words = high_bits > 0 ? 2 : 1;
+  p.high_bits = high_bits;
+  p.passes = 4 + 2 * ((high_bits + 15) / 16);
+  return p;
+}
+
+size_t sort_scratch_bytes(const SortPlan& plan) { return layout_of(plan).total; }
+
+dg_status sort_launch(dg_context* ctx, const SortPlan& plan, void* keys, uint32_t* values, void* keys_alt,
+                      uint32_t* values_alt, const uint32_t* count, void* scratch) {
+  if (plan.key_words == 2)
+    return launch_typed<2>(ctx, plan, keys, values, keys_alt, values_alt, count, scratch);
+  return launch_typed<1>(ctx, plan, keys, values, keys_alt, values_alt, count, scratch);
+}
+
+}  // namespace dg
+
+using namespace dg;
+
+struct dg_radix_sort {
+  dg_context* ctx;
+  SortPlan plan;
+  dg_buffer* keys;
+  dg_buffer* values;
+  dg_buffer* keys_alt;
+  dg_buffer* values_alt;
+  dg_buffer* scratch;
+  dg_buffer* count;  // borrowed, may be NULL
+};
+
+extern "C" {
+
+dg_status dg_radix_sort_create(dg_context* ctx, uint32_t capacity, uint32_t high_bits, dg_buffer* count,
+                               dg_radix_sort** out) {
+  DG_REQUIRE(ctx && out, "NULL argument");
+  DG_REQUIRE(high_bits <= 32, "high_bits is at most 32");
+  DG_REQUIRE(capacity < (1u << 30), "capacity must be below 2^30 keys");
+  DG_REQUIRE(!count || count->bytes >= 4, "count buffer too small");
+  auto* s = new dg_radix_sort{ctx, sort_plan(capacity, high_bits), nullptr, nullptr, nullptr, nullptr, nullptr, count};
+  size_t kb = (size_t)capacity * (high_bits > 0 ? 8 : 4);
+  dg_status st = alloc_buffer(ctx, kb, &s->keys);
+  if (st == DG_OK) st = alloc_buffer(ctx, (size_t)capacity * 4, &s->values);
+  if (st == DG_OK) st = alloc_buffer(ctx, kb, &s->keys_alt);
+  if (st == DG_OK) st = alloc_buffer(ctx, (size_t)capacity * 4, &s->values_alt);
+  if (st == DG_OK) st = alloc_buffer(ctx, sort_scratch_bytes(s->plan), &s->scratch);
+  if (st != DG_OK) {
+    dg_radix_sort_destroy(s);
+    return st;
+  }
+  *out = s;
+  return DG_OK;
+}
+
+dg_buffer* dg_radix_sort_keys(dg_radix_sort* s) { return s ? s->keys : nullptr; }
+dg_buffer* dg_radix_sort_values(dg_radix_sort* s) { return s ? s->values : nullptr; }
+uint32_t dg_radix_sort_capacity(const dg_radix_sort* s) { return s ? s->plan.capacity : 0; }
+
+dg_status dg_radix_sort_encode(dg_radix_sort* s) {
+  DG_REQUIRE(s, "NULL argument");
+  return sort_launch(s->ctx, s->plan, s->keys->ptr, typed<uint32_t>(s->values), s->keys_alt->ptr,
+                     typed<uint32_t>(s->values_alt), s->count ? typed<uint32_t>(s->count) : nullptr, s->scratch->ptr);
+}
+
+dg_status dg_radix_sort_destroy(dg_radix_sort* s) {
+  if (!s) return DG_OK;
+  free_buffer(s->keys);
+  free_buffer(s->values);
+  free_buffer(s->keys_alt);
+  free_buffer(s->values_alt);
+  free_buffer(s->scratch);
+  delete s;
+  return DG_OK;
+}
+
+}  // extern "C"

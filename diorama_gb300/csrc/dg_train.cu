@@ -1,0 +1,697 @@
+// Training: Adam with activation (src/shaders/adam.wgsl), densification as
+// stream compaction (src/shaders/densify.wgsl), and the Trainer loop of
+// src/trainer.ts, with each optimize() step optionally replayed as one captured
+// CUDA graph.
+#include "dg_common.cuh"
+#include "dg_loss.cuh"
+#include "dg_render.cuh"
+#include "dg_scan.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace dg {
+namespace {
+
+constexpr uint32_t RESET_SLOT = 3;          // opacity's Adam slot
+constexpr float RESET_LOGIT = -4.59511985013459f;  // logit(0.01), src/shaders/adam.wgsl:112
+constexpr float SPLIT_SHRINK = 1.6f;
+constexpr float LOG_SPLIT_SHRINK = 0.470003629245735553f;  // ln 1.6
+
+// AdamParams (src/shaders/adam.wgsl:9-22)
+struct AdamParams {
+  float bias_correction1, bias_correction2;
+  float position_lr, opacity_lr, scale_lr, rotation_lr, color_lr, sh_lr;
+  float viewport[2];
+  float pad[2];
+};
+
+// DensifyParams (src/shaders/densify.wgsl:149-161)
+struct DensifyParams {
+  float grad_threshold, clone_max_size, min_opacity, max_size;
+  uint32_t seed;
+};
+
+__device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
+
+__device__ __forceinline__ float adam_update(float value, float grad, float2& m, float lr, float bc1, float bc2) {
+  m.x = 0.9f * m.x + 0.1f * grad;
+  m.y = 0.999f * m.y + 0.001f * grad * grad;
+  return value - lr * (m.x / bc1) / (sqrtf(m.y / bc2) + 1e-15f);
+}
+
+// The activated value of raw slot k (src/shaders/adam.wgsl:60-71); slots 7 and 15 are not written.
+__device__ __forceinline__ float activated(uint32_t k, float raw) {
+  if (k >= 4 && k <= 6) return expf(raw);
+  if (k == 3) return sigmoidf_(raw);
+  if (k >= 12 && k <= 14) return 0.5f + SH_C0 * raw;
+  return raw;
+}
+
+// src/shaders/adam.wgsl:80-107, one thread per (Gaussian, moment slot): Adam's
+// slots are contiguous per Gaussian (16 raw parameters then 45 SH coefficients),
+// so consecutive threads read consecutive moments, parameters and gradients and
+// every access coalesces. Slots 7 and 15 (padding, which holds densification
+// stamps) are left alone.
+__global__ void __launch_bounds__(256) adam_kernel(const AdamParams* __restrict__ ap, float* __restrict__ params,
+                                                   float* __restrict__ sh, float2* __restrict__ moments,
+                                                   const float* __restrict__ ggrad, const float* __restrict__ sgrad,
+                                                   float* __restrict__ gaussians, uint32_t count) {
+  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= count * MOMENT_SLOTS) return;
+  const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
+  if (k == 7 || k == 15) return;
+  const float bc1 = ap->bias_correction1, bc2 = ap->bias_correction2;
+  float2 m = moments[e];
+  if (k < FLOATS_PER_GAUSSIAN) {
+    const size_t at = (size_t)i * FLOATS_PER_GAUSSIAN + k;
+    const float value = params[at];
+    float grad = ggrad[at];
+    float lr;
+    if (k < 3) {
+      lr = ap->position_lr;
+    } else if (k == 3) {
+      const float opacity = sigmoidf_(value);
+      grad = grad * opacity * (1.0f - opacity);
+      lr = ap->opacity_lr;
+    } else if (k < 7) {
+      grad = grad * expf(value);
+      lr = ap->scale_lr;
+    } else if (k < 12) {
+      lr = ap->rotation_lr;
+    } else {
+      grad = grad * SH_C0;
+      lr = ap->color_lr;
+    }
+    const float next = adam_update(value, grad, m, lr, bc1, bc2);
+    params[at] = next;
+    gaussians[at] = activated(k, next);
+  } else {
+    const size_t s = (size_t)i * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN);
+    sh[s] = adam_update(sh[s], sgrad[s], m, ap->sh_lr, bc1, bc2);
+  }
+  moments[e] = m;
+}
+
+// src/shaders/adam.wgsl:74-77, one thread per raw float.
+__global__ void activate_kernel(const float* __restrict__ params, float* __restrict__ gaussians, uint32_t count) {
+  const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (uint64_t)count * FLOATS_PER_GAUSSIAN) return;
+  const uint32_t k = (uint32_t)(e % FLOATS_PER_GAUSSIAN);
+  if (k == 7 || k == 15) return;
+  gaussians[e] = activated(k, params[e]);
+}
+
+// src/shaders/adam.wgsl:112-121
+__global__ void reset_opacity_kernel(float* __restrict__ params, float2* __restrict__ moments,
+                                     float* __restrict__ gaussians, uint32_t count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const size_t at = (size_t)i * FLOATS_PER_GAUSSIAN + 3;
+  const float v = fminf(params[at], RESET_LOGIT);
+  params[at] = v;
+  moments[(size_t)i * MOMENT_SLOTS + RESET_SLOT] = make_float2(0.f, 0.f);
+  gaussians[at] = sigmoidf_(v);
+}
+
+// src/shaders/adam.wgsl:126-134
+__global__ void stats_kernel(const AdamParams* __restrict__ ap, const float* __restrict__ splats,
+                             const float* __restrict__ splat_grads, float4* __restrict__ stats, uint32_t count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float radius = splats[(size_t)i * FLOATS_PER_SPLAT + 3];
+  if (radius == 0.0f) return;
+  const float gx = splat_grads[(size_t)i * SPLAT_GRADS] * ap->viewport[0] * 0.5f;
+  const float gy = splat_grads[(size_t)i * SPLAT_GRADS + 1] * ap->viewport[1] * 0.5f;
+  const float len = sqrtf(gx * gx + gy * gy);
+  const float4 s = stats[i];
+  stats[i] = make_float4(s.x + len, s.y + 1.0f, fmaxf(s.z, radius), 0.0f);
+}
+
+// What happens to Gaussian i (src/shaders/densify.wgsl:72-85): 0 drop, 1 keep, 2 clone, 3 split.
+__device__ __forceinline__ uint32_t densify_action(const DensifyParams& dp, const float* __restrict__ params,
+                                                   const float4* __restrict__ stats, uint32_t i) {
+  const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
+  const float4 s = stats[i];
+  const float grad = s.y > 0.0f ? s.x / s.y : 0.0f;
+  const float size = expf(fmaxf(p[4], fmaxf(p[5], p[6])));
+  const float opacity = sigmoidf_(p[3]);
+  auto removed = [&](float o, float sz) { return o < dp.min_opacity || (dp.max_size > 0.0f && sz > dp.max_size); };
+  if (grad >= dp.grad_threshold) {
+    if (size <= dp.clone_max_size) return removed(opacity, size) ? 0u : 2u;
+    return removed(opacity, size / SPLIT_SHRINK) ? 0u : 3u;
+  }
+  return removed(opacity, size) ? 0u : 1u;
+}
+
+// src/shaders/densify.wgsl:96-107
+__global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, const float* __restrict__ params,
+                                                            const float4* __restrict__ stats, uint32_t count,
+                                                            uint32_t* __restrict__ outputs,
+                                                            uint32_t* __restrict__ counters) {
+  __shared__ uint32_t local[4];
+  if (threadIdx.x < 4) local[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t i = blockIdx.x * 256 + threadIdx.x;
+  if (i < count) {
+    const uint32_t a = densify_action(dp, params, stats, i);
+    outputs[i] = a == 0 ? 0u : (a >= 2 ? 2u : 1u);
+    atomicAdd(&local[a], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 4 && local[threadIdx.x]) atomicAdd(&counters[threadIdx.x], local[threadIdx.x]);
+}
+
+__device__ __forceinline__ uint32_t pcg(uint32_t v) {
+  const uint32_t state = v * 747796405u + 2891336453u;
+  const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+  return (word >> 22u) ^ word;
+}
+
+__device__ __forceinline__ float unit_of(uint32_t h) { return ((float)(h >> 8u) + 0.5f) / 16777216.0f; }
+
+// src/shaders/densify.wgsl:148-180, split in two for coalescing. This kernel runs
+// one thread per (Gaussian, moment slot) and copies the Adam moments (kept for a
+// kept Gaussian and a clone's original, zero for new ones), the raw parameters
+// and the SH coefficients; densify_place_kernel then places split children.
+__global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
+                                                           const float4* __restrict__ stats,
+                                                           const float* __restrict__ sh,
+                                                           const float2* __restrict__ moments,
+                                                           const uint32_t* __restrict__ outputs, uint32_t count,
+                                                           float* __restrict__ new_params, float* __restrict__ new_sh,
+                                                           float2* __restrict__ new_moments) {
+  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= count * MOMENT_SLOTS) return;
+  const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
+  const uint32_t a = densify_action(dp, params, stats, i);
+  if (a == 0) return;
+  const uint32_t o = outputs[i];
+  const uint32_t copies = a == 1 ? 1u : 2u;
+  const float2 m = moments[e];
+  const float2 zero = make_float2(0.f, 0.f);
+  float value = 0.0f;
+  if (k < FLOATS_PER_GAUSSIAN)
+    value = params[(size_t)i * FLOATS_PER_GAUSSIAN + k];
+  else
+    value = sh[(size_t)i * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)];
+  for (uint32_t c = 0; c < copies; c++) {
+    const uint32_t dst = o + c;
+    const bool keep = (a == 1 || a == 2) && c == 0;
+    new_moments[(size_t)dst * MOMENT_SLOTS + k] = keep ? m : zero;
+    if (k < FLOATS_PER_GAUSSIAN) {
+      float v = value;
+      if (a == 2 && c == 1) {
+        if (k == 7) v = 1.0f;
+        if (k == 15) v = (float)dp.seed;
+      }
+      if (a == 3) {
+        if (k >= 4 && k <= 6) v = value - LOG_SPLIT_SHRINK;
+        if (k == 7) v = 2.0f;
+        if (k == 15) v = (float)dp.seed;
+      }
+      new_params[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = v;
+    } else {
+      new_sh[(size_t)dst * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)] = value;
+    }
+  }
+}
+
+// Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and Box-Muller.
+__global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__ params,
+                                     const float4* __restrict__ stats, const uint32_t* __restrict__ outputs,
+                                     uint32_t count, float* __restrict__ new_params) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  if (densify_action(dp, params, stats, i) != 3) return;
+  const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
+  // rotation_matrix (src/shaders/gaussianMath.wgsl:13-25)
+  float dot = p[8] * p[8];
+  dot = dot + p[9] * p[9];
+  dot = dot + p[10] * p[10];
+  dot = dot + p[11] * p[11];
+  const float len = sqrtf(dot);
+  const float qw = p[8] / len, qx = p[9] / len, qy = p[10] / len, qz = p[11] / len;
+  float r[3][3];
+  r[0][0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+  r[0][1] = 2.0f * (qx * qy + qw * qz);
+  r[0][2] = 2.0f * (qx * qz - qw * qy);
+  r[1][0] = 2.0f * (qx * qy - qw * qz);
+  r[1][1] = 1.0f - 2.0f * (qx * qx + qz * qz);
+  r[1][2] = 2.0f * (qy * qz + qw * qx);
+  r[2][0] = 2.0f * (qx * qz + qw * qy);
+  r[2][1] = 2.0f * (qy * qz - qw * qx);
+  r[2][2] = 1.0f - 2.0f * (qx * qx + qy * qy);
+  const uint32_t o = outputs[i];
+  for (uint32_t c = 0; c < 2; c++) {
+    const uint32_t h1 = pcg(dp.seed ^ pcg(2u * i + c));
+    const uint32_t h2 = pcg(h1), h3 = pcg(h2), h4 = pcg(h3);
+    const float tau = 6.283185307179586f;
+    const float r1 = sqrtf(-2.0f * logf(unit_of(h1)));
+    const float r2 = sqrtf(-2.0f * logf(unit_of(h3)));
+    const float n0 = r1 * cosf(tau * unit_of(h2)), n1 = r1 * sinf(tau * unit_of(h2)), n2 = r2 * cosf(tau * unit_of(h4));
+    const float sv[3] = {expf(p[4]) * n0, expf(p[5]) * n1, expf(p[6]) * n2};
+    float* out = new_params + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      float v = r[0][row] * sv[0];
+      v = v + r[1][row] * sv[1];
+      v = v + r[2][row] * sv[2];
+      out[row] = p[row] + v;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace dg
+
+using namespace dg;
+
+// Trainer (src/trainer.ts:103-446).
+struct dg_trainer {
+  dg_context* ctx;
+  dg_training_settings settings;
+  struct View {
+    dg_camera camera;
+    dg_buffer* image;
+  };
+  std::vector<View> views;
+  uint32_t iteration = 0, sh_degree = 0, adam_steps = 0, count = 0;
+  dg_renderer* renderer = nullptr;
+  dg_training_loss* loss = nullptr;
+  dg_buffer* target = nullptr;  // the "training render" rgba8 texture
+  dg_buffer* params = nullptr;
+  dg_buffer* moments = nullptr;
+  dg_buffer* stats = nullptr;
+  dg_buffer* adam_params = nullptr;
+  uint32_t random_state = 1;  // mulberry32(1), src/trainer.ts:121
+  std::vector<uint32_t> queue;
+  bool due_densify = false, due_reset = false;
+  std::vector<dg_densification> densifications;
+  // The captured optimize() step.
+  bool graph_enabled = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_launches = 0;
+  struct Key {
+    uint32_t count, capacity;
+    void *gaussians, *pairs, *pixel_grads;
+    bool operator==(const Key& o) const {
+      return count == o.count && capacity == o.capacity && gaussians == o.gaussians && pairs == o.pairs &&
+             pixel_grads == o.pixel_grads;
+    }
+  } graph_key{};
+};
+
+namespace dg {
+
+static double mulberry32_next(uint32_t& state) {
+  state = state + 0x6d2b79f5u;
+  uint32_t t = state;
+  t = (t ^ (t >> 15)) * (t | 1u);
+  t ^= t + (t ^ (t >> 7)) * (t | 61u);
+  return (double)(t ^ (t >> 14)) / 4294967296.0;
+}
+
+// Every view once, in a random order, then reshuffle (src/trainer.ts:395-404).
+static uint32_t next_view(dg_trainer* t) {
+  if (t->queue.empty()) {
+    t->queue.resize(t->views.size());
+    for (uint32_t k = 0; k < t->views.size(); k++) t->queue[k] = k;
+    for (int64_t i = (int64_t)t->queue.size() - 1; i > 0; i--) {
+      int64_t j = (int64_t)std::floor(mulberry32_next(t->random_state) * (double)(i + 1));
+      std::swap(t->queue[i], t->queue[j]);
+    }
+  }
+  uint32_t v = t->queue.back();
+  t->queue.pop_back();
+  return v;
+}
+
+static dg_status launch_stats(dg_trainer* t) {
+  dg_renderer* r = t->renderer;
+  stats_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
+      typed<AdamParams>(t->adam_params), typed<float>(r->splats), typed<float>(r->grad_splats),
+      typed<float4>(t->stats), t->count);
+  t->ctx->launches++;
+  DG_LAUNCHED("stats");
+  return DG_OK;
+}
+
+static dg_status launch_adam(dg_trainer* t) {
+  dg_renderer* r = t->renderer;
+  const uint64_t elements = (uint64_t)t->count * MOMENT_SLOTS;
+  adam_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, t->ctx->stream>>>(
+      typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float>(r->sh), typed<float2>(t->moments),
+      typed<float>(r->grad_gaussians), typed<float>(r->grad_sh), typed<float>(r->gaussians), t->count);
+  t->ctx->launches++;
+  DG_LAUNCHED("adam");
+  return DG_OK;
+}
+
+// The kernels of one optimize() step, in order. Everything the host decides per
+// step (camera, photo, SH degree, learning rates) is in device uniforms written
+// before this runs, so the same launches can be captured once and replayed.
+static dg_status launch_step(dg_trainer* t, bool with_adam) {
+  dg_renderer* r = t->renderer;
+  DG_TRY(renderer_launch_forward(r, t->target));
+  DG_TRY(loss_launch(t->loss, r->rasterizer->pixel_color));
+  DG_TRY(renderer_launch_backward(r, t->loss->pixel_grads, true));
+  DG_TRY(launch_stats(t));
+  if (with_adam) DG_TRY(launch_adam(t));
+  // The frame's pair count, for afterSubmit (src/tileRasterizer.ts:187-191).
+  dg_tile_rasterizer* tr = r->rasterizer;
+  DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, t->ctx->stream));
+  return DG_OK;
+}
+
+static void drop_graph(dg_trainer* t) {
+  if (t->graph_exec) cudaGraphExecDestroy(t->graph_exec);
+  t->graph_exec = nullptr;
+}
+
+static dg_status run_graph_step(dg_trainer* t) {
+  dg_renderer* r = t->renderer;
+  dg_trainer::Key key{t->count, r->rasterizer->pair_capacity, r->gaussians->ptr, r->rasterizer->keys->ptr,
+                      t->loss->pixel_grads->ptr};
+  if (!t->graph_exec || !(key == t->graph_key)) {
+    drop_graph(t);
+    cudaGraph_t graph;
+    const uint64_t before = t->ctx->launches;
+    DG_CUDA(cudaStreamBeginCapture(t->ctx->stream, cudaStreamCaptureModeThreadLocal));
+    t->ctx->capturing = true;
+    dg_status st = launch_step(t, true);
+    t->ctx->capturing = false;
+    cudaError_t end = cudaStreamEndCapture(t->ctx->stream, &graph);
+    if (st != DG_OK) {
+      if (end == cudaSuccess) cudaGraphDestroy(graph);
+      return st;
+    }
+    DG_CUDA(end);
+    cudaError_t inst = cudaGraphInstantiate(&t->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    DG_CUDA(inst);
+    t->graph_key = key;
+    t->graph_launches = t->ctx->launches - before;
+    t->ctx->launches = before;
+  }
+  DG_CUDA(cudaGraphLaunch(t->graph_exec, t->ctx->stream));
+  t->ctx->launches += t->graph_launches;
+  return DG_OK;
+}
+
+static dg_status storage(dg_trainer* t, size_t bytes, dg_buffer** out) { return alloc_buffer(t->ctx, bytes, out); }
+
+}  // namespace dg
+
+extern "C" {
+
+void dg_training_settings_default(dg_training_settings* s, double extent) {
+  if (!s) return;
+  s->extent = extent;
+  s->position_lr_steps = 30000;
+  s->position_lr[0] = 0.00016;
+  s->position_lr[1] = 0.0000016;
+  s->opacity_lr = 0.025;
+  s->scale_lr = 0.005;
+  s->rotation_lr = 0.001;
+  s->color_lr = 0.0025;
+  s->sh_lr = 0.0025 / 20;
+  s->sh_degree_interval = 1000;
+  s->densify_from = 500;
+  s->densify_until = 15000;
+  s->densify_interval = 100;
+  s->densify_grad_threshold = 0.0002;
+  s->percent_dense = 0.01;
+  s->min_opacity = 0.005;
+  s->opacity_reset_interval = 3000;
+  s->background[0] = s->background[1] = s->background[2] = 0.0f;
+}
+
+dg_status dg_trainer_create(dg_context* ctx, const float* params, const float* sh, uint32_t count,
+                            const dg_training_view* views, uint32_t view_count, const dg_training_settings* settings,
+                            dg_trainer** out) {
+  DG_REQUIRE(ctx && params && sh && views && settings && out, "NULL argument");
+  DG_REQUIRE(view_count > 0, "no training views");
+  DG_REQUIRE(count > 0, "no Gaussians");
+  DG_REQUIRE(count < (1u << 26), "at most 2^26 Gaussians (Adam indexes slots with 32 bits)");
+  const float w = views[0].camera.viewport[0], h = views[0].camera.viewport[1];
+  for (uint32_t k = 0; k < view_count; k++)
+    if (views[k].camera.viewport[0] != w || views[k].camera.viewport[1] != h)
+      return fail(DG_ERROR_INVALID_ARGUMENT, "All training views must be the same size.");
+  for (uint32_t k = 0; k < view_count; k++)
+    DG_REQUIRE(views[k].image && views[k].image->bytes >= (uint64_t)w * h * 4, "a view's image is too small");
+  auto* t = new dg_trainer();
+  t->ctx = ctx;
+  t->settings = *settings;
+  for (uint32_t k = 0; k < view_count; k++) t->views.push_back({views[k].camera, views[k].image});
+  t->count = count;
+  // Activate on the host once, as the reference does (src/trainer.ts:138-140).
+  std::vector<float> act((size_t)count * FLOATS_PER_GAUSSIAN, 0.0f);
+  for (size_t at = 0; at < act.size(); at += FLOATS_PER_GAUSSIAN) {
+    for (int k = 0; k < 3; k++) {
+      act[at + k] = params[at + k];
+      act[at + 4 + k] = (float)std::exp((double)params[at + 4 + k]);
+      act[at + 12 + k] = (float)(0.5 + 0.28209479177387814 * (double)params[at + 12 + k]);
+    }
+    act[at + 3] = (float)(1.0 / (1.0 + std::exp(-(double)params[at + 3])));
+    for (int k = 8; k < 12; k++) act[at + k] = params[at + k];
+  }
+  dg_status st = dg_renderer_create(ctx, 0, &t->renderer);
+  if (st == DG_OK) st = dg_renderer_set_gaussians(t->renderer, act.data(), count, sh, (uint64_t)count * SH_REST_FLOATS, 0);
+  if (st == DG_OK) st = dg_training_loss_create(ctx, (uint32_t)w, (uint32_t)h, &t->loss);
+  if (st == DG_OK) st = storage(t, (size_t)w * h * 4, &t->target);
+  if (st == DG_OK) st = storage(t, (size_t)count * FLOATS_PER_GAUSSIAN * 4, &t->params);
+  if (st == DG_OK) st = write_async(ctx, t->params->ptr, params, (size_t)count * FLOATS_PER_GAUSSIAN * 4);
+  if (st == DG_OK) st = storage(t, (size_t)count * MOMENT_SLOTS * 8, &t->moments);
+  if (st == DG_OK) st = storage(t, (size_t)count * 16, &t->stats);
+  if (st == DG_OK) st = storage(t, sizeof(AdamParams), &t->adam_params);
+  if (st == DG_OK) st = renderer_ensure_gradients(t->renderer);
+  if (st != DG_OK) {
+    dg_trainer_destroy(t);
+    return st;
+  }
+  *out = t;
+  return DG_OK;
+}
+
+dg_status dg_trainer_optimize(dg_trainer* t) {
+  DG_REQUIRE(t, "NULL argument");
+  const dg_training_settings& s = t->settings;
+  const uint32_t it = ++t->iteration;
+  dg_renderer* r = t->renderer;
+  if (it % s.sh_degree_interval == 0 && t->sh_degree < 3) DG_TRY(dg_renderer_set_sh_degree(r, ++t->sh_degree));
+  const bool densifying = it < s.densify_until;
+  const bool densify_now = densifying && it > s.densify_from && it % s.densify_interval == 0;
+  const dg_trainer::View& view = t->views[next_view(t)];
+  // Uniforms of this step: camera, background, photo, learning rates.
+  DG_TRY(renderer_prepare(r, &view.camera, s.background));
+  const void* photo = view.image->ptr;
+  DG_TRY(write_async(t->ctx, t->loss->target_slot->ptr, &photo, sizeof(photo)));
+  if (!densify_now) t->adam_steps++;
+  const double progress = std::min(1.0, it / s.position_lr_steps);
+  const double position_lr =
+      std::exp(std::log(s.position_lr[0]) * (1 - progress) + std::log(s.position_lr[1]) * progress) * s.extent;
+  AdamParams ap{};
+  ap.bias_correction1 = (float)(1 - std::pow(0.9, t->adam_steps));
+  ap.bias_correction2 = (float)(1 - std::pow(0.999, t->adam_steps));
+  ap.position_lr = (float)position_lr;
+  ap.opacity_lr = (float)s.opacity_lr;
+  ap.scale_lr = (float)s.scale_lr;
+  ap.rotation_lr = (float)s.rotation_lr;
+  ap.color_lr = (float)s.color_lr;
+  ap.sh_lr = (float)s.sh_lr;
+  ap.viewport[0] = view.camera.viewport[0];
+  ap.viewport[1] = view.camera.viewport[1];
+  DG_TRY(write_async(t->ctx, t->adam_params->ptr, &ap, sizeof(ap)));
+  if (t->graph_enabled && !densify_now) {
+    DG_TRY(run_graph_step(t));
+  } else {
+    DG_TRY(launch_step(t, !densify_now));
+  }
+  dg_tile_rasterizer* tr = r->rasterizer;
+  DG_CUDA(cudaEventRecord(tr->readback_event, t->ctx->stream));
+  tr->readback_state = 1;
+  DG_TRY(dg_tile_rasterizer_after_submit(tr, 0));
+  t->due_densify = densify_now;
+  t->due_reset = densifying && it % s.opacity_reset_interval == 0;
+  return DG_OK;
+}
+
+dg_status dg_trainer_maintain(dg_trainer* t) {
+  DG_REQUIRE(t, "NULL argument");
+  const bool densify = t->due_densify, reset = t->due_reset;
+  t->due_densify = t->due_reset = false;
+  if (densify) DG_TRY(dg_trainer_densify(t, t->iteration > t->settings.opacity_reset_interval));
+  if (reset) DG_TRY(dg_trainer_reset_opacity(t));
+  return DG_OK;
+}
+
+dg_status dg_trainer_step(dg_trainer* t) {
+  DG_TRY(dg_trainer_optimize(t));
+  return dg_trainer_maintain(t);
+}
+
+dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
+  DG_REQUIRE(t, "NULL argument");
+  dg_context* ctx = t->ctx;
+  const dg_training_settings& s = t->settings;
+  const uint32_t count = t->count;
+  DensifyParams dp;
+  dp.grad_threshold = (float)s.densify_grad_threshold;
+  dp.clone_max_size = (float)(s.percent_dense * s.extent);
+  dp.min_opacity = (float)s.min_opacity;
+  dp.max_size = prune_large ? (float)(0.1 * s.extent) : 0.0f;
+  dp.seed = t->iteration;
+  dg_buffer *outputs = nullptr, *counters = nullptr, *scratch = nullptr;
+  DG_TRY(alloc_buffer(ctx, (size_t)count * 4 + 4, &outputs));  // + the scan total
+  DG_TRY(alloc_buffer(ctx, 16, &counters));
+  DG_TRY(alloc_buffer(ctx, scan_scratch_bytes(count), &scratch));
+  densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(dp, typed<float>(t->params),
+                                                                      typed<float4>(t->stats), count,
+                                                                      typed<uint32_t>(outputs),
+                                                                      typed<uint32_t>(counters));
+  ctx->launches++;
+  DG_LAUNCHED("densify_count");
+  uint32_t* total_ptr = typed<uint32_t>(outputs) + count;
+  DG_TRY(scan_launch(ctx, typed<uint32_t>(outputs), count, nullptr, total_ptr, scratch->ptr));
+  uint32_t readback[5];
+  DG_CUDA(cudaMemcpyAsync(readback, total_ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  DG_CUDA(cudaMemcpyAsync(readback + 1, counters->ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const uint32_t new_count = readback[0];
+  if (new_count == 0) {
+    free_buffer(outputs);
+    free_buffer(counters);
+    free_buffer(scratch);
+    return fail(DG_ERROR_STATE, "Densification removed every Gaussian.");
+  }
+  t->densifications.push_back(
+      {t->iteration, count, new_count, readback[2], readback[3], readback[4], readback[1]});
+  dg_buffer *params = nullptr, *sh = nullptr, *moments = nullptr, *stats = nullptr, *gaussians = nullptr;
+  DG_TRY(storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &params));
+  DG_TRY(storage(t, (size_t)new_count * SH_REST_FLOATS * 4, &sh));
+  DG_TRY(storage(t, (size_t)new_count * MOMENT_SLOTS * 8, &moments));
+  DG_TRY(storage(t, (size_t)new_count * 16, &stats));
+  DG_TRY(storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &gaussians));
+  dg_renderer* r = t->renderer;
+  const uint64_t elements = (uint64_t)count * MOMENT_SLOTS;
+  densify_copy_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, ctx->stream>>>(
+      dp, typed<float>(t->params), typed<float4>(t->stats), typed<float>(r->sh), typed<float2>(t->moments),
+      typed<uint32_t>(outputs), count, typed<float>(params), typed<float>(sh), typed<float2>(moments));
+  densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(dp, typed<float>(t->params),
+                                                                      typed<float4>(t->stats), typed<uint32_t>(outputs),
+                                                                      count, typed<float>(params));
+  const uint64_t floats = (uint64_t)new_count * FLOATS_PER_GAUSSIAN;
+  activate_kernel<<<(uint32_t)((floats + 255) / 256), 256, 0, ctx->stream>>>(typed<float>(params),
+                                                                             typed<float>(gaussians), new_count);
+  ctx->launches += 3;
+  DG_LAUNCHED("densify scatter");
+  // Hand the new set to the renderer; the old buffers go once the work above is done.
+  drop_graph(t);
+  DG_TRY(dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree));
+  DG_TRY(renderer_ensure_gradients(r));
+  for (dg_buffer* b : {t->params, t->moments, t->stats, outputs, counters, scratch}) free_buffer(b);
+  t->params = params;
+  t->moments = moments;
+  t->stats = stats;
+  t->count = new_count;
+  return DG_OK;
+}
+
+dg_status dg_trainer_reset_opacity(dg_trainer* t) {
+  DG_REQUIRE(t, "NULL argument");
+  reset_opacity_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
+      typed<float>(t->params), typed<float2>(t->moments), typed<float>(t->renderer->gaussians), t->count);
+  t->ctx->launches++;
+  DG_LAUNCHED("reset_opacity");
+  return DG_OK;
+}
+
+dg_status dg_trainer_export_raw(dg_trainer* t, float* params, float* sh) {
+  DG_REQUIRE(t && params && sh, "NULL argument");
+  DG_CUDA(cudaMemcpyAsync(params, t->params->ptr, (size_t)t->count * FLOATS_PER_GAUSSIAN * 4, cudaMemcpyDeviceToHost,
+                          t->ctx->stream));
+  DG_CUDA(cudaMemcpyAsync(sh, t->renderer->sh->ptr, (size_t)t->count * SH_REST_FLOATS * 4, cudaMemcpyDeviceToHost,
+                          t->ctx->stream));
+  DG_CUDA(cudaStreamSynchronize(t->ctx->stream));
+  return DG_OK;
+}
+
+dg_status dg_trainer_last_loss(dg_trainer* t, double* out) {
+  DG_REQUIRE(t && out, "NULL argument");
+  return dg_training_loss_read(t->loss, out);
+}
+
+dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint32_t view_count, int32_t with_ssim,
+                              double* psnr, double* ssim) {
+  DG_REQUIRE(t && views && psnr && ssim, "NULL argument");
+  DG_REQUIRE(view_count > 0, "no views");
+  dg_context* ctx = t->ctx;
+  dg_buffer *sums = nullptr, *slot = nullptr;
+  DG_TRY(alloc_buffer(ctx, view_count * 16, &sums));
+  DG_TRY(alloc_buffer(ctx, 8 * view_count, &slot));
+  std::vector<const void*> photos(view_count);
+  for (uint32_t k = 0; k < view_count; k++) photos[k] = views[k].image->ptr;
+  DG_TRY(write_async(ctx, slot->ptr, photos.data(), 8 * view_count));
+  for (uint32_t k = 0; k < view_count; k++) {
+    const dg_camera& cam = views[k].camera;
+    DG_TRY(dg_renderer_encode(t->renderer, t->target, &cam, t->settings.background));
+    dg_buffer view_slot{ctx, static_cast<char*>(slot->ptr) + 8 * k, 8, false};
+    DG_TRY(metrics_launch(ctx, t->renderer->rasterizer->pixel_color, &view_slot, (uint32_t)cam.viewport[0],
+                          (uint32_t)cam.viewport[1], typed<double>(sums) + 2 * k));
+  }
+  std::vector<double> host(2 * view_count);
+  DG_CUDA(cudaMemcpyAsync(host.data(), sums->ptr, 16 * view_count, cudaMemcpyDeviceToHost, ctx->stream));
+  DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  double psnr_total = 0, ssim_total = 0;
+  for (uint32_t k = 0; k < view_count; k++) {
+    const double pixels = (double)(uint32_t)views[k].camera.viewport[0] * (uint32_t)views[k].camera.viewport[1];
+    psnr_total += 10.0 * std::log10(1.0 / (host[2 * k + 1] / (3.0 * pixels)));
+    ssim_total += host[2 * k] / (3.0 * pixels);
+  }
+  free_buffer(sums);
+  free_buffer(slot);
+  *psnr = psnr_total / view_count;
+  *ssim = with_ssim ? ssim_total / view_count : NAN;
+  return DG_OK;
+}
+
+uint32_t dg_trainer_iteration(const dg_trainer* t) { return t ? t->iteration : 0; }
+dg_status dg_trainer_set_iteration(dg_trainer* t, uint32_t iteration) {
+  DG_REQUIRE(t, "NULL argument");
+  t->iteration = iteration;
+  return DG_OK;
+}
+uint32_t dg_trainer_sh_degree(const dg_trainer* t) { return t ? t->sh_degree : 0; }
+uint32_t dg_trainer_count(const dg_trainer* t) { return t ? t->count : 0; }
+dg_renderer* dg_trainer_renderer(dg_trainer* t) { return t ? t->renderer : nullptr; }
+dg_buffer* dg_trainer_params(dg_trainer* t) { return t ? t->params : nullptr; }
+dg_buffer* dg_trainer_moments(dg_trainer* t) { return t ? t->moments : nullptr; }
+dg_buffer* dg_trainer_stats(dg_trainer* t) { return t ? t->stats : nullptr; }
+uint32_t dg_trainer_densification_count(const dg_trainer* t) { return t ? (uint32_t)t->densifications.size() : 0; }
+dg_status dg_trainer_densification(const dg_trainer* t, uint32_t index, dg_densification* out) {
+  DG_REQUIRE(t && out, "NULL argument");
+  DG_REQUIRE(index < t->densifications.size(), "no such densification");
+  *out = t->densifications[index];
+  return DG_OK;
+}
+
+dg_status dg_trainer_set_graph(dg_trainer* t, int32_t enabled) {
+  DG_REQUIRE(t, "NULL argument");
+  t->graph_enabled = enabled != 0;
+  if (!t->graph_enabled) drop_graph(t);
+  return DG_OK;
+}
+
+dg_status dg_trainer_destroy(dg_trainer* t) {
+  if (!t) return DG_OK;
+  if (t->ctx) cudaStreamSynchronize(t->ctx->stream);
+  drop_graph(t);
+  dg_renderer_destroy(t->renderer);
+  dg_training_loss_destroy(t->loss);
+  for (dg_buffer* b : {t->target, t->params, t->moments, t->stats, t->adam_params}) free_buffer(b);
+  delete t;
+  return DG_OK;
+}
+
+}  // extern "C"

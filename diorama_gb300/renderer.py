@@ -1,0 +1,211 @@
+"""GaussianRenderer (src/gaussianRenderer.ts) and TileRasterizer
+(src/tileRasterizer.ts) over the C ABI. Method names and argument meanings are
+the reference's; `encoder` arguments are accepted for the same call shape (work
+is enqueued on the device's stream as it is encoded)."""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .gaussians import FLOATS_PER_GAUSSIAN, SH_REST_FLOATS
+from .gpu import Buffer, Device, Texture, borrowed
+
+
+@dataclass
+class CameraData:
+    """src/gaussianRenderer.ts:11-15: column-major view and proj, viewport in pixels."""
+
+    view: list
+    proj: list
+    viewport: tuple
+
+    def to_c(self) -> _lib.Camera:
+        cam = _lib.Camera()
+        cam.view[:] = [float(v) for v in self.view]
+        cam.proj[:] = [float(v) for v in self.proj]
+        cam.viewport[:] = [float(self.viewport[0]), float(self.viewport[1])]
+        return cam
+
+
+@dataclass
+class SphericalHarmonics:
+    rest: np.ndarray
+    degree: int
+
+
+def _target_handle(target):
+    if target is None:
+        return None
+    if isinstance(target, Texture):
+        return target.buffer.handle
+    return target.handle
+
+
+class TileRasterizer:
+    """Tiles, sorts and blends `count` 2D splats from `splats`, reading the
+    viewport from `camera` (a buffer holding the 144-byte Camera uniform)."""
+
+    def __init__(self, device: Device, camera: Buffer, splats: Buffer, count: int, initialPairCapacity: int | None = None,
+                 *, _handle=None):
+        self.device = device
+        if _handle is None:
+            handle = c_void_p()
+            _lib.call("dg_tile_rasterizer_create", device.handle, camera.handle, splats.handle, count,
+                      initialPairCapacity or 0, ctypes.byref(handle))
+            self.handle, self.owned = handle, True
+        else:
+            self.handle, self.owned = c_void_p(_handle), False
+
+    @property
+    def lastPairCount(self) -> int:
+        return int(_lib.fn("dg_tile_rasterizer_last_pair_count")(self.handle))
+
+    @property
+    def pairCapacity(self) -> int:
+        return int(_lib.fn("dg_tile_rasterizer_pair_capacity")(self.handle))
+
+    @property
+    def debugBuffers(self) -> dict:
+        return {
+            "pairSplats": borrowed(self.device, _lib.fn("dg_tile_rasterizer_pair_splats")(self.handle)),
+            "ranges": borrowed(self.device, _lib.fn("dg_tile_rasterizer_ranges")(self.handle)),
+            "pairKeys": borrowed(self.device, _lib.fn("dg_tile_rasterizer_pair_keys")(self.handle)),
+            "tileOffsets": borrowed(self.device, _lib.fn("dg_tile_rasterizer_tile_offsets")(self.handle)),
+            "pairTotal": borrowed(self.device, _lib.fn("dg_tile_rasterizer_pair_total")(self.handle)),
+        }
+
+    @property
+    def pixelColor(self) -> Buffer | None:
+        return borrowed(self.device, _lib.fn("dg_tile_rasterizer_pixel_color")(self.handle))
+
+    @property
+    def pixelLast(self) -> Buffer | None:
+        return borrowed(self.device, _lib.fn("dg_tile_rasterizer_pixel_last")(self.handle))
+
+    def encode(self, encoder, target, viewport, background) -> None:
+        _lib.call("dg_tile_rasterizer_encode", self.handle, _target_handle(target), _lib.floats(viewport),
+                  _lib.floats(background))
+
+    def encodeBackward(self, encoder, viewport, pixelGrads: Buffer, splatGrads: Buffer) -> None:
+        _lib.call("dg_tile_rasterizer_encode_backward", self.handle, _lib.floats(viewport), pixelGrads.handle,
+                  splatGrads.handle)
+
+    def afterSubmit(self, wait: bool = True) -> None:
+        """Reads back the last frame's pair count and grows the pair buffers if it
+        did not fit. Blocks until that frame is done unless wait is False."""
+        _lib.call("dg_tile_rasterizer_after_submit", self.handle, int(wait))
+
+    def destroy(self) -> None:
+        if self.owned and self.handle:
+            _lib.call("dg_tile_rasterizer_destroy", self.handle)
+        self.handle = None
+
+
+class GaussianRenderer:
+    """Projects 3D Gaussians to 2D splats, then tiles, sorts and blends them; the
+    backward pass turns dL/d(pixel colour) into gradients of every parameter."""
+
+    def __init__(self, device: Device, options: dict | None = None, *, initialPairCapacity: int | None = None,
+                 _handle=None):
+        self.device = device
+        options = options or {}
+        capacity = initialPairCapacity or options.get("initialPairCapacity") or 0
+        if _handle is None:
+            handle = c_void_p()
+            _lib.call("dg_renderer_create", device.handle, capacity, ctypes.byref(handle))
+            self.handle, self.owned = handle, True
+        else:
+            self.handle, self.owned = c_void_p(_handle), False
+
+    def setGaussians(self, data, sh: SphericalHarmonics | dict | None = None) -> None:
+        arr = np.ascontiguousarray(data, np.float32).reshape(-1)
+        count = arr.size // FLOATS_PER_GAUSSIAN
+        rest, degree = None, 0
+        if sh is not None:
+            rest = sh.rest if isinstance(sh, SphericalHarmonics) else sh["rest"]
+            degree = sh.degree if isinstance(sh, SphericalHarmonics) else sh["degree"]
+            rest = np.ascontiguousarray(rest, np.float32).reshape(-1)
+        _lib.call("dg_renderer_set_gaussians", self.handle, arr.ctypes.data if count else None, count,
+                  rest.ctypes.data if rest is not None else None, rest.size if rest is not None else 0, degree)
+
+    def adoptGaussians(self, count: int, gaussians: Buffer, sh: Buffer, degree: int) -> None:
+        _lib.call("dg_renderer_adopt_gaussians", self.handle, count, gaussians.handle, sh.handle, degree)
+        gaussians.owned = False  # the renderer owns them now
+        sh.owned = False
+
+    def setShDegree(self, degree: int) -> None:
+        _lib.call("dg_renderer_set_sh_degree", self.handle, degree)
+
+    @property
+    def count(self) -> int:
+        return int(_lib.fn("dg_renderer_count")(self.handle))
+
+    def _buffer(self, name: str) -> Buffer | None:
+        return borrowed(self.device, _lib.fn(name)(self.handle))
+
+    @property
+    def splatBuffer(self) -> Buffer | None:
+        return self._buffer("dg_renderer_splat_buffer")
+
+    @property
+    def gaussianBuffer(self) -> Buffer | None:
+        return self._buffer("dg_renderer_gaussian_buffer")
+
+    @property
+    def shBuffer(self) -> Buffer | None:
+        return self._buffer("dg_renderer_sh_buffer")
+
+    @property
+    def pixelBuffer(self) -> Buffer | None:
+        return self._buffer("dg_renderer_pixel_buffer")
+
+    @property
+    def pixelLastBuffer(self) -> Buffer | None:
+        return self._buffer("dg_renderer_pixel_last_buffer")
+
+    @property
+    def gradients(self) -> dict | None:
+        g = self._buffer("dg_renderer_gradient_gaussians")
+        if g is None:
+            return None
+        return {"gaussians": g, "sh": self._buffer("dg_renderer_gradient_sh"),
+                "splats": self._buffer("dg_renderer_gradient_splats")}
+
+    @property
+    def tiles(self) -> TileRasterizer | None:
+        h = _lib.fn("dg_renderer_tiles")(self.handle)
+        return TileRasterizer(self.device, None, None, 0, _handle=h) if h else None
+
+    @property
+    def drawTiles(self) -> TileRasterizer | None:
+        h = _lib.fn("dg_renderer_draw_tiles")(self.handle)
+        return TileRasterizer(self.device, None, None, 0, _handle=h) if h else None
+
+    def encode(self, encoder, target, camera: CameraData, background) -> None:
+        cam = camera.to_c()
+        _lib.call("dg_renderer_encode", self.handle, _target_handle(target), ctypes.byref(cam),
+                  _lib.floats(background))
+
+    def encodeDraw(self, encoder, target, splats: Buffer, count: int, viewport, background) -> None:
+        _lib.call("dg_renderer_encode_draw", self.handle, _target_handle(target), splats.handle, count,
+                  _lib.floats(viewport), _lib.floats(background))
+
+    def encodeBackward(self, encoder, pixelGrads: Buffer) -> None:
+        _lib.call("dg_renderer_encode_backward", self.handle, pixelGrads.handle)
+
+    def afterSubmit(self, wait: bool = True) -> None:
+        _lib.call("dg_renderer_after_submit", self.handle, int(wait))
+
+    def destroy(self) -> None:
+        if self.owned and self.handle:
+            _lib.call("dg_renderer_destroy", self.handle)
+        self.handle = None
+
+
+def shRestFloats(count: int) -> int:
+    return count * SH_REST_FLOATS

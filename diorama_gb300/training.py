@@ -1,0 +1,232 @@
+"""TrainingLoss (src/trainingLoss.ts) and Trainer (src/trainer.ts) over the C ABI."""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from ctypes import c_double, c_void_p
+from dataclasses import dataclass, field, fields, replace
+
+import numpy as np
+
+from . import _lib
+from .gaussians import FLOATS_PER_GAUSSIAN, SH_REST_FLOATS
+from .gpu import Buffer, Device, Texture, borrowed
+from .renderer import CameraData, GaussianRenderer
+
+SH_C0 = 0.28209479177387814
+MOMENT_SLOTS = FLOATS_PER_GAUSSIAN + SH_REST_FLOATS
+
+
+class TrainingLoss:
+    """0.8 x L1 + 0.2 x (1 - SSIM) between a render and a photo, and its gradient."""
+
+    def __init__(self, device: Device, width: int, height: int):
+        self.device = device
+        self.width = width
+        self.height = height
+        handle = c_void_p()
+        _lib.call("dg_training_loss_create", device.handle, width, height, ctypes.byref(handle))
+        self.handle = handle
+        self.pixelGrads = borrowed(device, _lib.fn("dg_training_loss_pixel_grads")(handle))
+        self.pixelLoss = borrowed(device, _lib.fn("dg_training_loss_pixel_loss")(handle))
+
+    def encode(self, encoder, rendered: Buffer, target) -> None:
+        t = target.buffer if isinstance(target, Texture) else target
+        _lib.call("dg_training_loss_encode", self.handle, rendered.handle, t.handle)
+
+    def read(self) -> float:
+        out = c_double()
+        _lib.call("dg_training_loss_read", self.handle, ctypes.byref(out))
+        return out.value
+
+    def destroy(self) -> None:
+        if self.handle:
+            _lib.call("dg_training_loss_destroy", self.handle)
+            self.handle = None
+
+
+@dataclass
+class TrainingSettings:
+    """src/trainer.ts:37-63; the defaults are DEFAULT_SETTINGS (src/trainer.ts:65-82)."""
+
+    extent: float = 1.0
+    positionLrSteps: float = 30_000
+    positionLr: tuple = (0.00016, 0.0000016)
+    opacityLr: float = 0.025
+    scaleLr: float = 0.005
+    rotationLr: float = 0.001
+    colorLr: float = 0.0025
+    shLr: float = 0.0025 / 20
+    shDegreeInterval: int = 1000
+    densifyFrom: int = 500
+    densifyUntil: int = 15_000
+    densifyInterval: int = 100
+    densifyGradThreshold: float = 0.0002
+    percentDense: float = 0.01
+    minOpacity: float = 0.005
+    opacityResetInterval: int = 3000
+    background: tuple = (0.0, 0.0, 0.0)
+
+    def to_c(self) -> _lib.TrainingSettingsC:
+        s = _lib.TrainingSettingsC()
+        s.extent = self.extent
+        s.position_lr_steps = self.positionLrSteps
+        s.position_lr[:] = list(self.positionLr)
+        s.opacity_lr = self.opacityLr
+        s.scale_lr = self.scaleLr
+        s.rotation_lr = self.rotationLr
+        s.color_lr = self.colorLr
+        s.sh_lr = self.shLr
+        s.sh_degree_interval = self.shDegreeInterval
+        s.densify_from = self.densifyFrom
+        s.densify_until = self.densifyUntil
+        s.densify_interval = self.densifyInterval
+        s.densify_grad_threshold = self.densifyGradThreshold
+        s.percent_dense = self.percentDense
+        s.min_opacity = self.minOpacity
+        s.opacity_reset_interval = self.opacityResetInterval
+        s.background[:] = list(self.background)
+        return s
+
+
+DEFAULT_SETTINGS = TrainingSettings()
+
+
+@dataclass
+class TrainingView:
+    name: str
+    camera: CameraData
+    image: Texture
+
+
+@dataclass
+class RawGaussians:
+    params: np.ndarray
+    sh: np.ndarray
+
+
+@dataclass
+class Densification:
+    step: int
+    before: int
+    after: int
+    kept: int
+    cloned: int
+    split: int
+    removed: int
+
+
+def activate(params) -> np.ndarray:
+    """Raw parameters to the renderer's activated layout (src/trainer.ts:449-461), on the host."""
+    p = np.asarray(params, np.float64).reshape(-1, FLOATS_PER_GAUSSIAN)
+    out = np.zeros_like(p)
+    out[:, 0:3] = p[:, 0:3]
+    out[:, 4:7] = np.exp(p[:, 4:7])
+    out[:, 12:15] = 0.5 + SH_C0 * p[:, 12:15]
+    out[:, 3] = 1 / (1 + np.exp(-p[:, 3]))
+    out[:, 8:12] = p[:, 8:12]
+    return out.astype(np.float32).reshape(-1)
+
+
+def _views_c(views) -> ctypes.Array:
+    arr = (_lib.TrainingViewC * len(views))()
+    for k, v in enumerate(views):
+        arr[k].camera = v.camera.to_c()
+        image = v.image.buffer if isinstance(v.image, Texture) else v.image
+        arr[k].image = image.handle.value if isinstance(image.handle, c_void_p) else image.handle
+    return arr
+
+
+class Trainer:
+    """Trains Gaussians to match a set of photos, following the reference's loop."""
+
+    def __init__(self, device: Device, raw: RawGaussians, views, settings: TrainingSettings):
+        self.device = device
+        self.views = list(views)
+        self.settings = settings
+        params = np.ascontiguousarray(raw.params, np.float32).reshape(-1)
+        sh = np.ascontiguousarray(raw.sh, np.float32).reshape(-1)
+        count = params.size // FLOATS_PER_GAUSSIAN
+        if sh.size != count * SH_REST_FLOATS:
+            raise ValueError(f"Expected {count * SH_REST_FLOATS} spherical-harmonic floats, got {sh.size}.")
+        self._views_c = _views_c(self.views)
+        cs = settings.to_c()
+        handle = c_void_p()
+        _lib.call("dg_trainer_create", device.handle, params.ctypes.data, sh.ctypes.data, count, self._views_c,
+                  len(self.views), ctypes.byref(cs), ctypes.byref(handle))
+        self.handle = handle
+        self.renderer = GaussianRenderer(device, _handle=_lib.fn("dg_trainer_renderer")(handle))
+
+    @property
+    def iteration(self) -> int:
+        return int(_lib.fn("dg_trainer_iteration")(self.handle))
+
+    @iteration.setter
+    def iteration(self, value: int) -> None:
+        _lib.call("dg_trainer_set_iteration", self.handle, value)
+
+    @property
+    def shDegree(self) -> int:
+        return int(_lib.fn("dg_trainer_sh_degree")(self.handle))
+
+    @property
+    def count(self) -> int:
+        return int(_lib.fn("dg_trainer_count")(self.handle))
+
+    @property
+    def buffers(self) -> dict:
+        b = lambda name: borrowed(self.device, _lib.fn(name)(self.handle))  # noqa: E731
+        return {"params": b("dg_trainer_params"), "moments": b("dg_trainer_moments"), "stats": b("dg_trainer_stats")}
+
+    @property
+    def densifications(self) -> list[Densification]:
+        out = []
+        for k in range(int(_lib.fn("dg_trainer_densification_count")(self.handle))):
+            d = _lib.DensificationC()
+            _lib.call("dg_trainer_densification", self.handle, k, ctypes.byref(d))
+            out.append(Densification(d.step, d.before, d.after, d.kept, d.cloned, d.split, d.removed))
+        return out
+
+    def step(self) -> None:
+        _lib.call("dg_trainer_step", self.handle)
+
+    def optimize(self) -> None:
+        _lib.call("dg_trainer_optimize", self.handle)
+
+    def maintain(self) -> None:
+        _lib.call("dg_trainer_maintain", self.handle)
+
+    def densify(self, pruneLarge: bool) -> None:
+        _lib.call("dg_trainer_densify", self.handle, int(pruneLarge))
+
+    def resetOpacity(self) -> None:
+        _lib.call("dg_trainer_reset_opacity", self.handle)
+
+    def exportRaw(self) -> RawGaussians:
+        n = self.count
+        params = np.empty(n * FLOATS_PER_GAUSSIAN, np.float32)
+        sh = np.empty(n * SH_REST_FLOATS, np.float32)
+        _lib.call("dg_trainer_export_raw", self.handle, params.ctypes.data, sh.ctypes.data)
+        return RawGaussians(params, sh)
+
+    def lastLoss(self) -> float:
+        out = c_double()
+        _lib.call("dg_trainer_last_loss", self.handle, ctypes.byref(out))
+        return out.value
+
+    def evaluate(self, views, withSsim: bool = True) -> dict:
+        arr = _views_c(views)
+        psnr, ssim = c_double(), c_double()
+        _lib.call("dg_trainer_evaluate", self.handle, arr, len(views), int(withSsim), ctypes.byref(psnr),
+                  ctypes.byref(ssim))
+        return {"psnr": psnr.value, "ssim": ssim.value}
+
+    def setGraph(self, enabled: bool) -> None:
+        """Replay each optimize() step as one captured CUDA graph."""
+        _lib.call("dg_trainer_set_graph", self.handle, int(enabled))
+
+    def destroy(self) -> None:
+        if self.handle:
+            _lib.call("dg_trainer_destroy", self.handle)
+            self.handle = None

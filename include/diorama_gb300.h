@@ -1,0 +1,241 @@
+/*
+ * diorama_gb300: the C ABI of a GB300-native 3D Gaussian Splatting renderer and
+ * trainer that stands in for seanfourman/diorama's WebGPU path.
+ *
+ * Every entry point returns a dg_status (0 = DG_OK). On failure,
+ * dg_last_error() returns a message for the calling thread. Objects are opaque
+ * handles; sizes are plain integers; no entry point takes a framework type.
+ *
+ * The model the reference's TypeScript classes assume is kept:
+ *   - A dg_context is the GPUDevice plus its queue: one CUDA device and one
+ *     in-order stream. "encode" entry points enqueue work on that stream right
+ *     away; the work runs in call order, as a WebGPU queue runs submissions.
+ *   - dg_buffer stands in for GPUBuffer (rgba8unorm textures become byte
+ *     buffers of width*height*4). Objects own the buffers they create and free
+ *     them in their destroy entry point; "adopt" entry points take ownership.
+ *   - Readbacks (dg_buffer_read, *_read, *_after_submit with wait) block until
+ *     the work before them is done, like awaiting mapAsync.
+ * Each declaration names the reference interface it replaces (path:line in the
+ * reference project).
+ */
+#ifndef DIORAMA_GB300_H
+#define DIORAMA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t dg_status;
+#define DG_OK 0
+#define DG_ERROR_INVALID_ARGUMENT 1 /* a throw new Error(...) in the reference */
+#define DG_ERROR_CUDA 2             /* the CUDA runtime failed */
+#define DG_ERROR_OUT_OF_MEMORY 3
+#define DG_ERROR_DEVICE_WAIT 4 /* a bounded wait on the GPU gave up (see dg_context_check) */
+#define DG_ERROR_STATE 5       /* e.g. a backward pass before any forward pass */
+
+typedef struct dg_context dg_context;
+typedef struct dg_buffer dg_buffer;
+typedef struct dg_prefix_sum dg_prefix_sum;
+typedef struct dg_radix_sort dg_radix_sort;
+typedef struct dg_tile_rasterizer dg_tile_rasterizer;
+typedef struct dg_renderer dg_renderer;
+typedef struct dg_training_loss dg_training_loss;
+typedef struct dg_trainer dg_trainer;
+
+/* CameraData (src/gaussianRenderer.ts:11-15): column-major view and proj, viewport in pixels. */
+typedef struct dg_camera {
+  float view[16];
+  float proj[16];
+  float viewport[2];
+} dg_camera;
+
+/* ---- errors and version */
+const char* dg_last_error(void);
+int32_t dg_abi_version(void);
+
+/* ---- context: GPUDevice + queue (src/gpu.ts:8-46) */
+dg_status dg_context_create(int32_t device, dg_context** out);
+dg_status dg_context_destroy(dg_context* ctx);
+/* queue.onSubmittedWorkDone(): waits for everything enqueued so far. */
+dg_status dg_context_synchronize(dg_context* ctx);
+/* Reads and clears the device error word that bounded GPU waits set instead of
+ * hanging; returns DG_ERROR_DEVICE_WAIT if any bit was set (bits in *bits). */
+dg_status dg_context_check(dg_context* ctx, uint32_t* bits);
+/* Number of kernels this library has launched through ctx (for launch accounting). */
+dg_status dg_context_launch_count(dg_context* ctx, uint64_t* out);
+
+/* ---- buffers: device.createBuffer, queue.writeBuffer, readBuffer (src/readback.ts),
+ *      encoder.clearBuffer, encoder.copyBufferToBuffer. New buffers are zero-filled. */
+dg_status dg_buffer_create(dg_context* ctx, uint64_t bytes, dg_buffer** out);
+/* Wraps device memory the caller owns; dg_buffer_destroy then only drops the handle. */
+dg_status dg_buffer_wrap(dg_context* ctx, void* device_ptr, uint64_t bytes, dg_buffer** out);
+dg_status dg_buffer_destroy(dg_buffer* buffer);
+uint64_t dg_buffer_size(const dg_buffer* buffer);
+void* dg_buffer_device_pointer(const dg_buffer* buffer);
+dg_status dg_buffer_write(dg_buffer* buffer, uint64_t offset, const void* src, uint64_t bytes);
+dg_status dg_buffer_read(dg_buffer* buffer, uint64_t offset, void* dst, uint64_t bytes);
+dg_status dg_buffer_clear(dg_buffer* buffer, uint64_t offset, uint64_t bytes);
+dg_status dg_buffer_copy(dg_buffer* src, uint64_t src_offset, dg_buffer* dst, uint64_t dst_offset, uint64_t bytes);
+
+/* ---- PrefixSum (src/prefixSum.ts:10-103): exclusive u32 scan of data, in place.
+ * count (nullable) holds in element 0 how many values to scan, at most capacity. */
+dg_status dg_prefix_sum_create(dg_context* ctx, dg_buffer* data, uint32_t capacity, dg_buffer* count,
+                               dg_prefix_sum** out);
+dg_status dg_prefix_sum_encode(dg_prefix_sum* scan);
+/* .total: element 0 holds the sum once the scan has run. */
+dg_buffer* dg_prefix_sum_total(dg_prefix_sum* scan);
+dg_status dg_prefix_sum_destroy(dg_prefix_sum* scan);
+
+/* ---- RadixSort (src/radixSort.ts:27-142): stable LSD sort of u32 keys (high_bits = 0)
+ * or u64 keys stored as (low word, high word) sorting high_bits bits of the high word,
+ * each key carrying a u32 value. Sorted in place in .keys / .values. */
+dg_status dg_radix_sort_create(dg_context* ctx, uint32_t capacity, uint32_t high_bits, dg_buffer* count,
+                               dg_radix_sort** out);
+dg_buffer* dg_radix_sort_keys(dg_radix_sort* sort);
+dg_buffer* dg_radix_sort_values(dg_radix_sort* sort);
+uint32_t dg_radix_sort_capacity(const dg_radix_sort* sort);
+dg_status dg_radix_sort_encode(dg_radix_sort* sort);
+dg_status dg_radix_sort_destroy(dg_radix_sort* sort);
+
+/* ---- TileRasterizer (src/tileRasterizer.ts:29-317). camera is a buffer holding the
+ * 144-byte Camera uniform; splats FLOATS_PER_SPLAT floats each. initial_pair_capacity
+ * 0 picks max(2^16, 8*count) as the reference does. */
+dg_status dg_tile_rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
+                                    uint32_t initial_pair_capacity, dg_tile_rasterizer** out);
+/* target: rgba8 bytes (width*height*4), may be NULL. */
+dg_status dg_tile_rasterizer_encode(dg_tile_rasterizer* tr, dg_buffer* target, const float viewport[2],
+                                    const float background[3]);
+dg_status dg_tile_rasterizer_encode_backward(dg_tile_rasterizer* tr, const float viewport[2],
+                                             dg_buffer* pixel_grads, dg_buffer* splat_grads);
+/* afterSubmit(): reads back the last frame's pair count and grows the pair buffers
+ * to 2^ceil(log2(1.25 * pairs)) if it did not fit. wait = 0 returns at once if the
+ * frame has not finished. */
+dg_status dg_tile_rasterizer_after_submit(dg_tile_rasterizer* tr, int32_t wait);
+uint32_t dg_tile_rasterizer_last_pair_count(const dg_tile_rasterizer* tr);
+uint32_t dg_tile_rasterizer_pair_capacity(const dg_tile_rasterizer* tr);
+dg_buffer* dg_tile_rasterizer_pair_splats(dg_tile_rasterizer* tr); /* debugBuffers.pairSplats */
+dg_buffer* dg_tile_rasterizer_ranges(dg_tile_rasterizer* tr);      /* debugBuffers.ranges */
+dg_buffer* dg_tile_rasterizer_pair_keys(dg_tile_rasterizer* tr);   /* sorted (depth, tile) keys */
+dg_buffer* dg_tile_rasterizer_pixel_color(dg_tile_rasterizer* tr); /* .pixelColor, vec4 per pixel */
+dg_buffer* dg_tile_rasterizer_pixel_last(dg_tile_rasterizer* tr);  /* .pixelLast, u32 per pixel */
+dg_buffer* dg_tile_rasterizer_tile_offsets(dg_tile_rasterizer* tr);/* scanned per-splat first pair slots */
+dg_buffer* dg_tile_rasterizer_pair_total(dg_tile_rasterizer* tr);  /* element 0: pairs the last frame needed */
+dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr);
+
+/* ---- GaussianRenderer (src/gaussianRenderer.ts:55-311) */
+dg_status dg_renderer_create(dg_context* ctx, uint32_t initial_pair_capacity, dg_renderer** out);
+/* setGaussians(data, {rest, degree}): count Gaussians of 16 floats; sh_rest may be NULL
+ * (then sh_floats must be 0); otherwise sh_floats must equal 45 * count. count 0 clears. */
+dg_status dg_renderer_set_gaussians(dg_renderer* r, const float* data, uint32_t count, const float* sh_rest,
+                                    uint64_t sh_floats, uint32_t degree);
+/* adoptGaussians(count, gaussians, sh, degree): takes ownership of both buffers. */
+dg_status dg_renderer_adopt_gaussians(dg_renderer* r, uint32_t count, dg_buffer* gaussians, dg_buffer* sh,
+                                      uint32_t degree);
+dg_status dg_renderer_set_sh_degree(dg_renderer* r, uint32_t degree);
+/* encode(encoder, target, camera, background): target may be NULL. */
+dg_status dg_renderer_encode(dg_renderer* r, dg_buffer* target, const dg_camera* camera, const float background[3]);
+/* encodeDraw(encoder, target, splats, count, viewport, background) */
+dg_status dg_renderer_encode_draw(dg_renderer* r, dg_buffer* target, dg_buffer* splats, uint32_t count,
+                                  const float viewport[2], const float background[3]);
+/* encodeBackward(encoder, pixelGrads) */
+dg_status dg_renderer_encode_backward(dg_renderer* r, dg_buffer* pixel_grads);
+dg_status dg_renderer_after_submit(dg_renderer* r, int32_t wait);
+uint32_t dg_renderer_count(const dg_renderer* r);
+dg_buffer* dg_renderer_splat_buffer(dg_renderer* r);
+dg_buffer* dg_renderer_gaussian_buffer(dg_renderer* r);
+dg_buffer* dg_renderer_sh_buffer(dg_renderer* r);
+dg_buffer* dg_renderer_pixel_buffer(dg_renderer* r);
+dg_buffer* dg_renderer_pixel_last_buffer(dg_renderer* r);
+dg_buffer* dg_renderer_gradient_gaussians(dg_renderer* r);
+dg_buffer* dg_renderer_gradient_sh(dg_renderer* r);
+dg_buffer* dg_renderer_gradient_splats(dg_renderer* r);
+dg_tile_rasterizer* dg_renderer_tiles(dg_renderer* r);
+dg_tile_rasterizer* dg_renderer_draw_tiles(dg_renderer* r);
+dg_status dg_renderer_destroy(dg_renderer* r);
+
+/* ---- TrainingLoss (src/trainingLoss.ts:16-130): 0.8 L1 + 0.2 (1 - SSIM). */
+dg_status dg_training_loss_create(dg_context* ctx, uint32_t width, uint32_t height, dg_training_loss** out);
+/* encode(encoder, rendered, target): rendered vec4 per pixel, target rgba8 bytes. */
+dg_status dg_training_loss_encode(dg_training_loss* loss, dg_buffer* rendered, dg_buffer* target);
+dg_buffer* dg_training_loss_pixel_grads(dg_training_loss* loss);
+dg_buffer* dg_training_loss_pixel_loss(dg_training_loss* loss);
+/* read(): Σ pixel_loss + λ of the last encode. */
+dg_status dg_training_loss_read(dg_training_loss* loss, double* out);
+dg_status dg_training_loss_destroy(dg_training_loss* loss);
+
+/* ---- Trainer (src/trainer.ts:103-446) */
+
+/* TrainingSettings (src/trainer.ts:37-63). DEFAULT_SETTINGS (src/trainer.ts:65-82) via
+ * dg_training_settings_default. */
+typedef struct dg_training_settings {
+  double extent;
+  double position_lr_steps;
+  double position_lr[2];
+  double opacity_lr;
+  double scale_lr;
+  double rotation_lr;
+  double color_lr;
+  double sh_lr;
+  uint32_t sh_degree_interval;
+  uint32_t densify_from;
+  uint32_t densify_until;
+  uint32_t densify_interval;
+  double densify_grad_threshold;
+  double percent_dense;
+  double min_opacity;
+  uint32_t opacity_reset_interval;
+  float background[3];
+} dg_training_settings;
+void dg_training_settings_default(dg_training_settings* out, double extent);
+
+/* TrainingView (src/trainer.ts:20-24): a camera and a photo (rgba8 bytes of the
+ * viewport's size). The trainer keeps the pointer; the caller keeps the buffer alive. */
+typedef struct dg_training_view {
+  dg_camera camera;
+  dg_buffer* image;
+} dg_training_view;
+
+/* Densification (src/trainer.ts:87-95) */
+typedef struct dg_densification {
+  uint32_t step, before, after, kept, cloned, split, removed;
+} dg_densification;
+
+/* new Trainer(device, {params, sh}, views, settings): params 16 raw floats per
+ * Gaussian, sh 45 per Gaussian. Throws (DG_ERROR_INVALID_ARGUMENT) on views of mixed sizes. */
+dg_status dg_trainer_create(dg_context* ctx, const float* params, const float* sh, uint32_t count,
+                            const dg_training_view* views, uint32_t view_count, const dg_training_settings* settings,
+                            dg_trainer** out);
+dg_status dg_trainer_step(dg_trainer* t);     /* optimize() then maintain() */
+dg_status dg_trainer_optimize(dg_trainer* t); /* render, loss, backward, stats, Adam */
+dg_status dg_trainer_maintain(dg_trainer* t); /* densify / reset opacity when due */
+dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large);
+dg_status dg_trainer_reset_opacity(dg_trainer* t);
+/* exportRaw(): params (16 * count floats) and sh (45 * count floats). */
+dg_status dg_trainer_export_raw(dg_trainer* t, float* params, float* sh);
+dg_status dg_trainer_last_loss(dg_trainer* t, double* out);
+/* evaluate(views, withSsim): mean PSNR and SSIM of 8-bit-quantized renders, computed on the GPU. */
+dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint32_t view_count, int32_t with_ssim,
+                              double* psnr, double* ssim);
+uint32_t dg_trainer_iteration(const dg_trainer* t);
+dg_status dg_trainer_set_iteration(dg_trainer* t, uint32_t iteration);
+uint32_t dg_trainer_sh_degree(const dg_trainer* t);
+uint32_t dg_trainer_count(const dg_trainer* t);
+dg_renderer* dg_trainer_renderer(dg_trainer* t);
+dg_buffer* dg_trainer_params(dg_trainer* t);
+dg_buffer* dg_trainer_moments(dg_trainer* t);
+dg_buffer* dg_trainer_stats(dg_trainer* t);
+uint32_t dg_trainer_densification_count(const dg_trainer* t);
+dg_status dg_trainer_densification(const dg_trainer* t, uint32_t index, dg_densification* out);
+/* Runs each optimize() step as one replay of a captured CUDA graph (re-captured
+ * when the Gaussian count or the pair capacity changes). enabled = 0 launches each
+ * kernel directly. Results are identical either way. */
+dg_status dg_trainer_set_graph(dg_trainer* t, int32_t enabled);
+dg_status dg_trainer_destroy(dg_trainer* t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIORAMA_GB300_H */
