@@ -1,0 +1,121 @@
+"""Scenes and comparisons shared by the tests, following the reference's checks
+(src/checks/helpers.ts, src/checks/tiles.ts, src/checks/depthSort.ts)."""
+
+from __future__ import annotations
+
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+
+import oracle
+from diorama_gb300 import CameraData, Gaussian, packGaussians
+from diorama_gb300.mat4 import IDENTITY, perspective
+from diorama_gb300.random import mulberry32
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def cam_array(camera: CameraData) -> np.ndarray:
+    return oracle.camera_array(camera.view, camera.proj, camera.viewport)
+
+
+def random_scene(count: int, scale=(0.02, 0.4), opacity=(0.2, 0.95)) -> list[Gaussian]:
+    """src/checks/tiles.ts:169-186: Gaussians scattered through the view."""
+    random = mulberry32(11)
+    between = lambda lo, hi: lo + (hi - lo) * random()  # noqa: E731
+    out = []
+    for _ in range(count):
+        depth = between(2, 8)
+        position = (between(-1.2, 1.2) * depth, between(-0.9, 0.9) * depth, -depth)
+        sc = (between(*scale), between(*scale), between(*scale))
+        rotation = (between(-1, 1), between(-1, 1), between(-1, 1), between(-1, 1))
+        color = (random(), random(), random())
+        out.append(Gaussian(position=position, scale=sc, rotation=rotation, color=color, opacity=between(*opacity)))
+    return out
+
+
+TILES_VIEWPORT = (120, 90)
+TILES_CAMERA = CameraData(view=IDENTITY, proj=perspective(math.pi / 2, 120 / 90, 0.1, 100), viewport=TILES_VIEWPORT)
+
+
+def backward_fixture():
+    """The reference's backward fixture as arrays: activated Gaussians (16 floats
+    each), SH rest, camera, background, pixel gradients (vec4), image, gradients."""
+    d = json.loads((GOLDEN / "backward.json").read_text())
+    g = np.zeros((len(d["gaussians"]), 16), np.float32)
+    for i, x in enumerate(d["gaussians"]):
+        g[i, 0:3] = x["position"]
+        g[i, 3] = x["opacity"]
+        g[i, 4:7] = x["scale"]
+        g[i, 8:12] = x["rotation"]
+        g[i, 12:15] = x["color"]
+    W, H = d["viewport"]
+    pg = np.zeros((W * H, 4), np.float32)
+    pg[:, :3] = np.array(d["pixelGrads"]).reshape(-1, 3)
+    grads = {
+        "position": np.array([x["position"] for x in d["gradients"]]),
+        "scale": np.array([x["scale"] for x in d["gradients"]]),
+        "rotation": np.array([x["rotation"] for x in d["gradients"]]),
+        "opacity": np.array([[x["opacity"]] for x in d["gradients"]]),
+        "color": np.array([x["color"] for x in d["gradients"]]),
+        "sh": np.array([x["sh"] for x in d["gradients"]]),
+    }
+    return dict(
+        gaussians=g,
+        sh=np.array(d["shRest"], np.float32).reshape(-1),
+        camera=CameraData(view=d["view"], proj=d["proj"], viewport=(W, H)),
+        background=np.array(d["background"], np.float32),
+        degree=d["shDegree"],
+        pixel_grads=pg,
+        image=np.array(d["image"]).reshape(-1, 3),
+        grads=grads,
+        fd_error=d["finiteDifferenceError"],
+    )
+
+
+# Where each group sits in the 16-float gradient layout (src/checks/backward.ts:41-47).
+GROUPS = [("position", 0, 3), ("scale", 4, 3), ("rotation", 8, 4), ("opacity", 3, 1), ("color", 12, 3)]
+
+
+def group_errors(gaussian_grads: np.ndarray, sh_grads: np.ndarray, expected: dict) -> dict:
+    """Largest disagreement per group relative to the group's largest reference gradient."""
+    gg = np.asarray(gaussian_grads, np.float64).reshape(-1, 16)
+    out = {}
+    for name, off, size in GROUPS:
+        ref = np.asarray(expected[name], np.float64).reshape(len(gg), -1)
+        out[name] = float(np.abs(gg[:, off:off + size] - ref).max() / max(np.abs(ref).max(), 1e-30))
+    ref = np.asarray(expected["sh"], np.float64).reshape(len(gg), -1)
+    sg = np.asarray(sh_grads, np.float64).reshape(len(gg), -1)
+    out["sh"] = float(np.abs(sg - ref).max() / max(np.abs(ref).max(), 1e-30))
+    return out
+
+
+def loss_fixture():
+    d = json.loads((GOLDEN / "loss.json").read_text())
+    w, h = d["size"]
+    render = np.zeros((w * h, 4), np.float32)
+    render[:, :3] = np.array(d["render"]).reshape(-1, 3)
+    target = np.full((w * h, 4), 255, np.uint8)
+    target[:, :3] = np.array(d["target"]).reshape(-1, 3)
+    return dict(width=w, height=h, render=render, target=target, loss=d["loss"],
+                gradient=np.array(d["gradient"]).reshape(-1, 3), fd_error=d["finiteDifferenceError"])
+
+
+def stable_sort_reference(keys: np.ndarray) -> np.ndarray:
+    """The permutation of a stable sort by key (src/checks/depthSort.ts:94)."""
+    return np.argsort(keys, kind="stable").astype(np.uint32)
+
+
+def sort_keys(size: int) -> np.ndarray:
+    """src/checks/depthSort.ts:84-89: half full-range keys, half in 0..15."""
+    random = mulberry32(size)
+    out = np.zeros(size, np.uint32)
+    for i in range(size):
+        out[i] = math.floor(random() * 2**32) if i % 2 == 0 else math.floor(random() * 16)
+    return out
+
+
+def pack(gaussians) -> np.ndarray:
+    return packGaussians(gaussians)
