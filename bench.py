@@ -1,0 +1,392 @@
+"""Benchmark: training steps/s at 1.1M Gaussians.
+
+Workload (BASELINE configs 1 and 3): config 1's synthetic scene of 40 random
+planes and boxes grown to 1.1M Gaussians (SH degree 3), trained against
+photos rendered from a 500k-Gaussian ground truth on the same surfaces, seen
+by 263 training cameras on a jittered ring at 980x545 (fov 55 deg). One step
+is one Trainer.optimize(): preprocess, tile keys, radix sort, ranges, blend,
+L1 + D-SSIM loss, both backward passes, densification statistics and Adam,
+replayed as one captured CUDA graph. Densification is off in the timed steps
+(the steady state after the reference's step 15,000); the SH degree is
+already 3. The working set (~3 GB) is far larger than L2, so no flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the reference's algorithm on the host cores instead:
+the reference itself is TypeScript + WGSL that only runs in a browser's
+WebGPU, so its CPU implementation here is the oracle (oracle/oracle.c, a C
+restatement of its WGSL, OpenMP over all host threads), on the same workload.
+For N > 1 the path has no exchange step (training does not shard; see
+the design doc): each rank trains its own replica and the value is the sum.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from dataclasses import replace
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "train steps/s @1.1M Gaussians"
+UNIT = "steps/s"
+GROUND_TRUTH = 500_000
+SCENE_SEED, TRUTH_SEED = 22, 21
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--gaussians", type=int, default=1_100_000)
+    ap.add_argument("--views", type=int, default=263, help="training views (photos) to render and cycle through")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    return args
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    group = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        group = dist
+    return rank, world, local, group
+
+
+def reduce_max(group, value: float) -> float:
+    if group is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    group.all_reduce(t, op=group.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(group):
+    if group is not None:
+        group.barrier()
+
+
+def config(args, world):
+    return {
+        "workload": "config 3: config-1 planes-and-boxes scene grown to 1.1M Gaussians, one optimize() step per 980x545 "
+                    "training view, full step as one CUDA graph",
+        "gaussians": args.gaussians,
+        "viewport": [980, 545],
+        "training_views": args.views,
+        "sh_degree": 3,
+        "densify": "off in the timed steps (steady state past step 15,000)",
+        "l2": "working set ~3 GB > 129 MB L2; no flush needed",
+        "parallelism": f"replicas x{world}",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(args):
+    from diorama_gb300 import scenes
+
+    raw, sh = scenes.surface_scene(args.gaussians, SCENE_SEED, noise=0.01)
+    truth_raw, truth_sh = scenes.surface_scene(GROUND_TRUTH, TRUTH_SEED)
+    train_cams, _held = scenes.ring_cameras()
+    return raw, sh, truth_raw, truth_sh, train_cams[: args.views]
+
+
+# Algorithmic bytes per unit: what each kernel must move at minimum.
+def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6) -> float | None:
+    return {
+        "adam": 1708.0 * n,  # 59 trainable slots x (read p, g, m, v: 16 B; write p, m, v: 12 B) + 56 B activated
+        "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
+        "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
+        "sort_pass": 24.0 * pairs,  # per pass: read and write 8 B key + 4 B value
+        "sort_histogram": 8.0 * pairs,
+        "scan": 8.0 * n,
+        "duplicate": 20.0 * n + 12.0 * pairs,
+        "find_ranges": 8.0 * pairs + 8.0 * tiles,
+        "loss_ssim": 20.0 * pixels + 48.0 * pixels,
+        "loss_gradient": 20.0 * pixels + 48.0 * pixels + 20.0 * pixels,
+        "stats": (4 + 8 + 16 + 16) * float(n),
+    }.get(name)
+
+
+def run_ours(args, rank, world, local, group):
+    from diorama_gb300 import (DEFAULT_SETTINGS, Device, GaussianRenderer, RawGaussians, Trainer, TrainingView,
+                               activate)
+    from diorama_gb300.gpu import PinnedArray
+
+    raw, sh, truth_raw, truth_sh, cams = build_scene(args)
+    device = Device(local)
+    W, H = cams[0].viewport
+    photographer = GaussianRenderer(device)
+    photographer.setGaussians(activate(truth_raw), {"rest": truth_sh.reshape(-1), "degree": 3})
+    views = []
+    for k, cam in enumerate(cams):
+        tex = device.createTexture(W, H)
+        photographer.encode(None, tex, cam, (0, 0, 0))
+        views.append(TrainingView(f"view {k}", cam, tex))
+    device.synchronize()
+    photographer.destroy()
+    settings = replace(DEFAULT_SETTINGS, extent=4.0, shDegreeInterval=1, densifyUntil=0)
+    trainer = Trainer(device, RawGaussians(raw.reshape(-1), sh.reshape(-1)), views, settings)
+    trainer.setGraph(not args.no_graph)
+    for _ in range(args.warmup):
+        trainer.step()
+    trainer.renderer.afterSubmit()
+    trainer.step()  # re-capture if the warm-up grew the pair buffers
+    device.synchronize()
+    assert trainer.shDegree == 3
+
+    # Device-timed steps: CUDA events on the library's stream.
+    start, end = device.event(), device.event()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(group)
+    device.synchronize()
+    launches0 = device.launch_count
+    start.record()
+    for _ in range(args.steps):
+        trainer.step()
+    end.record()
+    ms = start.elapsed_ms(end)
+    device.synchronize()
+    barrier(group)
+    clocks = sampler.stop()
+    launches = device.launch_count - launches0
+    ms = reduce_max(group, ms)
+    value = world * args.steps / (ms / 1000.0)
+
+    # End to end through the public API: each step uploads its photo from pinned
+    # host memory and reads back the loss.
+    pinned = []
+    for v in views:
+        p = PinnedArray((H * W * 4,), np.uint8)
+        p.array[:] = v.image.read().reshape(-1)
+        pinned.append(p)
+    camera_bytes, adam_bytes = 144, 48
+    barrier(group)
+    device.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        k = trainer.nextView()
+        views[k].image.buffer.writePinned(pinned[k])
+        trainer.step()
+        trainer.lossValue()
+    e2e_s = reduce_max(group, time.perf_counter() - t0)
+    barrier(group)
+    e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * H * 4 + camera_bytes + adam_bytes
+           + 8 + 16, "d2h_bytes_per_step": 8 + 4}
+
+    # Per-kernel times: the same steps launched directly, each kernel bracketed by events.
+    trainer.setGraph(False)
+    device.synchronize()
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    for _ in range(args.steps):
+        trainer.step()
+    report = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    pairs = trainer.renderer.tiles.lastPairCount
+    n = trainer.count
+    tiles = math.ceil(W / 16) * math.ceil(H / 16)
+    total = sum(ms for _, ms in report.values())
+    kernels = {name: {"launches": c, "avg_us": 1000 * t / c, "share": t / total} for name, (c, t) in report.items()}
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_source = "measured" if "hbm_gbs" in peaks else "fallback"
+    roofline = None
+    memory_kernels = [k for k in kernels if algorithmic_bytes(k, n, pairs, W * H, tiles) is not None]
+    dominant = max(kernels, key=lambda k: kernels[k]["share"])
+    dom_mem = max(memory_kernels, key=lambda k: kernels[k]["share"]) if memory_kernels else None
+    if dom_mem:
+        launches_per_step = kernels[dom_mem]["launches"] / args.steps
+        by = algorithmic_bytes(dom_mem, n, pairs, W * H, tiles)
+        achieved = by / (kernels[dom_mem]["avg_us"] * 1e-6) / 1e9
+        roofline = {"kernel": dom_mem, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+                    "unit": "GB/s", "frac": round(achieved / hbm_peak, 3), "peak_source": peak_source,
+                    "algorithmic_bytes_per_launch": by, "launches_per_step": launches_per_step,
+                    "traffic": None}
+    blend = {}
+    for k in ("rasterize", "rasterize_backward"):
+        if k in kernels:
+            blend[k] = {"avg_us": round(kernels[k]["avg_us"], 1), "share": round(kernels[k]["share"], 3)}
+
+    result = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded planes-and-boxes scene; "
+        "the reference's Tanks and Temples photos are not available)",
+        "config": config(args, world), "e2e": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in e2e.items()},
+        "gpu_launches": launches, "roofline": roofline, "clocks": clocks,
+        "kernels": {k: {"avg_us": round(v["avg_us"], 2), "share": round(v["share"], 4), "launches": v["launches"]}
+                    for k, v in sorted(kernels.items(), key=lambda kv: -kv[1]["share"])},
+        "dominant_kernel": dominant, "blend": blend, "pairs": pairs, "gaussians": n,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args, raw, sh, views_host(views), cams, samples=1)
+    trainer.destroy()
+    for v in views:
+        v.image.destroy()
+    for p in pinned:
+        p.free()
+    device.destroy()
+    return result
+
+
+def views_host(views):
+    return [v.image.read() for v in views[:4]]
+
+
+def cpu_baseline(args, raw, sh, photos, cams, samples: int) -> dict:
+    """The oracle's optimize() step on the same workload, timed on the host cores."""
+    import oracle
+
+    params = np.ascontiguousarray(raw, np.float32).reshape(-1).copy()
+    shc = np.ascontiguousarray(sh, np.float32).reshape(-1).copy()
+    n = params.size // 16
+    moments = np.zeros(n * 61 * 2, np.float32)
+    stats = np.zeros(n * 4, np.float32)
+    gaussians = oracle.activate(params)
+    W, H = cams[0].viewport
+    bg = np.zeros(3, np.float32)
+    times = []
+    for s in range(samples):
+        cam = oracle.camera_array(cams[s % len(photos)].view, cams[s % len(photos)].proj, (W, H))
+        photo = np.ascontiguousarray(photos[s % len(photos)], np.uint8).reshape(-1)
+        t0 = time.perf_counter()
+        frame = oracle.render(cam, bg, gaussians, shc, 3)
+        _, pg, _ = oracle.loss(frame["pixel_color"], photo, W, H)
+        sg = oracle.rasterize_backward(cam, bg, frame["splats"], frame, pg)
+        gg, sgr = oracle.preprocess_backward(cam, gaussians, shc, 3, frame["splats"], sg)
+        oracle.accumulate_stats(frame["splats"], sg, (W, H), stats)
+        ap = np.array([0.1, 0.001, 1.6e-4 * 4, 0.025, 0.005, 0.001, 0.0025, 0.0025 / 20, W, H], np.float32)
+        oracle.adam_step(ap, params, shc, moments, gg, sgr, gaussians)
+        times.append(time.perf_counter() - t0)
+    sec = statistics.median(times)
+    return {"value": round(1.0 / sec, 4), "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{samples} full optimize() step(s) of the same workload ({n} Gaussians, {W}x{H}) by the C "
+                      f"oracle with OpenMP; median {sec:.2f} s"}
+
+
+def run_reference(args, rank, world, group):
+    """The reference's algorithm on the host (the oracle), rank 0 only."""
+    if rank != 0:
+        return None
+    import oracle
+    from diorama_gb300 import activate
+
+    raw, sh, truth_raw, truth_sh, cams = build_scene(args)
+    W, H = cams[0].viewport
+    truth = activate(truth_raw)
+    photos = []
+    for cam in cams[: max(1, min(4, len(cams)))]:
+        c = oracle.camera_array(cam.view, cam.proj, (W, H))
+        photos.append(oracle.render(c, np.zeros(3, np.float32), truth, truth_sh.reshape(-1), 3)["rgba8"])
+    base = cpu_baseline(args, raw, sh, photos, cams, samples=1)  # warm-up and per-step estimate
+    per_step = 1.0 / base["value"]
+    budget = 180.0
+    steps = max(1, min(args.steps, int(budget / per_step)))
+    timed = cpu_baseline(args, raw, sh, photos, cams, samples=steps)
+    value = timed["value"]
+    timed["sample"] = (f"{steps} of {args.steps} requested full optimize() steps (capped at ~{int(budget)} s of CPU "
+                       f"work), {timed['sample']}")
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": 1,
+        "ms_per_step": round(1000.0 / value, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded planes-and-boxes scene)", "config": config(args, world),
+        "impl": "reference", "cpu_baseline": timed,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is TypeScript + WGSL for a browser's WebGPU; its algorithm runs here as the C oracle "
+                "on the host cores",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local, group = dist_setup(args)
+    if args.impl == "reference":
+        result = run_reference(args, rank, world, group)
+    else:
+        result = run_ours(args, rank, world, local, group)
+    if rank == 0 and result is not None:
+        print(json.dumps(result), flush=True)
+    if group is not None:
+        group.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,17 @@ SIGNATURES = {
     "dg_context_synchronize": (None, [_P]),
     "dg_context_check": (None, [_P, POINTER(c_uint32)]),
     "dg_context_launch_count": (None, [_P, POINTER(c_uint64)]),
+    "dg_context_set_kernel_timing": (None, [_P, c_int32]),
+    "dg_context_kernel_timing_report": (None, [_P, ctypes.c_char_p, c_uint64]),
+    "dg_event_create": (None, [_P, POINTER(_P)]),
+    "dg_event_record": (None, [_P]),
+    "dg_event_elapsed": (None, [_P, _P, POINTER(c_float)]),
+    "dg_event_destroy": (None, [_P]),
+    "dg_host_alloc": (None, [c_uint64, POINTER(c_void_p)]),
+    "dg_host_free": (None, [c_void_p]),
+    "dg_buffer_write_pinned": (None, [_P, c_uint64, c_void_p, c_uint64]),
+    "dg_trainer_loss_value": (None, [_P, POINTER(c_double)]),
+    "dg_trainer_next_view": (None, [_P, POINTER(c_uint32)]),
     "dg_buffer_create": (None, [_P, c_uint64, POINTER(_P)]),
     "dg_buffer_wrap": (None, [_P, c_void_p, c_uint64, POINTER(_P)]),
     "dg_buffer_destroy": (None, [_P]),

@@ -70,9 +70,6 @@ dg_status cuda_fail(cudaError_t err, const char* what);
     if (!(cond)) return ::dg::fail(DG_ERROR_INVALID_ARGUMENT, msg); \
   } while (0)
 
-// Kernel launches report their own configuration errors.
-#define DG_LAUNCHED(name) DG_CUDA(cudaGetLastError())
-
 inline uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace dg
@@ -108,7 +105,34 @@ struct dg_context {
   bool capturing = false;
   // Kernels launched through this context (graph replays add their kernel count).
   uint64_t launches = 0;
+  // Per-kernel timing (dg_context_set_kernel_timing): an event pair around every
+  // launch made outside graph capture, summed per kernel name on request.
+  bool timing = false;
+  struct Timed {
+    const char* name;
+    cudaEvent_t start, end;
+  };
+  std::vector<Timed> timed;
+  std::vector<cudaEvent_t> timing_pool;
+  cudaEvent_t pending_start = nullptr;
 };
+
+namespace dg {
+// Kernel launch bookkeeping: counts the launch and, when kernel timing is on and
+// no graph is being captured, brackets it with an event pair.
+void timing_begin(dg_context* ctx);
+void timing_end(dg_context* ctx, const char* name);
+}  // namespace dg
+
+// DG_LAUNCH(ctx, "name", kernel<<<grid, block, smem, stream>>>(args...));
+#define DG_LAUNCH(ctx, name, ...)               \
+  do {                                          \
+    ::dg::timing_begin(ctx);                    \
+    __VA_ARGS__;                                \
+    (ctx)->launches++;                          \
+    ::dg::timing_end(ctx, name);                \
+    DG_CUDA(cudaGetLastError());                \
+  } while (0)
 
 namespace dg {
 // Enqueue a host→device copy with writeBuffer semantics (the source is

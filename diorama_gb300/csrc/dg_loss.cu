@@ -276,16 +276,14 @@ dg_status loss_launch(dg_training_loss* l, dg_buffer* rendered) {
   dg_context* ctx = l->ctx;
   const Window win = window_weights();
   dim3 grid(ceil_div(l->width, LT), ceil_div(l->height, LT));
-  ssim_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(l->target_slot),
-                                             (int)l->width, (int)l->height, win, typed<float>(l->partials), 0,
-                                             nullptr);
-  ctx->launches++;
-  DG_LAUNCHED("ssim_kernel");
-  gradient_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(l->target_slot),
-                                                 (int)l->width, (int)l->height, win, typed<float>(l->partials),
-                                                 typed<float4>(l->pixel_grads), typed<float>(l->pixel_loss));
-  ctx->launches++;
-  DG_LAUNCHED("gradient_kernel");
+  DG_LAUNCH(ctx, "loss_ssim",
+            ssim_kernel<<<grid, 256, 0, ctx->stream>>>(
+                typed<float4>(rendered), typed<const uchar4* const>(l->target_slot), (int)l->width, (int)l->height,
+                win, typed<float>(l->partials), 0, nullptr));
+  DG_LAUNCH(ctx, "loss_gradient",
+            gradient_kernel<<<grid, 256, 0, ctx->stream>>>(
+                typed<float4>(rendered), typed<const uchar4* const>(l->target_slot), (int)l->width, (int)l->height,
+                win, typed<float>(l->partials), typed<float4>(l->pixel_grads), typed<float>(l->pixel_loss)));
   return DG_OK;
 }
 
@@ -294,12 +292,12 @@ dg_status loss_sum_launch(dg_training_loss* l) {
   const uint32_t n = l->width * l->height;
   const uint32_t per_block = 4096;
   const uint32_t blocks = std::max(1u, ceil_div(n, per_block));
-  loss_sum_kernel<<<blocks, 256, 0, ctx->stream>>>(typed<float>(l->pixel_loss), n, typed<double>(l->sum_scratch),
-                                                   per_block);
-  loss_total_kernel<<<1, 32, 0, ctx->stream>>>(typed<double>(l->sum_scratch), blocks,
-                                                typed<double>(l->sum_scratch) + l->sum_blocks);
-  ctx->launches += 2;
-  DG_LAUNCHED("loss_sum");
+  DG_LAUNCH(ctx, "loss_sum",
+            loss_sum_kernel<<<blocks, 256, 0, ctx->stream>>>(typed<float>(l->pixel_loss), n,
+                                                             typed<double>(l->sum_scratch), per_block));
+  DG_LAUNCH(ctx, "loss_total",
+            loss_total_kernel<<<1, 32, 0, ctx->stream>>>(typed<double>(l->sum_scratch), blocks,
+                                                          typed<double>(l->sum_scratch) + l->sum_blocks));
   return DG_OK;
 }
 
@@ -307,10 +305,10 @@ dg_status metrics_launch(dg_context* ctx, dg_buffer* rendered, dg_buffer* target
                          double* sums_device) {
   const Window win = window_weights();
   dim3 grid(ceil_div(width, LT), ceil_div(height, LT));
-  ssim_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered), typed<const uchar4* const>(target_slot),
-                                             (int)width, (int)height, win, nullptr, 1, sums_device);
-  ctx->launches++;
-  DG_LAUNCHED("ssim_kernel(metrics)");
+  DG_LAUNCH(ctx, "metrics_ssim",
+            ssim_kernel<<<grid, 256, 0, ctx->stream>>>(typed<float4>(rendered),
+                                                       typed<const uchar4* const>(target_slot), (int)width,
+                                                       (int)height, win, nullptr, 1, sums_device));
   return DG_OK;
 }
 

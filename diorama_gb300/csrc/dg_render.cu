@@ -205,17 +205,19 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_kernel(const Camera* __
 // src/shaders/tiles.wgsl:65-84
 __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32_t* __restrict__ key_words,
                                                                     const uint32_t* __restrict__ pair_total,
-                                                                    uint32_t capacity, uint2* __restrict__ ranges) {
+                                                                    uint32_t capacity, uint32_t tiles,
+                                                                    uint2* __restrict__ ranges) {
   const uint32_t n = min(pair_total[0], capacity);
   const uint32_t i = blockIdx.x * RANGE_THREADS + threadIdx.x;
   if (i >= n) return;
   const uint32_t tile = key_words[2 * (size_t)i + 1];
+  if (tile >= tiles) return;  // only possible after a sort whose bounded wait gave up
   if (i == 0) {
     ranges[tile].x = 0;
   } else {
     const uint32_t prev = key_words[2 * (size_t)i - 1];
     if (tile != prev) {
-      ranges[prev].y = i;
+      if (prev < tiles) ranges[prev].y = i;
       ranges[tile].x = i;
     }
   }
@@ -761,33 +763,30 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
   DG_CUDA(cudaMemsetAsync(tr->ranges->ptr, 0, (size_t)tr->tiles_x * tr->tiles_y * 8, st));
   if (count > 0) {
     if (!counts_ready) {
-      count_tiles_kernel<<<ceil_div(count, 256), 256, 0, st>>>(cam, typed<float>(tr->splats), count,
-                                                              typed<uint32_t>(tr->tile_offsets));
-      ctx->launches++;
-      DG_LAUNCHED("count_tiles");
+      DG_LAUNCH(ctx, "count_tiles",
+                count_tiles_kernel<<<ceil_div(count, 256), 256, 0, st>>>(cam, typed<float>(tr->splats), count,
+                                                                        typed<uint32_t>(tr->tile_offsets)));
     }
   }
   DG_TRY(scan_launch(ctx, typed<uint32_t>(tr->tile_offsets), count, nullptr, typed<uint32_t>(tr->scan_total),
                      tr->scan_scratch->ptr));
   if (count > 0) {
-    duplicate_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
-        cam, typed<float>(tr->splats), typed<uint32_t>(tr->tile_offsets), count, tr->pair_capacity,
-        typed<uint64_t>(tr->keys), typed<uint32_t>(tr->values));
-    ctx->launches++;
-    DG_LAUNCHED("duplicate");
+    DG_LAUNCH(ctx, "duplicate",
+              duplicate_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
+                  cam, typed<float>(tr->splats), typed<uint32_t>(tr->tile_offsets), count, tr->pair_capacity,
+                  typed<uint64_t>(tr->keys), typed<uint32_t>(tr->values)));
   }
   DG_TRY(sort_launch(ctx, tr->plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
                      typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
-  find_ranges_kernel<<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0, st>>>(
-      typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total), tr->pair_capacity, typed<uint2>(tr->ranges));
-  ctx->launches++;
-  DG_LAUNCHED("find_ranges");
-  rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, st>>>(
-      cam, typed<float4>(tr->raster_params), typed<float>(tr->splats), typed<uint32_t>(tr->values),
-      typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
-      typed<uint32_t>(tr->pixel_last));
-  ctx->launches++;
-  DG_LAUNCHED("rasterize");
+  DG_LAUNCH(ctx, "find_ranges",
+            find_ranges_kernel<<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0, st>>>(
+                typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total), tr->pair_capacity,
+                tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+  DG_LAUNCH(ctx, "rasterize",
+            rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, st>>>(
+                cam, typed<float4>(tr->raster_params), typed<float>(tr->splats), typed<uint32_t>(tr->values),
+                typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
+                typed<uint32_t>(tr->pixel_last)));
   return DG_OK;
 }
 
@@ -802,12 +801,11 @@ dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr) {
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads) {
   dg_context* ctx = tr->ctx;
   DG_CUDA(cudaMemsetAsync(splat_grads->ptr, 0, (size_t)tr->count * SPLAT_GRADS * 4, ctx->stream));
-  rasterize_backward_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
-      typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
-      typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
-      typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads));
-  ctx->launches++;
-  DG_LAUNCHED("rasterize_backward");
+  DG_LAUNCH(ctx, "rasterize_backward",
+            rasterize_backward_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
+                typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
+                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
+                typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads)));
   return DG_OK;
 }
 
@@ -863,11 +861,11 @@ dg_status renderer_prepare(dg_renderer* r, const dg_camera* camera, const float 
 dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target) {
   dg_context* ctx = r->ctx;
   if (r->count > 0) {
-    preprocess_kernel<<<ceil_div(r->count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
-        typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
-        typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<uint32_t>(r->rasterizer->tile_offsets));
-    ctx->launches++;
-    DG_LAUNCHED("preprocess");
+    DG_LAUNCH(ctx, "preprocess",
+              preprocess_kernel<<<ceil_div(r->count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
+                  typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
+                  typed<uint32_t>(r->scene_params), typed<float>(r->splats),
+                  typed<uint32_t>(r->rasterizer->tile_offsets)));
   }
   return rasterizer_launch(r->rasterizer, target, true);
 }
@@ -883,12 +881,11 @@ dg_status renderer_ensure_gradients(dg_renderer* r) {
 dg_status renderer_launch_backward(dg_renderer* r, dg_buffer* pixel_grads, bool write_gaussian_grads) {
   DG_TRY(rasterizer_launch_backward(r->rasterizer, pixel_grads, r->grad_splats));
   if (!write_gaussian_grads || r->count == 0) return DG_OK;
-  preprocess_backward_kernel<<<ceil_div(r->count, 128), 128, 0, r->ctx->stream>>>(
-      typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
-      typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats),
-      typed<float>(r->grad_gaussians), typed<float>(r->grad_sh));
-  r->ctx->launches++;
-  DG_LAUNCHED("preprocess_backward");
+  DG_LAUNCH(r->ctx, "preprocess_backward",
+            preprocess_backward_kernel<<<ceil_div(r->count, 128), 128, 0, r->ctx->stream>>>(
+                typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
+                typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats),
+                typed<float>(r->grad_gaussians), typed<float>(r->grad_sh)));
   return DG_OK;
 }
 
@@ -1029,11 +1026,9 @@ dg_status dg_renderer_encode(dg_renderer* r, dg_buffer* target, const dg_camera*
   DG_TRY(renderer_prepare(r, camera, background));
   if (!r->has_scene) {
     if (target && pixels) {
-      clear_target_kernel<<<ceil_div(pixels, 256), 256, 0, r->ctx->stream>>>(typed<uchar4>(target), pixels,
-                                                                            background[0], background[1],
-                                                                            background[2]);
-      r->ctx->launches++;
-      DG_LAUNCHED("clear_target");
+      DG_LAUNCH(r->ctx, "clear_target",
+                clear_target_kernel<<<ceil_div(pixels, 256), 256, 0, r->ctx->stream>>>(
+                    typed<uchar4>(target), pixels, background[0], background[1], background[2]));
     }
     return DG_OK;
   }

@@ -3,7 +3,8 @@
 #include "dg_common.cuh"
 #include "dg_scan.cuh"
 
-#include <mutex>
+#include <algorithm>
+#include <cstdio>
 
 namespace dg {
 
@@ -82,6 +83,31 @@ dg_status alloc_buffer(dg_context* ctx, uint64_t bytes, dg_buffer** out) {
   return DG_OK;
 }
 
+static cudaEvent_t timing_event(dg_context* ctx) {
+  if (!ctx->timing_pool.empty()) {
+    cudaEvent_t e = ctx->timing_pool.back();
+    ctx->timing_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void timing_begin(dg_context* ctx) {
+  if (!ctx->timing || ctx->capturing) return;
+  ctx->pending_start = timing_event(ctx);
+  cudaEventRecord(ctx->pending_start, ctx->stream);
+}
+
+void timing_end(dg_context* ctx, const char* name) {
+  if (!ctx->timing || ctx->capturing || !ctx->pending_start) return;
+  cudaEvent_t end = timing_event(ctx);
+  cudaEventRecord(end, ctx->stream);
+  ctx->timed.push_back({name, ctx->pending_start, end});
+  ctx->pending_start = nullptr;
+}
+
 void free_buffer(dg_buffer* b) {
   if (!b) return;
   // Stream-ordered free: the GPU keeps the memory until work already enqueued is
@@ -143,6 +169,11 @@ dg_status dg_context_destroy(dg_context* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (auto& p : ctx->pending) cudaEventDestroy(p.done);
   for (auto e : ctx->free_events) cudaEventDestroy(e);
+  for (auto& t : ctx->timed) {
+    cudaEventDestroy(t.start);
+    cudaEventDestroy(t.end);
+  }
+  for (auto e : ctx->timing_pool) cudaEventDestroy(e);
   if (ctx->staging) cudaFreeHost(ctx->staging);
   if (ctx->device_error) cudaFree(ctx->device_error);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -172,6 +203,97 @@ dg_status dg_context_check(dg_context* ctx, uint32_t* bits) {
 dg_status dg_context_launch_count(dg_context* ctx, uint64_t* out) {
   DG_REQUIRE(ctx && out, "NULL argument");
   *out = ctx->launches;
+  return DG_OK;
+}
+
+dg_status dg_context_set_kernel_timing(dg_context* ctx, int32_t enabled) {
+  DG_REQUIRE(ctx, "NULL argument");
+  ctx->timing = enabled != 0;
+  return DG_OK;
+}
+
+dg_status dg_context_kernel_timing_report(dg_context* ctx, char* text, uint64_t capacity) {
+  DG_REQUIRE(ctx && text && capacity > 0, "NULL argument");
+  DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  struct Total {
+    std::string name;
+    uint64_t launches = 0;
+    double ms = 0;
+  };
+  std::vector<Total> totals;
+  for (auto& t : ctx->timed) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, t.start, t.end);
+    auto it = std::find_if(totals.begin(), totals.end(), [&](const Total& x) { return x.name == t.name; });
+    if (it == totals.end()) {
+      totals.push_back({t.name, 0, 0});
+      it = totals.end() - 1;
+    }
+    it->launches++;
+    it->ms += ms;
+    ctx->timing_pool.push_back(t.start);
+    ctx->timing_pool.push_back(t.end);
+  }
+  ctx->timed.clear();
+  std::string out;
+  for (auto& t : totals) out += t.name + " " + std::to_string(t.launches) + " " + std::to_string(t.ms) + "\n";
+  std::snprintf(text, capacity, "%s", out.c_str());
+  return DG_OK;
+}
+
+struct dg_event {
+  dg_context* ctx;
+  cudaEvent_t event;
+};
+
+dg_status dg_event_create(dg_context* ctx, dg_event** out) {
+  DG_REQUIRE(ctx && out, "NULL argument");
+  auto* e = new dg_event{ctx, nullptr};
+  cudaError_t err = cudaEventCreate(&e->event);
+  if (err != cudaSuccess) {
+    delete e;
+    return cuda_fail(err, "cudaEventCreate");
+  }
+  *out = e;
+  return DG_OK;
+}
+
+dg_status dg_event_record(dg_event* e) {
+  DG_REQUIRE(e, "NULL argument");
+  DG_CUDA(cudaEventRecord(e->event, e->ctx->stream));
+  return DG_OK;
+}
+
+dg_status dg_event_elapsed(dg_event* start, dg_event* end, float* ms) {
+  DG_REQUIRE(start && end && ms, "NULL argument");
+  DG_CUDA(cudaEventSynchronize(end->event));
+  DG_CUDA(cudaEventElapsedTime(ms, start->event, end->event));
+  return DG_OK;
+}
+
+dg_status dg_event_destroy(dg_event* e) {
+  if (!e) return DG_OK;
+  cudaEventDestroy(e->event);
+  delete e;
+  return DG_OK;
+}
+
+dg_status dg_host_alloc(uint64_t bytes, void** out) {
+  DG_REQUIRE(out, "NULL argument");
+  DG_CUDA(cudaMallocHost(out, bytes));
+  return DG_OK;
+}
+
+dg_status dg_host_free(void* ptr) {
+  if (ptr) DG_CUDA(cudaFreeHost(ptr));
+  return DG_OK;
+}
+
+dg_status dg_buffer_write_pinned(dg_buffer* b, uint64_t offset, const void* src, uint64_t bytes) {
+  DG_REQUIRE(b && (src || bytes == 0), "NULL argument");
+  DG_REQUIRE(offset + bytes <= b->bytes, "write past the end of the buffer");
+  if (bytes)
+    DG_CUDA(cudaMemcpyAsync(static_cast<char*>(b->ptr) + offset, src, bytes, cudaMemcpyHostToDevice, b->ctx->stream));
   return DG_OK;
 }
 

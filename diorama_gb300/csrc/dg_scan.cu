@@ -158,9 +158,9 @@ dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const 
   auto* ticket = static_cast<uint32_t*>(scratch);
   auto* status = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + 256);
   DG_CUDA(cudaMemsetAsync(scratch, 0, scan_scratch_bytes(capacity), ctx->stream));
-  scan_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, total, status, ticket, ctx->device_error);
-  ctx->launches++;
-  DG_LAUNCHED("scan_kernel");
+  DG_LAUNCH(ctx, "scan",
+            scan_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, total, status, ticket,
+                                                                 ctx->device_error));
   return DG_OK;
 }
 

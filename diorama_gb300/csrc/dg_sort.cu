@@ -219,6 +219,9 @@ __global__ void __launch_bounds__(SORT_THREADS, 2)
     K kk = s_keys[k];
     uint32_t dk = (uint32_t)(kk >> shift) & 0xffu;
     uint32_t out = s_base[dk] + k;
+    // Only a look-back that gave up (error bit already set) can place a key
+    // outside the output; drop it rather than write out of bounds.
+    if (out >= n) continue;
     keys_out[out] = kk;
     vals_out[out] = s_vals[k];
   }
@@ -258,21 +261,19 @@ dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32
   for (uint32_t p = 0; p < plan.passes; p++) shifts.shift[p] = p < 4 ? p * 8 : 32 + (p - 4) * 8;
   uint32_t hist_blocks = std::min<uint32_t>(ceil_div(plan.capacity, HIST_THREADS * 16), (uint32_t)ctx->sm_count * 4);
   hist_blocks = std::max(1u, hist_blocks);
-  sort_histogram_kernel<KW><<<hist_blocks, HIST_THREADS, 0, ctx->stream>>>(static_cast<const K*>(keys), plan.capacity,
-                                                                           count, plan.passes, shifts, hist);
-  ctx->launches++;
-  DG_LAUNCHED("sort_histogram_kernel");
+  DG_LAUNCH(ctx, "sort_histogram",
+            sort_histogram_kernel<KW><<<hist_blocks, HIST_THREADS, 0, ctx->stream>>>(
+                static_cast<const K*>(keys), plan.capacity, count, plan.passes, shifts, hist));
   size_t smem = pass_smem_bytes<KW>();
   K* in_k = static_cast<K*>(keys);
   uint32_t* in_v = values;
   K* out_k = static_cast<K*>(keys_alt);
   uint32_t* out_v = values_alt;
   for (uint32_t p = 0; p < plan.passes; p++) {
-    sort_pass_kernel<KW><<<l.max_tiles, SORT_THREADS, smem, ctx->stream>>>(
-        in_k, in_v, out_k, out_v, plan.capacity, count, shifts.shift[p], hist + p * RADIX,
-        status + (size_t)p * l.max_tiles * RADIX, tickets + p, ctx->device_error);
-    ctx->launches++;
-    DG_LAUNCHED("sort_pass_kernel");
+    DG_LAUNCH(ctx, "sort_pass",
+              sort_pass_kernel<KW><<<l.max_tiles, SORT_THREADS, smem, ctx->stream>>>(
+                  in_k, in_v, out_k, out_v, plan.capacity, count, shifts.shift[p], hist + p * RADIX,
+                  status + (size_t)p * l.max_tiles * RADIX, tickets + p, ctx->device_error));
     std::swap(in_k, out_k);
     std::swap(in_v, out_v);
   }

@@ -329,22 +329,21 @@ static uint32_t next_view(dg_trainer* t) {
 
 static dg_status launch_stats(dg_trainer* t) {
   dg_renderer* r = t->renderer;
-  stats_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
-      typed<AdamParams>(t->adam_params), typed<float>(r->splats), typed<float>(r->grad_splats),
-      typed<float4>(t->stats), t->count);
-  t->ctx->launches++;
-  DG_LAUNCHED("stats");
+  DG_LAUNCH(t->ctx, "stats",
+            stats_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
+                typed<AdamParams>(t->adam_params), typed<float>(r->splats), typed<float>(r->grad_splats),
+                typed<float4>(t->stats), t->count));
   return DG_OK;
 }
 
 static dg_status launch_adam(dg_trainer* t) {
   dg_renderer* r = t->renderer;
   const uint64_t elements = (uint64_t)t->count * MOMENT_SLOTS;
-  adam_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, t->ctx->stream>>>(
-      typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float>(r->sh), typed<float2>(t->moments),
-      typed<float>(r->grad_gaussians), typed<float>(r->grad_sh), typed<float>(r->gaussians), t->count);
-  t->ctx->launches++;
-  DG_LAUNCHED("adam");
+  DG_LAUNCH(t->ctx, "adam",
+            adam_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, t->ctx->stream>>>(
+                typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float>(r->sh),
+                typed<float2>(t->moments), typed<float>(r->grad_gaussians), typed<float>(r->grad_sh),
+                typed<float>(r->gaussians), t->count));
   return DG_OK;
 }
 
@@ -546,12 +545,10 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   DG_TRY(alloc_buffer(ctx, (size_t)count * 4 + 4, &outputs));  // + the scan total
   DG_TRY(alloc_buffer(ctx, 16, &counters));
   DG_TRY(alloc_buffer(ctx, scan_scratch_bytes(count), &scratch));
-  densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(dp, typed<float>(t->params),
-                                                                      typed<float4>(t->stats), count,
-                                                                      typed<uint32_t>(outputs),
-                                                                      typed<uint32_t>(counters));
-  ctx->launches++;
-  DG_LAUNCHED("densify_count");
+  DG_LAUNCH(ctx, "densify_count",
+            densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+                dp, typed<float>(t->params), typed<float4>(t->stats), count, typed<uint32_t>(outputs),
+                typed<uint32_t>(counters)));
   uint32_t* total_ptr = typed<uint32_t>(outputs) + count;
   DG_TRY(scan_launch(ctx, typed<uint32_t>(outputs), count, nullptr, total_ptr, scratch->ptr));
   uint32_t readback[5];
@@ -575,17 +572,18 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   DG_TRY(storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &gaussians));
   dg_renderer* r = t->renderer;
   const uint64_t elements = (uint64_t)count * MOMENT_SLOTS;
-  densify_copy_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, ctx->stream>>>(
-      dp, typed<float>(t->params), typed<float4>(t->stats), typed<float>(r->sh), typed<float2>(t->moments),
-      typed<uint32_t>(outputs), count, typed<float>(params), typed<float>(sh), typed<float2>(moments));
-  densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(dp, typed<float>(t->params),
-                                                                      typed<float4>(t->stats), typed<uint32_t>(outputs),
-                                                                      count, typed<float>(params));
+  DG_LAUNCH(ctx, "densify_copy",
+            densify_copy_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, ctx->stream>>>(
+                dp, typed<float>(t->params), typed<float4>(t->stats), typed<float>(r->sh), typed<float2>(t->moments),
+                typed<uint32_t>(outputs), count, typed<float>(params), typed<float>(sh), typed<float2>(moments)));
+  DG_LAUNCH(ctx, "densify_place",
+            densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+                dp, typed<float>(t->params), typed<float4>(t->stats), typed<uint32_t>(outputs), count,
+                typed<float>(params)));
   const uint64_t floats = (uint64_t)new_count * FLOATS_PER_GAUSSIAN;
-  activate_kernel<<<(uint32_t)((floats + 255) / 256), 256, 0, ctx->stream>>>(typed<float>(params),
-                                                                             typed<float>(gaussians), new_count);
-  ctx->launches += 3;
-  DG_LAUNCHED("densify scatter");
+  DG_LAUNCH(ctx, "activate",
+            activate_kernel<<<(uint32_t)((floats + 255) / 256), 256, 0, ctx->stream>>>(
+                typed<float>(params), typed<float>(gaussians), new_count));
   // Hand the new set to the renderer; the old buffers go once the work above is done.
   drop_graph(t);
   DG_TRY(dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree));
@@ -600,10 +598,10 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
 
 dg_status dg_trainer_reset_opacity(dg_trainer* t) {
   DG_REQUIRE(t, "NULL argument");
-  reset_opacity_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
-      typed<float>(t->params), typed<float2>(t->moments), typed<float>(t->renderer->gaussians), t->count);
-  t->ctx->launches++;
-  DG_LAUNCHED("reset_opacity");
+  DG_LAUNCH(t->ctx, "reset_opacity",
+            reset_opacity_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
+                typed<float>(t->params), typed<float2>(t->moments), typed<float>(t->renderer->gaussians),
+                t->count));
   return DG_OK;
 }
 
@@ -653,6 +651,26 @@ dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint
   free_buffer(slot);
   *psnr = psnr_total / view_count;
   *ssim = with_ssim ? ssim_total / view_count : NAN;
+  return DG_OK;
+}
+
+dg_status dg_trainer_next_view(dg_trainer* t, uint32_t* index) {
+  DG_REQUIRE(t && index, "NULL argument");
+  if (t->queue.empty()) {
+    // Refill exactly as next_view() would; it then takes the same view.
+    uint32_t v = next_view(t);
+    t->queue.push_back(v);
+  }
+  *index = t->queue.back();
+  return DG_OK;
+}
+
+dg_status dg_trainer_loss_value(dg_trainer* t, double* out) {
+  DG_REQUIRE(t && out, "NULL argument");
+  DG_TRY(loss_sum_launch(t->loss));
+  DG_CUDA(cudaMemcpyAsync(out, typed<double>(t->loss->sum_scratch) + t->loss->sum_blocks, 8, cudaMemcpyDeviceToHost,
+                          t->ctx->stream));
+  DG_CUDA(cudaStreamSynchronize(t->ctx->stream));
   return DG_OK;
 }
 

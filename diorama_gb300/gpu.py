@@ -45,6 +45,11 @@ class Buffer:
         arr = np.ascontiguousarray(data)
         _lib.call("dg_buffer_write", self.handle, offset, arr.ctypes.data, arr.nbytes)
 
+    def writePinned(self, pinned: "PinnedArray", offset: int = 0, nbytes: int | None = None) -> None:
+        """Enqueue an upload from pinned memory; keep it unchanged until the copy has run."""
+        nbytes = pinned.array.nbytes if nbytes is None else nbytes
+        _lib.call("dg_buffer_write_pinned", self.handle, offset, pinned.pointer, nbytes)
+
     def destroy(self) -> None:
         if self.owned and self.handle:
             _lib.call("dg_buffer_destroy", self.handle)
@@ -66,6 +71,47 @@ def borrowed(device: "Device", handle) -> Buffer | None:
     if not handle:
         return None
     return Buffer(device, c_void_p(handle), owned=False)
+
+
+class PinnedArray:
+    """A numpy array in pinned (page-locked) host memory."""
+
+    def __init__(self, shape, dtype=np.uint8):
+        dtype = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dtype.itemsize
+        ptr = c_void_p()
+        _lib.call("dg_host_alloc", max(nbytes, 1), ctypes.byref(ptr))
+        self.pointer = ptr.value
+        raw = (ctypes.c_uint8 * max(nbytes, 1)).from_address(self.pointer)
+        self.array = np.frombuffer(raw, np.uint8, nbytes).view(dtype).reshape(shape)
+
+    def free(self) -> None:
+        if self.pointer:
+            self.array = None
+            _lib.call("dg_host_free", c_void_p(self.pointer))
+            self.pointer = None
+
+
+class Event:
+    """A CUDA event recorded on the device's stream."""
+
+    def __init__(self, device: "Device"):
+        handle = c_void_p()
+        _lib.call("dg_event_create", device.handle, ctypes.byref(handle))
+        self.handle = handle
+
+    def record(self) -> None:
+        _lib.call("dg_event_record", self.handle)
+
+    def elapsed_ms(self, end: "Event") -> float:
+        ms = ctypes.c_float()
+        _lib.call("dg_event_elapsed", self.handle, end.handle, ctypes.byref(ms))
+        return ms.value
+
+    def destroy(self) -> None:
+        if self.handle:
+            _lib.call("dg_event_destroy", self.handle)
+            self.handle = None
 
 
 class Texture:
@@ -170,6 +216,22 @@ class Device:
         out = c_uint64()
         _lib.call("dg_context_launch_count", self.handle, ctypes.byref(out))
         return out.value
+
+    def setKernelTiming(self, enabled: bool) -> None:
+        _lib.call("dg_context_set_kernel_timing", self.handle, int(enabled))
+
+    def kernelTimingReport(self) -> dict:
+        """{kernel name: (launches, total ms)} since the last report; synchronizes."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        _lib.call("dg_context_kernel_timing_report", self.handle, buf, len(buf))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, launches, ms = line.split()
+            out[name] = (int(launches), float(ms))
+        return out
+
+    def event(self) -> Event:
+        return Event(self)
 
     def destroy(self) -> None:
         if self.handle:

@@ -215,6 +215,18 @@ class Trainer:
         _lib.call("dg_trainer_last_loss", self.handle, ctypes.byref(out))
         return out.value
 
+    def lossValue(self) -> float:
+        """The last step's loss, summed on the GPU (8 bytes read back)."""
+        out = c_double()
+        _lib.call("dg_trainer_loss_value", self.handle, ctypes.byref(out))
+        return out.value
+
+    def nextView(self) -> int:
+        """Index of the view the next optimize() renders."""
+        out = ctypes.c_uint32()
+        _lib.call("dg_trainer_next_view", self.handle, ctypes.byref(out))
+        return out.value
+
     def evaluate(self, views, withSsim: bool = True) -> dict:
         arr = _views_c(views)
         psnr, ssim = c_double(), c_double()

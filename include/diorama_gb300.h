@@ -65,6 +65,25 @@ dg_status dg_context_synchronize(dg_context* ctx);
 dg_status dg_context_check(dg_context* ctx, uint32_t* bits);
 /* Number of kernels this library has launched through ctx (for launch accounting). */
 dg_status dg_context_launch_count(dg_context* ctx, uint64_t* out);
+/* Per-kernel timing: while enabled, every kernel launched outside graph capture is
+ * bracketed by CUDA events on the context's stream. The report (synchronizes, then
+ * clears) is one line per kernel name: "name launches total_ms". No reference
+ * counterpart (the reference only times whole frames, src/checks/tiles.ts:188-218). */
+dg_status dg_context_set_kernel_timing(dg_context* ctx, int32_t enabled);
+dg_status dg_context_kernel_timing_report(dg_context* ctx, char* text, uint64_t capacity);
+
+/* ---- events on the context's stream, for timing work enqueued through it
+ * (the reference's performance.now() around onSubmittedWorkDone, src/checks/depthSort.ts:148-168). */
+typedef struct dg_event dg_event;
+dg_status dg_event_create(dg_context* ctx, dg_event** out);
+dg_status dg_event_record(dg_event* event);
+/* Waits for `end`, then the milliseconds between the two records. */
+dg_status dg_event_elapsed(dg_event* start, dg_event* end, float* ms);
+dg_status dg_event_destroy(dg_event* event);
+
+/* ---- pinned host memory, for uploads that overlap GPU work. */
+dg_status dg_host_alloc(uint64_t bytes, void** out);
+dg_status dg_host_free(void* ptr);
 
 /* ---- buffers: device.createBuffer, queue.writeBuffer, readBuffer (src/readback.ts),
  *      encoder.clearBuffer, encoder.copyBufferToBuffer. New buffers are zero-filled. */
@@ -75,6 +94,9 @@ dg_status dg_buffer_destroy(dg_buffer* buffer);
 uint64_t dg_buffer_size(const dg_buffer* buffer);
 void* dg_buffer_device_pointer(const dg_buffer* buffer);
 dg_status dg_buffer_write(dg_buffer* buffer, uint64_t offset, const void* src, uint64_t bytes);
+/* Like dg_buffer_write, but src is pinned memory from dg_host_alloc that the caller
+ * keeps unchanged until the queue has run the copy (no snapshot is taken). */
+dg_status dg_buffer_write_pinned(dg_buffer* buffer, uint64_t offset, const void* src, uint64_t bytes);
 dg_status dg_buffer_read(dg_buffer* buffer, uint64_t offset, void* dst, uint64_t bytes);
 dg_status dg_buffer_clear(dg_buffer* buffer, uint64_t offset, uint64_t bytes);
 dg_status dg_buffer_copy(dg_buffer* src, uint64_t src_offset, dg_buffer* dst, uint64_t dst_offset, uint64_t bytes);
@@ -215,6 +237,13 @@ dg_status dg_trainer_reset_opacity(dg_trainer* t);
 /* exportRaw(): params (16 * count floats) and sh (45 * count floats). */
 dg_status dg_trainer_export_raw(dg_trainer* t, float* params, float* sh);
 dg_status dg_trainer_last_loss(dg_trainer* t, double* out);
+/* The same loss summed on the GPU in a fixed order (8 bytes come back instead of
+ * one float per pixel). */
+dg_status dg_trainer_loss_value(dg_trainer* t, double* out);
+/* The index of the view the next optimize() renders (shuffling a new round first
+ * if needed, exactly as optimize() would): lets a caller upload that view's photo
+ * just in time. */
+dg_status dg_trainer_next_view(dg_trainer* t, uint32_t* index);
 /* evaluate(views, withSsim): mean PSNR and SSIM of 8-bit-quantized renders, computed on the GPU. */
 dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint32_t view_count, int32_t with_ssim,
                               double* psnr, double* ssim);
