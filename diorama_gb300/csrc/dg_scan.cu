@@ -13,6 +13,8 @@
 #include "dg_scan.cuh"
 
 #include <cuda/atomic>
+#include <mutex>
+#include <string>
 
 namespace dg {
 
@@ -164,9 +166,69 @@ dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const 
   return DG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The scan for callers that cannot allocate device memory.
+//
+// Some callers must not call cudaMalloc or any allocating routine: code that runs
+// under a memory budget fixed up front, code that cannot tolerate the implicit
+// synchronization an allocation may cause, or hosts that own every allocation
+// themselves. For them, dg_prefix_sum_no_alloc keeps the scan's look-back state
+// (a ticket, an error word and one status word per 4096-value tile) in the
+// file-scope array below instead of a buffer it allocates. The array is sized for
+// NO_ALLOC_MAX_VALUES values and, like any __device__ variable, is held by every
+// GPU that loads the library until the process exits.
+constexpr uint32_t NO_ALLOC_MAX_VALUES = 1u << 24;
+constexpr uint32_t NO_ALLOC_MAX_TILES = NO_ALLOC_MAX_VALUES / SCAN_TILE;     // 4096
+constexpr size_t NO_ALLOC_BYTES = 256 + (size_t)NO_ALLOC_MAX_TILES * 8;      // ~32.25 KB
+static __device__ __align__(256) unsigned char g_no_alloc_scratch[NO_ALLOC_BYTES];
+
+// Host code must not use g_no_alloc_scratch's name as an address: on the host it
+// is only a stand-in for the symbol. The device address is looked up once per
+// device, with that device current, and kept here.
+constexpr int NO_ALLOC_MAX_DEVICES = 64;
+static void* g_no_alloc_address[NO_ALLOC_MAX_DEVICES] = {};
+static std::mutex g_no_alloc_lock;
+
+static dg_status no_alloc_scratch_address(void** out) {
+  int device = -1;
+  DG_CUDA(cudaGetDevice(&device));
+  DG_REQUIRE(device >= 0 && device < NO_ALLOC_MAX_DEVICES, "device index out of range for the no-alloc scan");
+  std::lock_guard<std::mutex> hold(g_no_alloc_lock);
+  if (!g_no_alloc_address[device]) {
+    void* ptr = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&ptr, g_no_alloc_scratch);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(no-alloc scan scratch)");
+    g_no_alloc_address[device] = ptr;
+  }
+  *out = g_no_alloc_address[device];
+  return DG_OK;
+}
+
 }  // namespace dg
 
 using namespace dg;
+
+extern "C" dg_status dg_prefix_sum_no_alloc(void* stream, uint32_t* data, uint32_t count, uint32_t* total) {
+  DG_REQUIRE(data && total, "NULL argument");
+  if (count > NO_ALLOC_MAX_VALUES)
+    return fail(DG_ERROR_INVALID_ARGUMENT, "dg_prefix_sum_no_alloc scans at most " +
+                                               std::to_string(NO_ALLOC_MAX_VALUES) + " values; got " +
+                                               std::to_string(count));
+  void* scratch = nullptr;
+  DG_TRY(no_alloc_scratch_address(&scratch));
+  auto s = static_cast<cudaStream_t>(stream);
+  const uint32_t tiles = std::max(1u, ceil_div(count, SCAN_TILE));
+  auto* ticket = static_cast<uint32_t*>(scratch);
+  auto* error = ticket + 1;
+  auto* status = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + 256);
+  // The previous call left its ticket and status words behind: clear what this
+  // call's tiles will read (the error word keeps any earlier give-up).
+  DG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
+  DG_CUDA(cudaMemsetAsync(status, 0, (size_t)tiles * sizeof(uint64_t), s));
+  scan_kernel<<<tiles, SCAN_THREADS, 0, s>>>(data, count, nullptr, total, status, ticket, error);
+  DG_CUDA(cudaGetLastError());
+  return DG_OK;
+}
 
 struct dg_prefix_sum {
   dg_context* ctx;

@@ -109,6 +109,18 @@ dg_status dg_prefix_sum_encode(dg_prefix_sum* scan);
 /* .total: element 0 holds the sum once the scan has run. */
 dg_buffer* dg_prefix_sum_total(dg_prefix_sum* scan);
 dg_status dg_prefix_sum_destroy(dg_prefix_sum* scan);
+/* The same exclusive scan for callers that cannot allocate device memory (a fixed
+ * memory budget, no implicit synchronization allowed, or a host that owns every
+ * allocation). It has no counterpart in the reference. It allocates nothing: the
+ * scan's look-back state lives in a ~32 KB array inside the library that every
+ * GPU loading the library holds until exit. data (count u32 values, scanned in
+ * place) and total (one u32) are device pointers the caller owns; stream is a
+ * cudaStream_t (NULL for the legacy default stream) on the current device.
+ * At most 16,777,216 values; larger counts return DG_ERROR_INVALID_ARGUMENT.
+ * The first call on each device looks up the array's device address, so make
+ * that first call before any stream capture. All calls share the one array, so
+ * calls whose work overlaps on the GPU (other streams, other threads) race. */
+dg_status dg_prefix_sum_no_alloc(void* stream, uint32_t* data, uint32_t count, uint32_t* total);
 
 /* ---- RadixSort (src/radixSort.ts:27-142): stable LSD sort of u32 keys (high_bits = 0)
  * or u64 keys stored as (low word, high word) sorting high_bits bits of the high word,
