@@ -228,10 +228,15 @@ __device__ __forceinline__ unsigned char to_unorm8(float v) {
   return (unsigned char)__float2uint_rn(clampf(v, 0.0f, 1.0f) * 255.0f);
 }
 
-// src/shaders/rasterize.wgsl:32-100: one CTA per 16x16 tile, one thread per pixel.
-// The tile's splats are staged 256 at a time through shared memory; a pixel stops
-// before the splat that would take its transmittance below 1e-4, and the CTA stops
-// loading once every pixel has stopped.
+// src/shaders/rasterize.wgsl:32-100: one CTA per 16x16 tile, one thread per pixel,
+// each warp an 8x4 block. The tile's list is walked in windows of 256 entries;
+// each window is staged in shared memory keeping only the splats that can reach a
+// warp block (a splat rejected there has alpha below 1/255 at every pixel of the
+// block, so skipping it changes nothing), and a warp skips splats outside its
+// block. At a pixel, a power under the splat's cutoff skips the exp with the same
+// outcome. A pixel stops before the splat that would take its transmittance below
+// 1e-4, and the CTA stops once every pixel has. Results are bit-identical to the
+// plain loop over every list entry.
 __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict__ camera,
                                                         const float4* __restrict__ raster_params,
                                                         const float* __restrict__ splats,
@@ -239,52 +244,44 @@ __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict
                                                         const uint2* __restrict__ ranges, uchar4* __restrict__ target,
                                                         float4* __restrict__ pixel_color,
                                                         uint32_t* __restrict__ pixel_last) {
-  __shared__ float2 s_mean[BLEND_BATCH];
-  __shared__ float4 s_conic[BLEND_BATCH];  // a, b, c, opacity
-  __shared__ float4 s_color[BLEND_BATCH];
+  __shared__ BlendStage st;
   const uint32_t tid = threadIdx.x;
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
   const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
   const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
-  const uint32_t px = blockIdx.x * TILE + (tid % TILE), py = blockIdx.y * TILE + (tid / TILE);
+  const uint32_t px = blockIdx.x * TILE + tile_pixel_x(tid), py = blockIdx.y * TILE + tile_pixel_y(tid);
   const bool inside = (float)px < vpx && (float)py < vpy;
   const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+  const float tile_x0 = (float)(blockIdx.x * TILE), tile_y0 = (float)(blockIdx.y * TILE);
+  const uint32_t warp_bit = 1u << (tid >> 5);
   const uint2 run = ranges[tile];
   float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
   bool done = !inside;
-  uint32_t visited = 0, last = 0;
+  uint32_t last = 0;
   for (uint32_t start = run.x; start < run.y; start += BLEND_BATCH) {
     if (__syncthreads_count(done) == BLEND_BATCH) break;
-    const uint32_t k = start + tid;
-    if (k < run.y) {
-      const float4* s = reinterpret_cast<const float4*>(splats + (size_t)pair_splats[k] * FLOATS_PER_SPLAT);
-      const float4 s0 = s[0], s1 = s[1], s2 = s[2];
-      s_mean[tid] = make_float2(s0.x, s0.y);
-      s_conic[tid] = make_float4(s1.x, s1.y, s1.z, s2.w);
-      s_color[tid] = s2;
-    }
-    __syncthreads();
-    const uint32_t batch = min((uint32_t)BLEND_BATCH, run.y - start);
-    for (uint32_t j = 0; j < batch && !done; j++) {
-      visited++;
-      const float2 m = s_mean[j];
-      const float4 con = s_conic[j];
-      const float dx = cx - m.x, dy = cy - m.y;
-      const float power = -0.5f * (con.x * dx * dx + con.z * dy * dy) - con.y * dx * dy;
+    const uint32_t staged = stage_window(st, splats, pair_splats, run.x, start, min(start + BLEND_BATCH, run.y),
+                                         tile_x0, tile_y0);
+    for (uint32_t j = 0; j < staged && !done; j++) {
+      if (!(st.mask[j] & warp_bit)) continue;
+      const float2 m = st.mean[j];
+      const float4 q = st.quad[j];
+      const float power = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
+      if (power < q.w) continue;  // alpha < 1/255 for certain
       if (power > 0.0f) continue;
-      const float alpha = fminf(0.99f, con.w * exp_blend(power));
+      const float4 c = st.color[j];
+      const float alpha = fminf(0.99f, c.w * exp_blend(power));
       if (alpha < 1.0f / 255.0f) continue;
       const float remaining = T * (1.0f - alpha);
       if (remaining < 0.0001f) {
         done = true;
         continue;
       }
-      const float4 c = s_color[j];
       r = r + c.x * alpha * T;
       g = g + c.y * alpha * T;
       b = b + c.z * alpha * T;
       T = remaining;
-      last = visited;
+      last = st.pos[j] + 1;
     }
   }
   if (inside) {
@@ -295,380 +292,6 @@ __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict
     pixel_last[p] = last;
     if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
   }
-}
-
-// Sums 16 values over the warp. Afterwards lanes 2s and 2s+1 both hold the total
-// of value s: each halving step swaps half of the values with the partner lane,
-// so 8 + 4 + 2 + 1 + 1 shuffles move everything instead of 5 per value.
-__device__ __forceinline__ float warp_transpose_reduce16(float v[16], int lane) {
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const bool upper = lane & 16;
-    float send = upper ? v[k] : v[k + 8];
-    float keep = upper ? v[k + 8] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-  }
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const bool upper = lane & 8;
-    float send = upper ? v[k] : v[k + 4];
-    float keep = upper ? v[k + 4] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-  }
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    const bool upper = lane & 4;
-    float send = upper ? v[k] : v[k + 2];
-    float keep = upper ? v[k + 2] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-  }
-  {
-    const bool upper = lane & 2;
-    float send = upper ? v[0] : v[1];
-    float keep = upper ? v[1] : v[0];
-    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-  }
-  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
-}
-
-// src/shaders/rasterizeBackward.wgsl:50-163. Each pixel walks its tile's list back
-// to front from its last blended splat, recovering the transmittance in front of
-// each splat by dividing the final one by (1 - alpha). A splat's 9 gradient shares
-// are summed over each warp's 32 pixels with shuffles, the 8 warps' sums meet in
-// shared memory, and each batch's per-splat totals go to global memory with one
-// atomic add per nonzero value. Splats past the tile's largest `last` cannot
-// contribute and are skipped.
-__global__ void __launch_bounds__(256) rasterize_backward_kernel(
-    const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
-    const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const float4* __restrict__ pixel_color,
-    const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads) {
-  __shared__ float2 s_mean[BWD_BATCH];
-  __shared__ float4 s_conic[BWD_BATCH];
-  __shared__ float4 s_color[BWD_BATCH];
-  __shared__ uint32_t s_index[BWD_BATCH];
-  __shared__ float s_acc[BWD_BATCH * SPLAT_GRADS];
-  __shared__ uint32_t s_max_last;
-  const uint32_t tid = threadIdx.x;
-  const int lane = tid & 31;
-  const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
-  const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
-  const uint32_t px = blockIdx.x * TILE + (tid % TILE), py = blockIdx.y * TILE + (tid / TILE);
-  const bool inside = (float)px < vpx && (float)py < vpy;
-  const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-  const uint2 run = ranges[tile];
-  float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
-  uint32_t last = 0;
-  if (inside) {
-    const uint32_t p = py * (uint32_t)vpx + px;
-    Tf = pixel_color[p].w;
-    last = pixel_last[p];
-    const float4 pg = pixel_grads[p];
-    pgx = pg.x;
-    pgy = pg.y;
-    pgz = pg.z;
-  }
-  if (tid == 0) s_max_last = 0;
-  for (uint32_t k = tid; k < BWD_BATCH * SPLAT_GRADS; k += 256) s_acc[k] = 0.0f;
-  __syncthreads();
-  if (last) atomicMax(&s_max_last, last);
-  __syncthreads();
-  const float4 bg = raster_params[0];
-  float bg_grad = bg.x * pgx;
-  bg_grad = bg_grad + bg.y * pgy;
-  bg_grad = bg_grad + bg.z * pgz;
-  float T = Tf;
-  float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
-  float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
-  const uint32_t end = run.x + s_max_last;
-  for (uint32_t batch_end = end; batch_end > run.x;) {
-    const uint32_t batch_start = batch_end - run.x > BWD_BATCH ? batch_end - BWD_BATCH : run.x;
-    const uint32_t n = batch_end - batch_start;
-    if (tid < n) {
-      const uint32_t index = pair_splats[batch_start + tid];
-      const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
-      const float4 s0 = s[0], s1 = s[1], s2 = s[2];
-      s_mean[tid] = make_float2(s0.x, s0.y);
-      s_conic[tid] = make_float4(s1.x, s1.y, s1.z, s2.w);
-      s_color[tid] = s2;
-      s_index[tid] = index;
-    }
-    __syncthreads();
-    for (uint32_t slot = n; slot > 0; slot--) {
-      const uint32_t j = slot - 1;
-      float v[16];
-#pragma unroll
-      for (int q = 0; q < 16; q++) v[q] = 0.0f;
-      bool contributes = false;
-      if (inside && batch_start + j - run.x < last) {
-        const float2 m = s_mean[j];
-        const float4 con = s_conic[j];
-        const float dx = cx - m.x, dy = cy - m.y;
-        const float power = -0.5f * (con.x * dx * dx + con.z * dy * dy) - con.y * dx * dy;
-        if (power <= 0.0f) {
-          const float G = exp_blend(power);
-          const float alpha = fminf(0.99f, con.w * G);
-          if (alpha >= 1.0f / 255.0f) {
-            contributes = true;
-            const float4 c = s_color[j];
-            T = T / (1.0f - alpha);
-            bhx = na * ncx + (1.0f - na) * bhx;
-            bhy = na * ncy + (1.0f - na) * bhy;
-            bhz = na * ncz + (1.0f - na) * bhz;
-            na = alpha;
-            ncx = c.x;
-            ncy = c.y;
-            ncz = c.z;
-            float dotv = (c.x - bhx) * pgx;
-            dotv = dotv + (c.y - bhy) * pgy;
-            dotv = dotv + (c.z - bhz) * pgz;
-            const float alpha_grad = T * dotv - Tf / (1.0f - alpha) * bg_grad;
-            const float power_grad = alpha_grad * con.w * G;
-            v[0] = power_grad * (con.x * dx + con.y * dy);
-            v[1] = power_grad * (con.y * dx + con.z * dy);
-            v[2] = power_grad * (-0.5f * dx * dx);
-            v[3] = power_grad * (-dx * dy);
-            v[4] = power_grad * (-0.5f * dy * dy);
-            v[5] = alpha_grad * G;
-            v[6] = alpha * T * pgx;
-            v[7] = alpha * T * pgy;
-            v[8] = alpha * T * pgz;
-          }
-        }
-      }
-      if (__any_sync(0xffffffffu, contributes)) {
-        const float total = warp_transpose_reduce16(v, lane);
-        const int which = lane >> 1;
-        if ((lane & 1) == 0 && which < (int)SPLAT_GRADS && total != 0.0f)
-          atomicAdd(&s_acc[j * SPLAT_GRADS + which], total);
-      }
-    }
-    __syncthreads();
-    for (uint32_t k = tid; k < n * SPLAT_GRADS; k += 256) {
-      const float total = s_acc[k];
-      if (total != 0.0f) {
-        atomicAdd(&splat_grads[(size_t)s_index[k / SPLAT_GRADS] * SPLAT_GRADS + k % SPLAT_GRADS], total);
-        s_acc[k] = 0.0f;
-      }
-    }
-    __syncthreads();
-    batch_end = batch_start;
-  }
-}
-
-// src/shaders/preprocessBackward.wgsl:28-181: one thread per Gaussian. Writes the
-// 16-float Gaussian gradient (slots 7 and 15 zero) and the 45 SH gradients.
-__global__ void __launch_bounds__(128) preprocess_backward_kernel(
-    const Camera* __restrict__ camera, const float* __restrict__ gaussians, const float* __restrict__ sh,
-    uint32_t count, const uint32_t* __restrict__ scene_params, const float* __restrict__ splats,
-    const float* __restrict__ splat_grads, float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
-  __shared__ Camera s_cam;
-  load_camera(s_cam, camera);
-  __syncthreads();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const Camera& cam = s_cam;
-  const uint32_t degree = scene_params[0];
-  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
-  float* gg = gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN;
-  float* sg = sh_grads + (size_t)i * SH_REST_FLOATS;
-  float out[16];
-#pragma unroll
-  for (int k = 0; k < 16; k++) out[k] = 0.0f;
-  bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
-  if (!visible) {
-#pragma unroll
-    for (int k = 0; k < 4; k++) reinterpret_cast<float4*>(gg)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (uint32_t k = 0; k < SH_REST_FLOATS; k++) sg[k] = 0.0f;
-    return;
-  }
-  float grad[9];
-#pragma unroll
-  for (int k = 0; k < 9; k++) grad[k] = splat_grads[(size_t)i * SPLAT_GRADS + k];
-  float g[16];
-  {
-    const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      float4 q = gp[k];
-      g[4 * k] = q.x; g[4 * k + 1] = q.y; g[4 * k + 2] = q.z; g[4 * k + 3] = q.w;
-    }
-  }
-  Projection p;
-  project(cam, g, p);
-  const float depth = p.depth;
-  const float ratio0 = p.t[0] / depth, ratio1 = p.t[1] / depth;
-  const float free0 = fabsf(ratio0) > p.limit[0] ? 0.0f : 1.0f;
-  const float free1 = fabsf(ratio1) > p.limit[1] ? 0.0f : 1.0f;
-  const float depth2 = depth * depth, depth3 = depth2 * depth;
-  const float a = p.a, b = p.b, c = p.c, det = p.det;
-  // 1. conic -> 2D covariance
-  const float det2 = det * det;
-  const float a_grad = (-c * c * grad[2] + b * c * grad[3] - b * b * grad[4]) / det2;
-  const float b_grad = (2.0f * b * c * grad[2] - (det + 2.0f * b * b) * grad[3] + 2.0f * a * b * grad[4]) / det2;
-  const float c_grad = (-b * b * grad[2] + a * b * grad[3] - a * a * grad[4]) / det2;
-  const float G2[2][2] = {{a_grad, 0.5f * b_grad}, {0.5f * b_grad, c_grad}};
-  // 2. Σ' = T Σ Tᵀ with T = J W
-  float Gjw[3][2];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 2; row++) {
-      float v = G2[0][row] * p.jw[col][0];
-      v = v + G2[1][row] * p.jw[col][1];
-      Gjw[col][row] = v;
-    }
-  float cov3d_grad[3][3];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 3; row++) {
-      float v = p.jw[row][0] * Gjw[col][0];
-      v = v + p.jw[row][1] * Gjw[col][1];
-      cov3d_grad[col][row] = v;
-    }
-  float t3[3][2];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 2; row++) {
-      float v = (2.0f * Gjw[0][row]) * p.cov3d[col][0];
-      v = v + (2.0f * Gjw[1][row]) * p.cov3d[col][1];
-      v = v + (2.0f * Gjw[2][row]) * p.cov3d[col][2];
-      t3[col][row] = v;
-    }
-  float jg[3][2];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 2; row++) {
-      float v = t3[0][row] * p.w[0][col];
-      v = v + t3[1][row] * p.w[1][col];
-      v = v + t3[2][row] * p.w[2][col];
-      jg[col][row] = v;
-    }
-  // 3. J moves with t
-  float tg[3];
-  tg[0] = jg[2][0] * free0 * p.focal[0] / depth2;
-  tg[1] = jg[2][1] * free1 * -p.focal[1] / depth2;
-  tg[2] = 0.0f;
-  const float depth_grad = jg[0][0] * (-p.focal[0] / depth2) + jg[1][1] * (p.focal[1] / depth2) +
-                           jg[2][0] * (-(1.0f + free0) * p.focal[0] * p.tx / depth3) +
-                           jg[2][1] * ((1.0f + free1) * p.focal[1] * p.ty / depth3);
-  tg[2] = tg[2] - depth_grad;
-  // 4. the 2D center
-  float clip[4];
-#pragma unroll
-  for (int row = 0; row < 4; row++) {
-    float v = cam.proj[0 * 4 + row] * p.t[0];
-    v = v + cam.proj[1 * 4 + row] * p.t[1];
-    v = v + cam.proj[2 * 4 + row] * p.t[2];
-    v = v + cam.proj[3 * 4 + row] * 1.0f;
-    clip[row] = v;
-  }
-  const float ng0 = grad[0] * 0.5f * cam.viewport[0], ng1 = grad[1] * -0.5f * cam.viewport[1];
-  float ndc_dot = ng0 * clip[0];
-  ndc_dot = ndc_dot + ng1 * clip[1];
-  const float clip_grad[4] = {ng0 / clip[3], ng1 / clip[3], 0.0f, -ndc_dot / (clip[3] * clip[3])};
-#pragma unroll
-  for (int col = 0; col < 3; col++) {
-    float v = cam.proj[col * 4 + 0] * clip_grad[0];
-    v = v + cam.proj[col * 4 + 1] * clip_grad[1];
-    v = v + cam.proj[col * 4 + 2] * clip_grad[2];
-    v = v + cam.proj[col * 4 + 3] * clip_grad[3];
-    tg[col] = tg[col] + v;
-  }
-  // 5. colour
-  float campos[3], off[3], dir[3], basis[15];
-  camera_position(cam, campos);
-  off[0] = g[0] - campos[0];
-  off[1] = g[1] - campos[1];
-  off[2] = g[2] - campos[2];
-  const float dist = normalize3(off, dir);
-  sh_basis(dir, basis);
-  const float* coef = sh + (size_t)i * SH_REST_FLOATS;
-  float raw_color[3] = {g[12], g[13], g[14]};
-  for (uint32_t k = 0; k < basis_count; k++)
-#pragma unroll
-    for (int ch = 0; ch < 3; ch++) raw_color[ch] = raw_color[ch] + basis[k] * coef[k * 3 + ch];
-  float raw_grad[3];
-#pragma unroll
-  for (int ch = 0; ch < 3; ch++) raw_grad[ch] = raw_color[ch] < 0.0f ? 0.0f : grad[6 + ch];
-  float dgrad[3] = {0.0f, 0.0f, 0.0f};
-  {
-    float bgrad[15][3];
-    sh_basis_gradient(dir, bgrad);
-    for (uint32_t k = 0; k < SH_REST_FLOATS / 3; k++) {
-      if (k < basis_count) {
-#pragma unroll
-        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = basis[k] * raw_grad[ch];
-        float d = coef[k * 3] * raw_grad[0];
-        d = d + coef[k * 3 + 1] * raw_grad[1];
-        d = d + coef[k * 3 + 2] * raw_grad[2];
-#pragma unroll
-        for (int ax = 0; ax < 3; ax++) dgrad[ax] = dgrad[ax] + bgrad[k][ax] * d;
-      } else {
-#pragma unroll
-        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = 0.0f;
-      }
-    }
-  }
-  float dd = dir[0] * dgrad[0];
-  dd = dd + dir[1] * dgrad[1];
-  dd = dd + dir[2] * dgrad[2];
-  // 6. position
-#pragma unroll
-  for (int col = 0; col < 3; col++) {
-    float v = p.w[col][0] * tg[0];
-    v = v + p.w[col][1] * tg[1];
-    v = v + p.w[col][2] * tg[2];
-    out[col] = v + (dgrad[col] - dir[col] * dd) / dist;
-  }
-  // 7. scale and rotation
-  float mg[3][3];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 3; row++) {
-      float v = 2.0f * cov3d_grad[0][row] * p.m[col][0];
-      v = v + 2.0f * cov3d_grad[1][row] * p.m[col][1];
-      v = v + 2.0f * cov3d_grad[2][row] * p.m[col][2];
-      mg[col][row] = v;
-    }
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    float v = mg[k][0] * p.r[k][0];
-    v = v + mg[k][1] * p.r[k][1];
-    v = v + mg[k][2] * p.r[k][2];
-    out[4 + k] = v;
-  }
-  float rg[3][3];
-#pragma unroll
-  for (int col = 0; col < 3; col++)
-#pragma unroll
-    for (int row = 0; row < 3; row++) rg[col][row] = mg[col][row] * g[4 + col];
-  const float qw = p.q[0], qx = p.q[1], qy = p.q[2], qz = p.q[3];
-  const float g00 = rg[0][0], g01 = rg[1][0], g02 = rg[2][0];
-  const float g10 = rg[0][1], g11 = rg[1][1], g12 = rg[2][1];
-  const float g20 = rg[0][2], g21 = rg[1][2], g22 = rg[2][2];
-  float qg[4];
-  qg[0] = 2.0f * (-qz * g01 + qy * g02 + qz * g10 - qx * g12 - qy * g20 + qx * g21);
-  qg[1] = 2.0f * (qy * g01 + qz * g02 + qy * g10 - 2.0f * qx * g11 - qw * g12 + qz * g20 + qw * g21 - 2.0f * qx * g22);
-  qg[2] = 2.0f * (-2.0f * qy * g00 + qx * g01 + qw * g02 + qx * g10 + qz * g12 - qw * g20 + qz * g21 - 2.0f * qy * g22);
-  qg[3] = 2.0f * (-2.0f * qz * g00 - qw * g01 + qx * g02 + qw * g10 - 2.0f * qz * g11 + qy * g12 + qx * g20 + qy * g21);
-  float qd = p.q[0] * qg[0];
-  qd = qd + p.q[1] * qg[1];
-  qd = qd + p.q[2] * qg[2];
-  qd = qd + p.q[3] * qg[3];
-  out[3] = grad[5];
-#pragma unroll
-  for (int k = 0; k < 4; k++) out[8 + k] = (qg[k] - p.q[k] * qd) / p.qlen;
-  out[12] = raw_grad[0];
-  out[13] = raw_grad[1];
-  out[14] = raw_grad[2];
-#pragma unroll
-  for (int k = 0; k < 4; k++)
-    reinterpret_cast<float4*>(gg)[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
 }
 
 // The empty-scene render pass: clear the target to the background (src/gaussianRenderer.ts:178-184).
@@ -801,12 +424,7 @@ dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr) {
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads) {
   dg_context* ctx = tr->ctx;
   DG_CUDA(cudaMemsetAsync(splat_grads->ptr, 0, (size_t)tr->count * SPLAT_GRADS * 4, ctx->stream));
-  DG_LAUNCH(ctx, "rasterize_backward",
-            rasterize_backward_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
-                typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
-                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads)));
-  return DG_OK;
+  return launch_rasterize_backward(tr, pixel_grads, splat_grads);
 }
 
 // ------------------------------------------------------------ GaussianRenderer
@@ -881,12 +499,7 @@ dg_status renderer_ensure_gradients(dg_renderer* r) {
 dg_status renderer_launch_backward(dg_renderer* r, dg_buffer* pixel_grads, bool write_gaussian_grads) {
   DG_TRY(rasterizer_launch_backward(r->rasterizer, pixel_grads, r->grad_splats));
   if (!write_gaussian_grads || r->count == 0) return DG_OK;
-  DG_LAUNCH(r->ctx, "preprocess_backward",
-            preprocess_backward_kernel<<<ceil_div(r->count, 128), 128, 0, r->ctx->stream>>>(
-                typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
-                typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats),
-                typed<float>(r->grad_gaussians), typed<float>(r->grad_sh)));
-  return DG_OK;
+  return launch_preprocess_backward(r);
 }
 
 const Camera* renderer_camera(dg_renderer* r) { return typed<const Camera>(r->camera); }

@@ -74,6 +74,8 @@ dg_status renderer_prepare(dg_renderer* r, const dg_camera* camera, const float 
 dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target);
 dg_status renderer_ensure_gradients(dg_renderer* r);
 dg_status renderer_launch_backward(dg_renderer* r, dg_buffer* pixel_grads, bool write_gaussian_grads);
-// The preprocess backward alone, for callers that fuse the Adam step into it.
 const Camera* renderer_camera(dg_renderer* r);
+// The backward kernels (dg_render_bwd.cu).
+dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
+dg_status launch_preprocess_backward(dg_renderer* r);
 }  // namespace dg

@@ -201,6 +201,123 @@ __device__ __forceinline__ void sh_basis_gradient(const float d[3], float g[15][
   g[14][0] = C3[6] * (3.0f * xx - 3.0f * yy); g[14][1] = C3[6] * (-6.0f * x * y); g[14][2] = C3[6] * 0.0f;
 }
 
+// ------------------------------------------------------------------ blending
+// The exponent of a splat at a pixel, `power = -0.5 (a dx^2 + c dy^2) - b dx dy`
+// (src/shaders/rasterize.wgsl:68), from A = -0.5 a and C = -0.5 c. Scaling by
+// -0.5 is exact, so ((A dx) dx + (C dy) dy) equals -0.5 ((a dx) dx + (c dy) dy)
+// bit for bit. Written with round-to-nearest intrinsics, which the compiler never
+// fuses, so the forward and backward passes compute identical powers whatever
+// their --fmad setting.
+__device__ __forceinline__ float blend_power(float A, float b, float C, float dx, float dy) {
+  const float s = __fadd_rn(__fmul_rn(__fmul_rn(A, dx), dx), __fmul_rn(__fmul_rn(C, dy), dy));
+  return __fsub_rn(s, __fmul_rn(__fmul_rn(b, dx), dy));
+}
+
+// A power below which alpha = opacity * exp(power) is certainly under 1/255, so
+// the exp can be skipped with the same outcome: ln(1 / (255 opacity)), lowered by
+// 1e-3 to cover the float error of exp_blend and of the product (~1e-7 relative).
+__device__ __forceinline__ float blend_cutoff(float opacity) {
+  return logf(1.0f / (255.0f * opacity)) - 1e-3f;
+}
+
+// Whether a splat can reach any pixel center of the rectangle
+// [dxl, dxh] x [dyl, dyh] (offsets pixel - mean): the maximum of the concave
+// quadratic q = A dx^2 - b dx dy + C dy^2 over the rectangle, compared with the
+// cutoff. The maximum is at the mean if the rectangle holds it, else on an edge,
+// where each 1D maximum is clamped to the edge. The margin covers the rounding
+// of both this maximum and the per-pixel power (a few ulps of the terms' sizes),
+// so a splat this rejects would have been skipped at every pixel anyway.
+__device__ __forceinline__ bool rect_reachable(float A, float b, float C, float kx, float ky, float cut, float dxl,
+                                               float dxh, float dyl, float dyh) {
+  if (dxl <= 0.0f && dxh >= 0.0f && dyl <= 0.0f && dyh >= 0.0f) return 0.0f >= cut;
+  auto q = [&](float dx, float dy) { return A * dx * dx + C * dy * dy - b * dx * dy; };
+  const float y1 = fminf(fmaxf(ky * dxl, dyl), dyh), y2 = fminf(fmaxf(ky * dxh, dyl), dyh);
+  const float x1 = fminf(fmaxf(kx * dyl, dxl), dxh), x2 = fminf(fmaxf(kx * dyh, dxl), dxh);
+  const float qmax = fmaxf(fmaxf(q(dxl, y1), q(dxh, y2)), fmaxf(q(x1, dyl), q(x2, dyh)));
+  const float mx = fmaxf(fabsf(dxl), fabsf(dxh)), my = fmaxf(fabsf(dyl), fabsf(dyh));
+  const float terms = fabsf(A) * mx * mx + fabsf(C) * my * my + fabsf(b) * mx * my;
+  return qmax + 1e-6f * terms + 1e-6f >= cut;
+}
+
+// The pixel blocks of a 16x16 tile: warp w covers the 8x4 block at
+// (8 * (w & 1), 4 * (w >> 1)); lane l is pixel (l & 7, l >> 3) of it.
+__device__ __forceinline__ uint32_t tile_pixel_x(uint32_t tid) { return ((tid >> 5) & 1u) * 8u + (tid & 7u); }
+__device__ __forceinline__ uint32_t tile_pixel_y(uint32_t tid) { return (tid >> 6) * 4u + ((tid >> 3) & 3u); }
+
+// For one splat and one tile, a bit per warp block the splat can reach. Also
+// returns the staged form of the splat's quadratic (A, b, C, cut).
+__device__ __forceinline__ uint32_t warp_reach_mask(float mx, float my, float a, float b, float c, float opacity,
+                                                    float tile_x0, float tile_y0, float4& quad) {
+  const float A = -0.5f * a, C = -0.5f * c;
+  const float cut = blend_cutoff(opacity);
+  quad = make_float4(A, b, C, cut);
+  if (!(cut < 0.0f)) return 0u;  // opacity below 1/255 (or not a number): it never blends
+  // argmax of q along dx for a fixed dy is kx dy (dq/ddx = 2A dx - b dy = 0), and along dy is ky dx.
+  const float kx = b / (2.0f * A), ky = b / (2.0f * C);
+  uint32_t mask = 0;
+#pragma unroll
+  for (int w = 0; w < 8; w++) {
+    const float x0 = tile_x0 + (float)((w & 1) * 8) + 0.5f, y0 = tile_y0 + (float)((w >> 1) * 4) + 0.5f;
+    if (rect_reachable(A, b, C, kx, ky, cut, x0 - mx, x0 + 7.0f - mx, y0 - my, y0 + 3.0f - my)) mask |= 1u << w;
+  }
+  return mask;
+}
+
+// A window of up to 256 entries of a tile's sorted list, staged in shared memory:
+// only the splats that reach at least one of the tile's warp blocks, in list
+// order, each with its position in the list (for pixel_last) and its warp mask.
+constexpr int STAGE = 256;
+struct BlendStage {
+  float2 mean[STAGE];
+  float4 quad[STAGE];   // A = -0.5 a, b, C = -0.5 c, cutoff
+  float4 color[STAGE];  // rgb, opacity
+  uint32_t pos[STAGE];  // position in the tile's list
+  uint32_t index[STAGE];
+  uint8_t mask[STAGE];
+  uint32_t warp_count[STAGE / 32];
+};
+
+// Stages list entries [lo, hi) of the tile whose sorted run starts at run_x;
+// returns how many were kept. Every thread of the 256-thread CTA must call it.
+__device__ __forceinline__ uint32_t stage_window(BlendStage& st, const float* __restrict__ splats,
+                                                 const uint32_t* __restrict__ pair_splats, uint32_t run_x,
+                                                 uint32_t lo, uint32_t hi, float tile_x0, float tile_y0) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t k = lo + tid;
+  uint32_t mask = 0, index = 0;
+  float2 mean = make_float2(0.f, 0.f);
+  float4 quad = make_float4(0.f, 0.f, 0.f, 0.f), color = quad;
+  if (k < hi) {
+    index = pair_splats[k];
+    const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
+    const float4 s0 = s[0], s1 = s[1];
+    color = s[2];
+    mean = make_float2(s0.x, s0.y);
+    mask = warp_reach_mask(s0.x, s0.y, s1.x, s1.y, s1.z, color.w, tile_x0, tile_y0, quad);
+  }
+  const uint32_t kept = __ballot_sync(0xffffffffu, mask != 0u);
+  if (lane == 0) st.warp_count[warp] = __popc(kept);
+  __syncthreads();
+  uint32_t base = 0, total = 0;
+#pragma unroll
+  for (uint32_t w = 0; w < STAGE / 32; w++) {
+    const uint32_t c = st.warp_count[w];
+    base += w < warp ? c : 0u;
+    total += c;
+  }
+  if (mask) {
+    const uint32_t at = base + __popc(kept & ((1u << lane) - 1u));
+    st.mean[at] = mean;
+    st.quad[at] = quad;
+    st.color[at] = color;
+    st.pos[at] = k - run_x;
+    st.index[at] = index;
+    st.mask[at] = (uint8_t)mask;
+  }
+  __syncthreads();
+  return total;
+}
+
 // tile_count / tile_rect (src/shaders/common.wgsl:31-42).
 __device__ __forceinline__ uint2 tile_grid(const Camera& cam) {
   return make_uint2(((uint32_t)cam.viewport[0] + TILE - 1u) / TILE, ((uint32_t)cam.viewport[1] + TILE - 1u) / TILE);
