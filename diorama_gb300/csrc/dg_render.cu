@@ -16,8 +16,6 @@ namespace {
 constexpr int PRE_THREADS = 128;
 constexpr int DUP_THREADS = 256;
 constexpr int RANGE_THREADS = 256;
-constexpr int BLEND_BATCH = 256;
-constexpr int BWD_BATCH = 256;
 
 __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
   const float* s = reinterpret_cast<const float*>(src);
@@ -229,14 +227,14 @@ __device__ __forceinline__ unsigned char to_unorm8(float v) {
 }
 
 // src/shaders/rasterize.wgsl:32-100: one CTA per 16x16 tile, one thread per pixel,
-// each warp an 8x4 block. The tile's list is walked in windows of 256 entries;
-// each window is staged in shared memory keeping only the splats that can reach a
-// warp block (a splat rejected there has alpha below 1/255 at every pixel of the
-// block, so skipping it changes nothing), and a warp skips splats outside its
-// block. At a pixel, a power under the splat's cutoff skips the exp with the same
-// outcome. A pixel stops before the splat that would take its transmittance below
-// 1e-4, and the CTA stops once every pixel has. Results are bit-identical to the
-// plain loop over every list entry.
+// each warp an 8x4 block that walks the tile's list on its own (no CTA barriers,
+// so a warp whose pixels are all done stops without waiting for the others). The
+// list is staged 32 entries at a time into the warp's slice of shared memory,
+// keeping only splats that can reach the block: a splat rejected there has alpha
+// below 1/255 at every pixel of the block, so skipping it changes nothing. At a
+// pixel, a power under the splat's cutoff skips the exp with the same outcome. A
+// pixel stops before the splat that would take its transmittance below 1e-4.
+// Results are bit-identical to the plain loop over every list entry.
 __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict__ camera,
                                                         const float4* __restrict__ raster_params,
                                                         const float* __restrict__ splats,
@@ -244,26 +242,26 @@ __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict
                                                         const uint2* __restrict__ ranges, uchar4* __restrict__ target,
                                                         float4* __restrict__ pixel_color,
                                                         uint32_t* __restrict__ pixel_last) {
-  __shared__ BlendStage st;
+  __shared__ WarpStage stages[8];
   const uint32_t tid = threadIdx.x;
+  WarpStage& st = stages[tid >> 5];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
   const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
   const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
   const uint32_t px = blockIdx.x * TILE + tile_pixel_x(tid), py = blockIdx.y * TILE + tile_pixel_y(tid);
   const bool inside = (float)px < vpx && (float)py < vpy;
   const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-  const float tile_x0 = (float)(blockIdx.x * TILE), tile_y0 = (float)(blockIdx.y * TILE);
-  const uint32_t warp_bit = 1u << (tid >> 5);
+  // The warp block's first pixel center.
+  const float x0 = (float)(blockIdx.x * TILE + tile_pixel_x(tid & ~31u)) + 0.5f;
+  const float y0 = (float)(blockIdx.y * TILE + tile_pixel_y(tid & ~31u)) + 0.5f;
   const uint2 run = ranges[tile];
   float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
   bool done = !inside;
   uint32_t last = 0;
-  for (uint32_t start = run.x; start < run.y; start += BLEND_BATCH) {
-    if (__syncthreads_count(done) == BLEND_BATCH) break;
-    const uint32_t staged = stage_window(st, splats, pair_splats, run.x, start, min(start + BLEND_BATCH, run.y),
-                                         tile_x0, tile_y0);
+  for (uint32_t start = run.x; start < run.y; start += 32) {
+    if (__all_sync(0xffffffffu, done)) break;
+    const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, start, run.y, x0, y0);
     for (uint32_t j = 0; j < staged && !done; j++) {
-      if (!(st.mask[j] & warp_bit)) continue;
       const float2 m = st.mean[j];
       const float4 q = st.quad[j];
       const float power = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
@@ -283,6 +281,7 @@ __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict
       T = remaining;
       last = st.pos[j] + 1;
     }
+    __syncwarp();
   }
   if (inside) {
     const float4 bg = raster_params[0];

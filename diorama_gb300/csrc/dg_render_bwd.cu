@@ -18,66 +18,86 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
   for (int k = threadIdx.x; k < 36; k += blockDim.x) d[k] = s[k];
 }
 
-// Sums 16 values over the warp. Afterwards lanes 2s and 2s+1 both hold the total
-// of value s: each halving step swaps half of the values with the partner lane,
-// so 8 + 4 + 2 + 1 + 1 shuffles move everything instead of 5 per value.
-__device__ __forceinline__ float warp_transpose_reduce16(float v[16], int lane) {
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    const bool upper = lane & 16;
-    const float send = upper ? v[k] : v[k + 8];
-    const float keep = upper ? v[k + 8] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-  }
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const bool upper = lane & 8;
-    const float send = upper ? v[k] : v[k + 4];
-    const float keep = upper ? v[k + 4] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-  }
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    const bool upper = lane & 4;
-    const float send = upper ? v[k] : v[k + 2];
-    const float keep = upper ? v[k + 2] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-  }
+// Sums 9 values over the warp with 12 shuffles instead of 45. Each halving step
+// swaps half of a lane's values with its partner's, so the set a lane holds
+// halves each time: values 0-4 / 5-8 at distance 16, then 3 / 2 of those at 8,
+// 2 / 1 at 4, 1 / 1 at 2, and a plain add at 1. Afterwards the lanes 2p and
+// 2p+1 of pair p hold the total of value reduce9_slot(2p), or padding when that is -1.
+__device__ __forceinline__ float warp_reduce9(const float v[9], int lane) {
+  float w[5];
   {
-    const bool upper = lane & 2;
-    const float send = upper ? v[0] : v[1];
-    const float keep = upper ? v[1] : v[0];
-    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    const bool upper = lane & 16;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const float lo = v[k], hi = k < 4 ? v[5 + k] : 0.0f;
+      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 16);
+      w[k] = (upper ? hi : lo) + got;
+    }
   }
-  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+  float x[3];
+  {
+    const bool upper = lane & 8;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float lo = w[k], hi = k < 2 ? w[3 + k] : 0.0f;
+      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 8);
+      x[k] = (upper ? hi : lo) + got;
+    }
+  }
+  float y[2];
+  {
+    const bool upper = lane & 4;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const float lo = x[k], hi = k < 1 ? x[2] : 0.0f;
+      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 4);
+      y[k] = (upper ? hi : lo) + got;
+    }
+  }
+  const bool upper = lane & 2;
+  const float z = (upper ? y[1] : y[0]) + __shfl_xor_sync(0xffffffffu, upper ? y[0] : y[1], 2);
+  return z + __shfl_xor_sync(0xffffffffu, z, 1);
 }
 
-// src/shaders/rasterizeBackward.wgsl:50-163. One CTA per 16x16 tile, each warp an
-// 8x4 pixel block. Each pixel walks its tile's list back to front from its last
-// blended splat, recovering the transmittance in front of each splat by dividing
-// the final one by (1 - alpha). The list is staged in windows of 256 entries
-// (front to back within a window, windows back to front) keeping only splats that
-// reach a warp block; splats past the tile's largest `last` are never staged. A
-// splat's 9 gradient shares are summed over the warp's 32 pixels with shuffles,
-// the 8 warps' sums meet in shared memory, and each window's per-splat totals go
-// to global memory with one atomic add per nonzero value.
+// Which value lane pair p = lane >> 1 ends up holding (bits of p: 16-, 8-, 4-, 2-lane
+// halves), packed 4 bits per pair with 15 meaning padding. Each lane extracts its
+// entry once; an indexed constant-memory table would serialize across the warp.
+__device__ __forceinline__ int reduce9_slot(int lane) {
+  const uint64_t table = 0xFFF8F765FF43F210ull;  // nibble p = slot of pair p (0xF: padding)
+  const int slot = (int)((table >> (4 * (lane >> 1))) & 0xFull);
+  return slot == 15 ? -1 : slot;
+}
+
+// src/shaders/rasterizeBackward.wgsl:50-163. One CTA per 16x16 tile; each warp
+// is an 8x4 pixel block and walks the tile's list on its own, back to front from
+// the largest `last` among its pixels, with no CTA barrier until the end: each
+// pixel recovers the transmittance in front of each splat by dividing the final
+// one by (1 - alpha). The list is staged 32 entries at a time into the warp's
+// slice of shared memory, keeping only splats that can reach the block. A splat's
+// 9 gradient shares are summed over the warp's 32 pixels with shuffles and added
+// into a per-tile accumulator indexed by list position (shared memory for the
+// first ACC_CAP positions, global memory past that); at the end the tile's totals
+// go to global memory with one atomic add per nonzero value.
+constexpr uint32_t ACC_CAP = 1536;
+
 __global__ void __launch_bounds__(256) rasterize_backward_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const float4* __restrict__ pixel_color,
     const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads) {
-  __shared__ BlendStage st;
-  __shared__ float s_acc[STAGE * SPLAT_GRADS];
+  __shared__ WarpStage stages[8];
+  __shared__ float s_acc[ACC_CAP * SPLAT_GRADS];
   __shared__ uint32_t s_max_last;
   const uint32_t tid = threadIdx.x;
   const int lane = tid & 31;
-  const uint32_t warp_bit = 1u << (tid >> 5);
+  WarpStage& st = stages[tid >> 5];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
   const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
   const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
   const uint32_t px = blockIdx.x * TILE + tile_pixel_x(tid), py = blockIdx.y * TILE + tile_pixel_y(tid);
   const bool inside = (float)px < vpx && (float)py < vpy;
   const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-  const float tile_x0 = (float)(blockIdx.x * TILE), tile_y0 = (float)(blockIdx.y * TILE);
+  const float x0 = (float)(blockIdx.x * TILE + tile_pixel_x(tid & ~31u)) + 0.5f;
+  const float y0 = (float)(blockIdx.y * TILE + tile_pixel_y(tid & ~31u)) + 0.5f;
   const uint2 run = ranges[tile];
   float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
   uint32_t last = 0;
@@ -91,27 +111,32 @@ __global__ void __launch_bounds__(256) rasterize_backward_kernel(
     pgz = pg.z;
   }
   if (tid == 0) s_max_last = 0;
-  for (uint32_t k = tid; k < STAGE * SPLAT_GRADS; k += 256) s_acc[k] = 0.0f;
   __syncthreads();
   if (last) atomicMax(&s_max_last, last);
+  // Splats at or past a warp's largest `last` contribute nothing to that warp.
+  const uint32_t warp_last = __reduce_max_sync(0xffffffffu, last);
   __syncthreads();
+  const uint32_t held = min(s_max_last, ACC_CAP);
+  for (uint32_t k = tid; k < held * SPLAT_GRADS; k += 256) s_acc[k] = 0.0f;
+  __syncthreads();
+  // The even lane of each pair adds the value its pair holds after the reduction.
+  const int my_slot = (lane & 1) ? -1 : reduce9_slot(lane);
   const float4 bg = raster_params[0];
   const float bg_grad = bg.x * pgx + bg.y * pgy + bg.z * pgz;
   float T = Tf;
   float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
   float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
-  const uint32_t end = run.x + s_max_last;
-  for (uint32_t window_end = end; window_end > run.x;) {
-    const uint32_t window_start = window_end - run.x > (uint32_t)STAGE ? window_end - STAGE : run.x;
-    const uint32_t staged = stage_window(st, splats, pair_splats, run.x, window_start, window_end, tile_x0, tile_y0);
+  for (uint32_t end = run.x + warp_last; end > run.x;) {
+    const uint32_t lo = end - run.x > 32u ? end - 32u : run.x;
+    const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, lo, end, x0, y0);
     for (uint32_t slot = staged; slot > 0; slot--) {
       const uint32_t j = slot - 1;
-      if (!(st.mask[j] & warp_bit)) continue;  // warp-uniform: the splat misses this block
-      float v[16];
+      const uint32_t pos = st.pos[j];
+      float v[9];
 #pragma unroll
-      for (int q = 0; q < 16; q++) v[q] = 0.0f;
+      for (int q = 0; q < 9; q++) v[q] = 0.0f;
       bool contributes = false;
-      if (inside && st.pos[j] < last) {
+      if (inside && pos < last) {
         const float2 m = st.mean[j];
         const float4 q = st.quad[j];
         const float dx = cx - m.x, dy = cy - m.y;
@@ -150,22 +175,23 @@ __global__ void __launch_bounds__(256) rasterize_backward_kernel(
         }
       }
       if (__any_sync(0xffffffffu, contributes)) {
-        const float total = warp_transpose_reduce16(v, lane);
-        const int which = lane >> 1;
-        if ((lane & 1) == 0 && which < (int)SPLAT_GRADS && total != 0.0f)
-          atomicAdd(&s_acc[j * SPLAT_GRADS + which], total);
+        const float total = warp_reduce9(v, lane);
+        if (my_slot >= 0 && total != 0.0f) {
+          if (pos < ACC_CAP)
+            atomicAdd(&s_acc[pos * SPLAT_GRADS + my_slot], total);
+          else
+            atomicAdd(&splat_grads[(size_t)st.index[j] * SPLAT_GRADS + my_slot], total);
+        }
       }
     }
-    __syncthreads();
-    for (uint32_t k = tid; k < staged * SPLAT_GRADS; k += 256) {
-      const float total = s_acc[k];
-      if (total != 0.0f) {
-        atomicAdd(&splat_grads[(size_t)st.index[k / SPLAT_GRADS] * SPLAT_GRADS + k % SPLAT_GRADS], total);
-        s_acc[k] = 0.0f;
-      }
-    }
-    __syncthreads();
-    window_end = window_start;
+    __syncwarp();
+    end = lo;
+  }
+  __syncthreads();
+  for (uint32_t k = tid; k < held * SPLAT_GRADS; k += 256) {
+    const float total = s_acc[k];
+    if (total != 0.0f)
+      atomicAdd(&splat_grads[(size_t)pair_splats[run.x + k / SPLAT_GRADS] * SPLAT_GRADS + k % SPLAT_GRADS], total);
   }
 }
 

@@ -244,78 +244,51 @@ __device__ __forceinline__ bool rect_reachable(float A, float b, float C, float 
 __device__ __forceinline__ uint32_t tile_pixel_x(uint32_t tid) { return ((tid >> 5) & 1u) * 8u + (tid & 7u); }
 __device__ __forceinline__ uint32_t tile_pixel_y(uint32_t tid) { return (tid >> 6) * 4u + ((tid >> 3) & 3u); }
 
-// For one splat and one tile, a bit per warp block the splat can reach. Also
-// returns the staged form of the splat's quadratic (A, b, C, cut).
-__device__ __forceinline__ uint32_t warp_reach_mask(float mx, float my, float a, float b, float c, float opacity,
-                                                    float tile_x0, float tile_y0, float4& quad) {
-  const float A = -0.5f * a, C = -0.5f * c;
-  const float cut = blend_cutoff(opacity);
-  quad = make_float4(A, b, C, cut);
-  if (!(cut < 0.0f)) return 0u;  // opacity below 1/255 (or not a number): it never blends
-  // argmax of q along dx for a fixed dy is kx dy (dq/ddx = 2A dx - b dy = 0), and along dy is ky dx.
-  const float kx = b / (2.0f * A), ky = b / (2.0f * C);
-  uint32_t mask = 0;
-#pragma unroll
-  for (int w = 0; w < 8; w++) {
-    const float x0 = tile_x0 + (float)((w & 1) * 8) + 0.5f, y0 = tile_y0 + (float)((w >> 1) * 4) + 0.5f;
-    if (rect_reachable(A, b, C, kx, ky, cut, x0 - mx, x0 + 7.0f - mx, y0 - my, y0 + 3.0f - my)) mask |= 1u << w;
-  }
-  return mask;
-}
-
-// A window of up to 256 entries of a tile's sorted list, staged in shared memory:
-// only the splats that reach at least one of the tile's warp blocks, in list
-// order, each with its position in the list (for pixel_last) and its warp mask.
-constexpr int STAGE = 256;
-struct BlendStage {
-  float2 mean[STAGE];
-  float4 quad[STAGE];   // A = -0.5 a, b, C = -0.5 c, cutoff
-  float4 color[STAGE];  // rgb, opacity
-  uint32_t pos[STAGE];  // position in the tile's list
-  uint32_t index[STAGE];
-  uint8_t mask[STAGE];
-  uint32_t warp_count[STAGE / 32];
+// A warp's own window of up to 32 list entries, staged in its slice of shared
+// memory: only the splats that can reach the warp's 8x4 pixel block, in list order.
+struct WarpStage {
+  float2 mean[32];
+  float4 quad[32];   // A = -0.5 a, b, C = -0.5 c, cutoff
+  float4 color[32];  // rgb, opacity
+  uint32_t pos[32];  // position in the tile's list
+  uint32_t index[32];
 };
 
-// Stages list entries [lo, hi) of the tile whose sorted run starts at run_x;
-// returns how many were kept. Every thread of the 256-thread CTA must call it.
-__device__ __forceinline__ uint32_t stage_window(BlendStage& st, const float* __restrict__ splats,
-                                                 const uint32_t* __restrict__ pair_splats, uint32_t run_x,
-                                                 uint32_t lo, uint32_t hi, float tile_x0, float tile_y0) {
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t k = lo + tid;
-  uint32_t mask = 0, index = 0;
+// Stages list entries [lo, min(lo + 32, hi)) for the calling warp, whose pixel
+// centers span [x0, x0 + 7] x [y0, y0 + 3]; returns how many were kept. All 32
+// lanes must call it.
+__device__ __forceinline__ uint32_t stage_warp_window(WarpStage& st, const float* __restrict__ splats,
+                                                      const uint32_t* __restrict__ pair_splats, uint32_t run_x,
+                                                      uint32_t lo, uint32_t hi, float x0, float y0) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t k = lo + lane;
+  bool keep = false;
   float2 mean = make_float2(0.f, 0.f);
   float4 quad = make_float4(0.f, 0.f, 0.f, 0.f), color = quad;
+  uint32_t index = 0;
   if (k < hi) {
     index = pair_splats[k];
     const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
     const float4 s0 = s[0], s1 = s[1];
     color = s[2];
     mean = make_float2(s0.x, s0.y);
-    mask = warp_reach_mask(s0.x, s0.y, s1.x, s1.y, s1.z, color.w, tile_x0, tile_y0, quad);
+    const float A = -0.5f * s1.x, b = s1.y, C = -0.5f * s1.z;
+    const float cut = blend_cutoff(color.w);
+    quad = make_float4(A, b, C, cut);
+    keep = cut < 0.0f && rect_reachable(A, b, C, b / (2.0f * A), b / (2.0f * C), cut, x0 - mean.x, x0 + 7.0f - mean.x,
+                                        y0 - mean.y, y0 + 3.0f - mean.y);
   }
-  const uint32_t kept = __ballot_sync(0xffffffffu, mask != 0u);
-  if (lane == 0) st.warp_count[warp] = __popc(kept);
-  __syncthreads();
-  uint32_t base = 0, total = 0;
-#pragma unroll
-  for (uint32_t w = 0; w < STAGE / 32; w++) {
-    const uint32_t c = st.warp_count[w];
-    base += w < warp ? c : 0u;
-    total += c;
-  }
-  if (mask) {
-    const uint32_t at = base + __popc(kept & ((1u << lane) - 1u));
+  const uint32_t kept = __ballot_sync(0xffffffffu, keep);
+  if (keep) {
+    const uint32_t at = __popc(kept & ((1u << lane) - 1u));
     st.mean[at] = mean;
     st.quad[at] = quad;
     st.color[at] = color;
     st.pos[at] = k - run_x;
     st.index[at] = index;
-    st.mask[at] = (uint8_t)mask;
   }
-  __syncthreads();
-  return total;
+  __syncwarp();
+  return __popc(kept);
 }
 
 // tile_count / tile_rect (src/shaders/common.wgsl:31-42).

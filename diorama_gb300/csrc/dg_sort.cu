@@ -101,7 +101,7 @@ __device__ __forceinline__ uint32_t block_exclusive_256(uint32_t v, uint32_t* s_
 }
 
 template <int KW>
-__global__ void __launch_bounds__(SORT_THREADS, 2)
+__global__ void __launch_bounds__(SORT_THREADS, 3)
     sort_pass_kernel(const typename KeyOf<KW>::type* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                      typename KeyOf<KW>::type* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                      uint32_t capacity, const uint32_t* __restrict__ count, uint32_t shift,

@@ -48,49 +48,73 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
   return raw;
 }
 
-// src/shaders/adam.wgsl:80-107, one thread per (Gaussian, moment slot): Adam's
-// slots are contiguous per Gaussian (16 raw parameters then 45 SH coefficients),
-// so consecutive threads read consecutive moments, parameters and gradients and
-// every access coalesces. Slots 7 and 15 (padding, which holds densification
+// src/shaders/adam.wgsl:80-107, one warp per Gaussian: lanes 0-31 take moment
+// slots 0-31 (the 16 raw parameters, then SH coefficients 0-15) and lanes 0-28
+// slots 32-60 (SH 16-44). A Gaussian's moments are 488 contiguous bytes and its
+// parameters, SH coefficients and gradients are contiguous runs too, so every
+// access coalesces, and the per-slot chain rule is written without branches so
+// the warp never splits. Slots 7 and 15 (padding, which holds densification
 // stamps) are left alone.
+struct AdamLanes {
+  float bc1, bc2, lr_param, sh_lr;
+  uint32_t kind;  // 0 position/rotation, 1 opacity, 2 scale, 3 colour, 4 padding
+};
+
+__device__ __forceinline__ void adam_param_slot(const AdamLanes& L, float* __restrict__ params,
+                                                float2* __restrict__ moments, const float* __restrict__ ggrad,
+                                                float* __restrict__ gaussians, size_t at, size_t slot) {
+  if (L.kind == 4) return;
+  float2 m = moments[slot];
+  const float value = params[at];
+  float grad = ggrad[at];
+  // One exp serves both chain rules: exp(value) for a scale, exp(-value) for the opacity's sigmoid.
+  const float e = expf(L.kind == 1 ? -value : value);
+  const float opacity = 1.0f / (1.0f + e);
+  grad = L.kind == 2 ? grad * e : L.kind == 1 ? grad * opacity * (1.0f - opacity) : L.kind == 3 ? grad * SH_C0 : grad;
+  const float next = adam_update(value, grad, m, L.lr_param, L.bc1, L.bc2);
+  params[at] = next;
+  moments[slot] = m;
+  const float e2 = expf(L.kind == 1 ? -next : next);
+  gaussians[at] = L.kind == 2 ? e2 : L.kind == 1 ? 1.0f / (1.0f + e2) : L.kind == 3 ? 0.5f + SH_C0 * next : next;
+}
+
+__device__ __forceinline__ void adam_sh_slot(const AdamLanes& L, float* __restrict__ sh, float2* __restrict__ moments,
+                                             const float* __restrict__ sgrad, size_t s, size_t slot) {
+  float2 m = moments[slot];
+  const float next = adam_update(sh[s], sgrad[s], m, L.sh_lr, L.bc1, L.bc2);
+  sh[s] = next;
+  moments[slot] = m;
+}
+
 __global__ void __launch_bounds__(256) adam_kernel(const AdamParams* __restrict__ ap, float* __restrict__ params,
                                                    float* __restrict__ sh, float2* __restrict__ moments,
                                                    const float* __restrict__ ggrad, const float* __restrict__ sgrad,
                                                    float* __restrict__ gaussians, uint32_t count) {
-  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
-  if (e >= count * MOMENT_SLOTS) return;
-  const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
-  if (k == 7 || k == 15) return;
-  const float bc1 = ap->bias_correction1, bc2 = ap->bias_correction2;
-  float2 m = moments[e];
-  if (k < FLOATS_PER_GAUSSIAN) {
-    const size_t at = (size_t)i * FLOATS_PER_GAUSSIAN + k;
-    const float value = params[at];
-    float grad = ggrad[at];
-    float lr;
-    if (k < 3) {
-      lr = ap->position_lr;
-    } else if (k == 3) {
-      const float opacity = sigmoidf_(value);
-      grad = grad * opacity * (1.0f - opacity);
-      lr = ap->opacity_lr;
-    } else if (k < 7) {
-      grad = grad * expf(value);
-      lr = ap->scale_lr;
-    } else if (k < 12) {
-      lr = ap->rotation_lr;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  AdamLanes L;
+  L.bc1 = ap->bias_correction1;
+  L.bc2 = ap->bias_correction2;
+  L.sh_lr = ap->sh_lr;
+  // Lane k < 16 holds raw parameter k: its group's learning rate and chain rule.
+  L.kind = lane < 3 ? 0u : lane == 3 ? 1u : lane < 7 ? 2u : lane == 7 ? 4u : lane < 12 ? 0u : lane < 15 ? 3u : 4u;
+  L.lr_param = lane < 3 ? ap->position_lr
+               : lane == 3 ? ap->opacity_lr
+               : lane < 7 ? ap->scale_lr
+               : lane < 12 ? ap->rotation_lr
+                           : ap->color_lr;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
+    const size_t slot0 = (size_t)i * MOMENT_SLOTS;
+    if (lane < FLOATS_PER_GAUSSIAN) {
+      adam_param_slot(L, params, moments, ggrad, gaussians, (size_t)i * FLOATS_PER_GAUSSIAN + lane, slot0 + lane);
     } else {
-      grad = grad * SH_C0;
-      lr = ap->color_lr;
+      adam_sh_slot(L, sh, moments, sgrad, (size_t)i * SH_REST_FLOATS + (lane - FLOATS_PER_GAUSSIAN), slot0 + lane);
     }
-    const float next = adam_update(value, grad, m, lr, bc1, bc2);
-    params[at] = next;
-    gaussians[at] = activated(k, next);
-  } else {
-    const size_t s = (size_t)i * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN);
-    sh[s] = adam_update(sh[s], sgrad[s], m, ap->sh_lr, bc1, bc2);
+    if (lane < MOMENT_SLOTS - 32) {
+      adam_sh_slot(L, sh, moments, sgrad, (size_t)i * SH_REST_FLOATS + (lane + 32 - FLOATS_PER_GAUSSIAN),
+                   slot0 + 32 + lane);
+    }
   }
-  moments[e] = m;
 }
 
 // src/shaders/adam.wgsl:74-77, one thread per raw float.
@@ -338,9 +362,8 @@ static dg_status launch_stats(dg_trainer* t) {
 
 static dg_status launch_adam(dg_trainer* t) {
   dg_renderer* r = t->renderer;
-  const uint64_t elements = (uint64_t)t->count * MOMENT_SLOTS;
   DG_LAUNCH(t->ctx, "adam",
-            adam_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, t->ctx->stream>>>(
+            adam_kernel<<<ceil_div(t->count, 8), 256, 0, t->ctx->stream>>>(
                 typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<float>(r->grad_gaussians), typed<float>(r->grad_sh),
                 typed<float>(r->gaussians), t->count));
