@@ -28,13 +28,16 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
 // coefficients are staged through shared memory with coalesced loads (45 floats
 // per Gaussian; the odd stride makes the per-thread reads conflict-free). When
 // tile_counts is given, the tiles each splat touches are written too
-// (src/shaders/tiles.wgsl:24-35, fused).
+// (src/shaders/tiles.wgsl:24-35, fused); when depth_keys is given, the depth's
+// bits (0 when culled) and the splat's index, the input of the depth sort.
 __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* __restrict__ camera,
                                                                  const float* __restrict__ gaussians,
                                                                  const float* __restrict__ sh, uint32_t count,
                                                                  const uint32_t* __restrict__ scene_params,
                                                                  float* __restrict__ splats,
-                                                                 uint32_t* __restrict__ tile_counts) {
+                                                                 uint32_t* __restrict__ tile_counts,
+                                                                 uint32_t* __restrict__ depth_keys,
+                                                                 uint32_t* __restrict__ depth_order) {
   __shared__ Camera s_cam;
   __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
   load_camera(s_cam, camera);
@@ -69,11 +72,13 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
   }
   float4* out = reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT);
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (depth_order) depth_order[i] = i;
   auto culled = [&]() {
     out[0] = zero;
     out[1] = zero;
     out[2] = zero;
     if (tile_counts) tile_counts[i] = 0;
+    if (depth_keys) depth_keys[i] = 0;
   };
   if (-view_z(cam, g) <= 0.2f) return culled();
   Projection p;
@@ -118,6 +123,98 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
     uint4 rect = tile_rect(mx, my, radius, tile_grid(cam));
     tile_counts[i] = (rect.z - rect.x) * (rect.w - rect.y);
   }
+  if (depth_keys) depth_keys[i] = __float_as_uint(p.depth);
+}
+
+// The depth-first tile sort (the renderer's path). The reference sorts 64-bit
+// (tile, depth) keys (src/shaders/tiles.wgsl:37-60, src/radixSort.ts:101-104).
+// Here the splats are first sorted by depth alone (stable, so equal depths keep
+// index order), their pairs are then emitted in that order, and a stable sort on
+// the 16-bit tile index finishes the job. Within a tile the pairs end up by depth
+// with ties by splat index: exactly the reference's order, from sorting N 32-bit
+// keys plus K 16-bit ones instead of K 48-bit ones.
+
+// Tiles touched by the j-th splat in depth order, for the scan.
+__global__ void gather_counts_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
+                                     uint32_t n, uint32_t* __restrict__ out) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) out[j] = counts[order[j]];
+}
+
+// duplicate_kernel's warp-cooperative emission over splats in depth order: the
+// pairs of 32 consecutive sorted splats are one contiguous run of slots. Keys are
+// the tile index alone (u32), values the splat index.
+__global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Camera* __restrict__ camera,
+                                                                       const float* __restrict__ splats,
+                                                                       const uint32_t* __restrict__ order,
+                                                                       const uint32_t* __restrict__ offsets,
+                                                                       uint32_t count, uint32_t capacity,
+                                                                       uint32_t* __restrict__ keys,
+                                                                       uint32_t* __restrict__ values) {
+  __shared__ uint32_t s_excl[DUP_THREADS];
+  __shared__ uint32_t s_x0[DUP_THREADS];
+  __shared__ uint32_t s_y0[DUP_THREADS];
+  __shared__ uint32_t s_w[DUP_THREADS];
+  __shared__ uint32_t s_index[DUP_THREADS];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t j = blockIdx.x * DUP_THREADS + threadIdx.x;
+  const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
+  if (first >= count) return;  // warp-uniform
+  const Camera& cam = *camera;
+  const uint2 tiles = tile_grid(cam);
+  uint32_t n = 0, index = 0;
+  uint4 rect = make_uint4(0, 0, 0, 0);
+  if (j < count) {
+    index = order[j];
+    const float4 s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT)[0];
+    if (s.w != 0.0f) {
+      rect = tile_rect(s.x, s.y, s.w, tiles);
+      n = (rect.z - rect.x) * (rect.w - rect.y);
+    }
+  }
+  uint32_t incl = n;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  const uint32_t slot0 = offsets[first];
+  uint32_t* excl = s_excl + warp * 32;
+  excl[lane] = incl - n;
+  s_x0[threadIdx.x] = rect.x;
+  s_y0[threadIdx.x] = rect.y;
+  s_w[threadIdx.x] = rect.z - rect.x;
+  s_index[threadIdx.x] = index;
+  __syncwarp();
+  for (uint32_t k = lane; k < total; k += 32) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1)
+      if (excl[lo + step] <= k) lo += step;
+    const int src = warp * 32 + lo;
+    const uint32_t local = k - excl[lo];
+    const uint32_t w = s_w[src];
+    const uint32_t y = s_y0[src] + local / w;
+    const uint32_t x = s_x0[src] + local % w;
+    const uint32_t slot = slot0 + k;
+    if (slot < capacity) {
+      keys[slot] = y * tiles.x + x;
+      values[slot] = s_index[src];
+    }
+  }
+}
+
+// The reference's sorted 64-bit keys (tile << 32 | depth bits), rebuilt from the
+// depth-first path's tile keys and splats, for inspection.
+__global__ void materialize_keys_kernel(const uint32_t* __restrict__ tile_keys, const uint32_t* __restrict__ values,
+                                        const float* __restrict__ splats, const uint32_t* __restrict__ pair_total,
+                                        uint32_t capacity, uint64_t* __restrict__ out) {
+  const uint32_t n = min(pair_total[0], capacity);
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t depth_bits = __float_as_uint(splats[(size_t)values[k] * FLOATS_PER_SPLAT + 2]);
+  out[k] = ((uint64_t)tile_keys[k] << 32) | depth_bits;
 }
 
 // src/shaders/tiles.wgsl:24-35 (for splats the renderer did not preprocess).
@@ -200,7 +297,10 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_kernel(const Camera* __
   }
 }
 
-// src/shaders/tiles.wgsl:65-84
+// src/shaders/tiles.wgsl:65-84. The tile index is word STRIDE - 1 of each key:
+// the high word of the reference's 64-bit keys, or the whole u32 key of the
+// depth-first path.
+template <int STRIDE>
 __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32_t* __restrict__ key_words,
                                                                     const uint32_t* __restrict__ pair_total,
                                                                     uint32_t capacity, uint32_t tiles,
@@ -208,12 +308,12 @@ __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32
   const uint32_t n = min(pair_total[0], capacity);
   const uint32_t i = blockIdx.x * RANGE_THREADS + threadIdx.x;
   if (i >= n) return;
-  const uint32_t tile = key_words[2 * (size_t)i + 1];
+  const uint32_t tile = key_words[STRIDE * (size_t)i + (STRIDE - 1)];
   if (tile >= tiles) return;  // only possible after a sort whose bounded wait gave up
   if (i == 0) {
     ranges[tile].x = 0;
   } else {
-    const uint32_t prev = key_words[2 * (size_t)i - 1];
+    const uint32_t prev = key_words[STRIDE * (size_t)(i - 1) + (STRIDE - 1)];
     if (tile != prev) {
       if (prev < tiles) ranges[prev].y = i;
       ranges[tile].x = i;
@@ -312,19 +412,21 @@ static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
   free_buffer(tr->sort_scratch);
   tr->keys = tr->values = tr->keys_alt = tr->values_alt = tr->sort_scratch = nullptr;
   tr->plan = sort_plan(capacity, TILE_INDEX_BITS);
+  tr->tile_plan = sort_plan_low_bits(capacity, TILE_INDEX_BITS);
   tr->pair_capacity = capacity;
   DG_TRY(alloc_buffer(ctx, (size_t)capacity * 8, &tr->keys));
   DG_TRY(alloc_buffer(ctx, (size_t)capacity * 4, &tr->values));
   DG_TRY(alloc_buffer(ctx, (size_t)capacity * 8, &tr->keys_alt));
   DG_TRY(alloc_buffer(ctx, (size_t)capacity * 4, &tr->values_alt));
-  DG_TRY(alloc_buffer(ctx, sort_scratch_bytes(tr->plan), &tr->sort_scratch));
+  DG_TRY(alloc_buffer(ctx, std::max(sort_scratch_bytes(tr->plan), sort_scratch_bytes(tr->tile_plan)),
+                      &tr->sort_scratch));
   return DG_OK;
 }
 
 dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity) { return make_pairs(tr, capacity); }
 
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
-                            uint32_t initial_pair_capacity, dg_tile_rasterizer** out) {
+                            uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out) {
   auto* tr = new dg_tile_rasterizer();
   tr->ctx = ctx;
   tr->camera = camera;
@@ -339,6 +441,17 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
     st = fail(DG_ERROR_CUDA, "event");
   uint32_t capacity = initial_pair_capacity ? initial_pair_capacity : std::max(1u << 16, count * 8u);
   if (st == DG_OK) st = make_pairs(tr, capacity);
+  tr->depth_first = depth_first;
+  if (st == DG_OK && depth_first) {
+    const size_t n = std::max(count, 1u);
+    tr->depth_plan = sort_plan_low_bits(std::max(count, 1u), 32);
+    st = alloc_buffer(ctx, n * 4, &tr->depth_keys);
+    if (st == DG_OK) st = alloc_buffer(ctx, n * 4, &tr->depth_values);
+    if (st == DG_OK) st = alloc_buffer(ctx, n * 4, &tr->depth_keys_alt);
+    if (st == DG_OK) st = alloc_buffer(ctx, n * 4, &tr->depth_values_alt);
+    if (st == DG_OK) st = alloc_buffer(ctx, sort_scratch_bytes(tr->depth_plan), &tr->depth_scratch);
+    if (st == DG_OK) st = alloc_buffer(ctx, n * 4, &tr->counts_sorted);
+  }
   if (st != DG_OK) {
     dg_tile_rasterizer_destroy(tr);
     return st;
@@ -383,6 +496,35 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
   const uint32_t count = tr->count;
   const auto* cam = typed<const Camera>(tr->camera);
   DG_CUDA(cudaMemsetAsync(tr->ranges->ptr, 0, (size_t)tr->tiles_x * tr->tiles_y * 8, st));
+  if (tr->depth_first && counts_ready) {
+    // tile_offsets holds each splat's tile count; depth_keys/depth_values its depth
+    // bits and index (both written by the renderer's preprocess).
+    uint32_t* order = typed<uint32_t>(tr->depth_values);
+    if (count > 0) {
+      DG_TRY(sort_launch(ctx, tr->depth_plan, tr->depth_keys->ptr, order, tr->depth_keys_alt->ptr,
+                         typed<uint32_t>(tr->depth_values_alt), nullptr, tr->depth_scratch->ptr));
+      DG_LAUNCH(ctx, "gather_counts",
+                gather_counts_kernel<<<ceil_div(count, 256), 256, 0, st>>>(
+                    order, typed<uint32_t>(tr->tile_offsets), count, typed<uint32_t>(tr->counts_sorted)));
+    }
+    DG_TRY(scan_launch(ctx, typed<uint32_t>(tr->counts_sorted), count, nullptr, typed<uint32_t>(tr->scan_total),
+                       tr->scan_scratch->ptr));
+    if (count > 0) {
+      DG_LAUNCH(ctx, "duplicate",
+                duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
+                    cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count,
+                    tr->pair_capacity, typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values)));
+    }
+    DG_TRY(sort_launch(ctx, tr->tile_plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
+                       typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
+    DG_LAUNCH(ctx, "find_ranges",
+              find_ranges_kernel<1><<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0,
+                                      st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
+                                            tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+    tr->keys_are_tiles = true;
+    return launch_rasterize(tr, target);
+  }
+  tr->keys_are_tiles = false;
   if (count > 0) {
     if (!counts_ready) {
       DG_LAUNCH(ctx, "count_tiles",
@@ -401,15 +543,36 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
   DG_TRY(sort_launch(ctx, tr->plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
                      typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
   DG_LAUNCH(ctx, "find_ranges",
-            find_ranges_kernel<<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0, st>>>(
-                typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total), tr->pair_capacity,
-                tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+            find_ranges_kernel<2><<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0,
+                                    st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
+                                          tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+  return launch_rasterize(tr, target);
+}
+
+dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
+  dg_context* ctx = tr->ctx;
   DG_LAUNCH(ctx, "rasterize",
-            rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, st>>>(
-                cam, typed<float4>(tr->raster_params), typed<float>(tr->splats), typed<uint32_t>(tr->values),
-                typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last)));
+            rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
+                typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
+                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr,
+                typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last)));
   return DG_OK;
+}
+
+// The sorted keys in the reference's 64-bit form, rebuilt if the last frame took
+// the depth-first path.
+dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr) {
+  if (!tr->keys_are_tiles) return tr->keys;
+  if (!tr->keys64 || tr->keys64->bytes < (uint64_t)tr->pair_capacity * 8) {
+    free_buffer(tr->keys64);
+    tr->keys64 = nullptr;
+    if (alloc_buffer(tr->ctx, (size_t)tr->pair_capacity * 8, &tr->keys64) != DG_OK) return nullptr;
+  }
+  materialize_keys_kernel<<<std::max(1u, ceil_div(tr->pair_capacity, 256)), 256, 0, tr->ctx->stream>>>(
+      typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values), typed<float>(tr->splats), typed<uint32_t>(tr->scan_total),
+      tr->pair_capacity, typed<uint64_t>(tr->keys64));
+  tr->ctx->launches++;
+  return tr->keys64;
 }
 
 dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr) {
@@ -454,7 +617,7 @@ static dg_status create_scene(dg_renderer* r, uint32_t count, dg_buffer* gaussia
   const uint32_t params[4] = {degree, 0, 0, 0};
   DG_TRY(write_async(r->ctx, r->scene_params->ptr, params, sizeof(params)));
   DG_TRY(alloc_buffer(r->ctx, (size_t)count * FLOATS_PER_SPLAT * 4, &r->splats));
-  DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, &r->rasterizer));
+  DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, true, &r->rasterizer));
   return DG_OK;
 }
 
@@ -482,7 +645,8 @@ dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target) {
               preprocess_kernel<<<ceil_div(r->count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
                   typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                   typed<uint32_t>(r->scene_params), typed<float>(r->splats),
-                  typed<uint32_t>(r->rasterizer->tile_offsets)));
+                  typed<uint32_t>(r->rasterizer->tile_offsets), typed<uint32_t>(r->rasterizer->depth_keys),
+                  typed<uint32_t>(r->rasterizer->depth_values)));
   }
   return rasterizer_launch(r->rasterizer, target, true);
 }
@@ -514,7 +678,7 @@ dg_status dg_tile_rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffe
   DG_REQUIRE(ctx && camera && splats && out, "NULL argument");
   DG_REQUIRE(camera->bytes >= sizeof(Camera), "camera buffer is smaller than the 144-byte Camera uniform");
   DG_REQUIRE(splats->bytes >= (uint64_t)count * FLOATS_PER_SPLAT * 4, "splat buffer too small for count");
-  return rasterizer_create(ctx, camera, splats, count, initial_pair_capacity, out);
+  return rasterizer_create(ctx, camera, splats, count, initial_pair_capacity, false, out);
 }
 
 dg_status dg_tile_rasterizer_encode(dg_tile_rasterizer* tr, dg_buffer* target, const float viewport[2],
@@ -556,7 +720,7 @@ uint32_t dg_tile_rasterizer_last_pair_count(const dg_tile_rasterizer* tr) { retu
 uint32_t dg_tile_rasterizer_pair_capacity(const dg_tile_rasterizer* tr) { return tr ? tr->pair_capacity : 0; }
 dg_buffer* dg_tile_rasterizer_pair_splats(dg_tile_rasterizer* tr) { return tr ? tr->values : nullptr; }
 dg_buffer* dg_tile_rasterizer_ranges(dg_tile_rasterizer* tr) { return tr ? tr->ranges : nullptr; }
-dg_buffer* dg_tile_rasterizer_pair_keys(dg_tile_rasterizer* tr) { return tr ? tr->keys : nullptr; }
+dg_buffer* dg_tile_rasterizer_pair_keys(dg_tile_rasterizer* tr) { return tr ? rasterizer_sorted_keys(tr) : nullptr; }
 dg_buffer* dg_tile_rasterizer_pixel_color(dg_tile_rasterizer* tr) { return tr ? tr->pixel_color : nullptr; }
 dg_buffer* dg_tile_rasterizer_pixel_last(dg_tile_rasterizer* tr) { return tr ? tr->pixel_last : nullptr; }
 dg_buffer* dg_tile_rasterizer_tile_offsets(dg_tile_rasterizer* tr) { return tr ? tr->tile_offsets : nullptr; }
@@ -565,7 +729,9 @@ dg_buffer* dg_tile_rasterizer_pair_total(dg_tile_rasterizer* tr) { return tr ? t
 dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
   if (!tr) return DG_OK;
   for (dg_buffer* b : {tr->tile_offsets, tr->scan_total, tr->scan_scratch, tr->raster_params, tr->keys, tr->values,
-                       tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last})
+                       tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last,
+                       tr->depth_keys, tr->depth_values, tr->depth_keys_alt, tr->depth_values_alt, tr->depth_scratch,
+                       tr->counts_sorted, tr->keys64})
     free_buffer(b);
   if (tr->readback_event) {
     cudaEventSynchronize(tr->readback_event);

@@ -33,6 +33,18 @@ struct dg_tile_rasterizer {
   uint32_t last_pair_count;
   uint32_t tiles_x, tiles_y;
   float viewport[2];
+  // The depth-first tile sort (the renderer's path, dg_render.cu): splats sorted
+  // by depth, their pairs emitted in that order and sorted by tile index alone.
+  bool depth_first;
+  bool keys_are_tiles;  // the last frame left u32 tile indices in `keys`
+  dg::SortPlan depth_plan, tile_plan;
+  dg_buffer* depth_keys;
+  dg_buffer* depth_values;  // splat indices, sorted by depth
+  dg_buffer* depth_keys_alt;
+  dg_buffer* depth_values_alt;
+  dg_buffer* depth_scratch;
+  dg_buffer* counts_sorted;  // tile counts in depth order, then their scan
+  dg_buffer* keys64;         // the reference's 64-bit sorted keys, rebuilt on request
 };
 
 namespace dg {
@@ -44,8 +56,10 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
 dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr);
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
-                            uint32_t initial_pair_capacity, dg_tile_rasterizer** out);
+                            uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);
 dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity);
+dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
+dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr);
 }  // namespace dg
 
 // GaussianRenderer (src/gaussianRenderer.ts:55-311).

@@ -258,7 +258,7 @@ dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32
   auto* status = reinterpret_cast<uint32_t*>(s + l.status);
   DG_CUDA(cudaMemsetAsync(scratch, 0, l.total, ctx->stream));
   PassShifts shifts{};
-  for (uint32_t p = 0; p < plan.passes; p++) shifts.shift[p] = p < 4 ? p * 8 : 32 + (p - 4) * 8;
+  for (uint32_t p = 0; p < plan.passes; p++) shifts.shift[p] = plan.shift[p];
   uint32_t hist_blocks = std::min<uint32_t>(ceil_div(plan.capacity, HIST_THREADS * 16), (uint32_t)ctx->sm_count * 4);
   hist_blocks = std::max(1u, hist_blocks);
   DG_LAUNCH(ctx, "sort_histogram",
@@ -292,11 +292,22 @@ dg_status sort_init() {
 }
 
 SortPlan sort_plan(uint32_t capacity, uint32_t high_bits) {
-  SortPlan p;
+  SortPlan p{};
   p.capacity = capacity;
   p.key_words = high_bits > 0 ? 2 : 1;
   p.high_bits = high_bits;
   p.passes = 4 + 2 * ((high_bits + 15) / 16);
+  for (uint32_t k = 0; k < p.passes; k++) p.shift[k] = k < 4 ? k * 8 : 32 + (k - 4) * 8;
+  return p;
+}
+
+SortPlan sort_plan_low_bits(uint32_t capacity, uint32_t bits) {
+  SortPlan p{};
+  p.capacity = capacity;
+  p.key_words = 1;
+  p.high_bits = 0;
+  p.passes = 2 * ((bits + 15) / 16);
+  for (uint32_t k = 0; k < p.passes; k++) p.shift[k] = k * 8;
   return p;
 }
 

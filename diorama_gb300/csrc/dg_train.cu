@@ -34,12 +34,6 @@ struct DensifyParams {
 
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.0f / (1.0f + expf(-x)); }
 
-__device__ __forceinline__ float adam_update(float value, float grad, float2& m, float lr, float bc1, float bc2) {
-  m.x = 0.9f * m.x + 0.1f * grad;
-  m.y = 0.999f * m.y + 0.001f * grad * grad;
-  return value - lr * (m.x / bc1) / (sqrtf(m.y / bc2) + 1e-15f);
-}
-
 // The activated value of raw slot k (src/shaders/adam.wgsl:60-71); slots 7 and 15 are not written.
 __device__ __forceinline__ float activated(uint32_t k, float raw) {
   if (k >= 4 && k <= 6) return expf(raw);
@@ -55,35 +49,13 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
 // access coalesces, and the per-slot chain rule is written without branches so
 // the warp never splits. Slots 7 and 15 (padding, which holds densification
 // stamps) are left alone.
-struct AdamLanes {
-  float bc1, bc2, lr_param, sh_lr;
-  uint32_t kind;  // 0 position/rotation, 1 opacity, 2 scale, 3 colour, 4 padding
-};
-
-__device__ __forceinline__ void adam_param_slot(const AdamLanes& L, float* __restrict__ params,
-                                                float2* __restrict__ moments, const float* __restrict__ ggrad,
-                                                float* __restrict__ gaussians, size_t at, size_t slot) {
-  if (L.kind == 4) return;
-  float2 m = moments[slot];
-  const float value = params[at];
-  float grad = ggrad[at];
-  // One exp serves both chain rules: exp(value) for a scale, exp(-value) for the opacity's sigmoid.
-  const float e = expf(L.kind == 1 ? -value : value);
-  const float opacity = 1.0f / (1.0f + e);
-  grad = L.kind == 2 ? grad * e : L.kind == 1 ? grad * opacity * (1.0f - opacity) : L.kind == 3 ? grad * SH_C0 : grad;
-  const float next = adam_update(value, grad, m, L.lr_param, L.bc1, L.bc2);
-  params[at] = next;
-  moments[slot] = m;
-  const float e2 = expf(L.kind == 1 ? -next : next);
-  gaussians[at] = L.kind == 2 ? e2 : L.kind == 1 ? 1.0f / (1.0f + e2) : L.kind == 3 ? 0.5f + SH_C0 * next : next;
-}
-
-__device__ __forceinline__ void adam_sh_slot(const AdamLanes& L, float* __restrict__ sh, float2* __restrict__ moments,
-                                             const float* __restrict__ sgrad, size_t s, size_t slot) {
-  float2 m = moments[slot];
-  const float next = adam_update(sh[s], sgrad[s], m, L.sh_lr, L.bc1, L.bc2);
-  sh[s] = next;
-  moments[slot] = m;
+// Adam's update with the bias corrections applied as reciprocals computed once:
+// within two ulps of value - lr (m/bc1) / (sqrt(v/bc2) + eps).
+__device__ __forceinline__ float adam_step_fast(float value, float grad, float2& m, float lr, float inv_bc1,
+                                                float inv_bc2) {
+  m.x = 0.9f * m.x + 0.1f * grad;
+  m.y = 0.999f * m.y + 0.001f * grad * grad;
+  return value - lr * (m.x * inv_bc1) * __frcp_rn(sqrtf(m.y * inv_bc2) + 1e-15f);
 }
 
 __global__ void __launch_bounds__(256) adam_kernel(const AdamParams* __restrict__ ap, float* __restrict__ params,
@@ -91,29 +63,70 @@ __global__ void __launch_bounds__(256) adam_kernel(const AdamParams* __restrict_
                                                    const float* __restrict__ ggrad, const float* __restrict__ sgrad,
                                                    float* __restrict__ gaussians, uint32_t count) {
   const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  AdamLanes L;
-  L.bc1 = ap->bias_correction1;
-  L.bc2 = ap->bias_correction2;
-  L.sh_lr = ap->sh_lr;
-  // Lane k < 16 holds raw parameter k: its group's learning rate and chain rule.
-  L.kind = lane < 3 ? 0u : lane == 3 ? 1u : lane < 7 ? 2u : lane == 7 ? 4u : lane < 12 ? 0u : lane < 15 ? 3u : 4u;
-  L.lr_param = lane < 3 ? ap->position_lr
-               : lane == 3 ? ap->opacity_lr
-               : lane < 7 ? ap->scale_lr
-               : lane < 12 ? ap->rotation_lr
-                           : ap->color_lr;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += warps) {
-    const size_t slot0 = (size_t)i * MOMENT_SLOTS;
-    if (lane < FLOATS_PER_GAUSSIAN) {
-      adam_param_slot(L, params, moments, ggrad, gaussians, (size_t)i * FLOATS_PER_GAUSSIAN + lane, slot0 + lane);
-    } else {
-      adam_sh_slot(L, sh, moments, sgrad, (size_t)i * SH_REST_FLOATS + (lane - FLOATS_PER_GAUSSIAN), slot0 + lane);
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= count) return;
+  const float inv_bc1 = 1.0f / ap->bias_correction1, inv_bc2 = 1.0f / ap->bias_correction2;
+  // Round 1: lane k < 16 holds raw parameter k (its group's learning rate and chain
+  // rule), lanes 16-31 SH coefficients 0-15. Round 2: lanes 0-28 SH 16-44.
+  // kind: 0 position/rotation, 1 opacity, 2 scale, 3 colour, 4 padding, 5 SH.
+  const uint32_t kind = lane >= 16  ? 5u
+                        : lane < 3  ? 0u
+                        : lane == 3 ? 1u
+                        : lane < 7  ? 2u
+                        : lane == 7 ? 4u
+                        : lane < 12 ? 0u
+                        : lane < 15 ? 3u
+                                    : 4u;
+  const float lr1 = kind == 5   ? ap->sh_lr
+                    : lane < 3  ? ap->position_lr
+                    : lane == 3 ? ap->opacity_lr
+                    : lane < 7  ? ap->scale_lr
+                    : lane < 12 ? ap->rotation_lr
+                                : ap->color_lr;
+  const float sh_lr = ap->sh_lr;
+  const size_t slot0 = (size_t)i * MOMENT_SLOTS;
+  const bool param = lane < FLOATS_PER_GAUSSIAN;
+  const bool second = lane < MOMENT_SLOTS - 32;
+  float* p1 = param ? params + (size_t)i * FLOATS_PER_GAUSSIAN + lane : sh + (size_t)i * SH_REST_FLOATS + (lane - 16);
+  const float* g1 = param ? ggrad + (size_t)i * FLOATS_PER_GAUSSIAN + lane : sgrad + (size_t)i * SH_REST_FLOATS + (lane - 16);
+  const size_t s2 = (size_t)i * SH_REST_FLOATS + 16 + lane;
+  // Every load of both rounds is in flight before any arithmetic.
+  float2 m1 = moments[slot0 + lane];
+  const float x1 = *p1, d1 = *g1;
+  float2 m2 = make_float2(0.f, 0.f);
+  float x2 = 0.f, d2 = 0.f;
+  if (second) {
+    m2 = moments[slot0 + 32 + lane];
+    x2 = sh[s2];
+    d2 = sgrad[s2];
+  }
+  if (kind != 4) {
+    // One exp serves both chain rules: exp(value) for a scale, exp(-value) for the opacity's sigmoid.
+    float grad = d1;
+    if (kind == 1 || kind == 2) {
+      const float e = expf(kind == 1 ? -x1 : x1);
+      const float opacity = 1.0f / (1.0f + e);
+      grad = kind == 2 ? grad * e : grad * opacity * (1.0f - opacity);
+    } else if (kind == 3) {
+      grad = grad * SH_C0;
     }
-    if (lane < MOMENT_SLOTS - 32) {
-      adam_sh_slot(L, sh, moments, sgrad, (size_t)i * SH_REST_FLOATS + (lane + 32 - FLOATS_PER_GAUSSIAN),
-                   slot0 + 32 + lane);
+    const float n1 = adam_step_fast(x1, grad, m1, lr1, inv_bc1, inv_bc2);
+    *p1 = n1;
+    moments[slot0 + lane] = m1;
+    if (param) {
+      float act = n1;
+      if (kind == 1 || kind == 2) {
+        const float e = expf(kind == 1 ? -n1 : n1);
+        act = kind == 2 ? e : 1.0f / (1.0f + e);
+      } else if (kind == 3) {
+        act = 0.5f + SH_C0 * n1;
+      }
+      gaussians[(size_t)i * FLOATS_PER_GAUSSIAN + lane] = act;
     }
+  }
+  if (second) {
+    sh[s2] = adam_step_fast(x2, d2, m2, sh_lr, inv_bc1, inv_bc2);
+    moments[slot0 + 32 + lane] = m2;
   }
 }
 

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import oracle
-from diorama_gb300 import GaussianRenderer, TrainingLoss, scenes
+from diorama_gb300 import GaussianRenderer, TileRasterizer, TrainingLoss, scenes
 from helpers import GOLDEN, cam_array, group_errors
 
 pytestmark = pytest.mark.gpu
@@ -72,10 +72,27 @@ def test_config2_sort_scan_ranges_bit_exact(device):
     assert np.array_equal(splats.view(np.uint32), oracle.preprocess(cam, act, sh, 3).view(np.uint32))
     offsets, total, keys, values, ranges = oracle.tile_stage(cam, splats)
     assert total > 5_000_000
+    # The renderer's depth-first tile sort: same pairs, order and ranges.
     assert int(debug["pairTotal"].read(np.uint32)[0]) == total == tiles.lastPairCount
-    assert np.array_equal(debug["tileOffsets"].read(np.uint32)[: offsets.size], offsets)
     assert np.array_equal(debug["pairKeys"].read(np.uint64)[:total], keys)
     assert np.array_equal(debug["pairSplats"].read(np.uint32)[:total], values)
     assert np.array_equal(debug["ranges"].read(np.uint32)[: ranges.size], ranges)
+
+    # The reference-structured TileRasterizer on the same splats: the scan of tile
+    # counts, the 64-bit (tile, depth) keys sorted in 6 passes, the permutation and
+    # the ranges.
+    camera_buf = device.upload(cam)  # the 144-byte Camera uniform
+    tr = TileRasterizer(device, camera_buf, r.splatBuffer, splats.size // 12, tiles.pairCapacity)
+    tr.encode(None, None, camera.viewport, (0, 0, 0))
+    tr.afterSubmit()
+    d2 = tr.debugBuffers
+    assert int(d2["pairTotal"].read(np.uint32)[0]) == total == tr.lastPairCount
+    assert np.array_equal(d2["tileOffsets"].read(np.uint32)[: offsets.size], offsets)
+    assert np.array_equal(d2["pairKeys"].read(np.uint64)[:total], keys)
+    assert np.array_equal(d2["pairSplats"].read(np.uint32)[:total], values)
+    assert np.array_equal(d2["ranges"].read(np.uint32)[: ranges.size], ranges)
+    assert np.array_equal(tr.pixelColor.read(np.float32), r.pixelBuffer.read(np.float32))
     assert device.check() == 0
+    tr.destroy()
+    camera_buf.destroy()
     r.destroy()
