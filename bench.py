@@ -169,7 +169,10 @@ def build_scene(args):
 # Algorithmic bytes per unit: what each kernel must move at minimum.
 def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6) -> float | None:
     return {
-        "adam": 1708.0 * n,  # 59 trainable slots x (read p, g, m, v: 16 B; write p, m, v: 12 B) + 56 B activated
+        # Trainable slots x (read p, g, m, v: 16 B; write p, m, v: 12 B): 45 SH slots, then
+        # 14 Gaussian slots plus the 56 B of activated parameters.
+        "adam_sh": 1260.0 * n,
+        "adam_param": 448.0 * n,
         "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
         "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
         "sort_pass": 24.0 * pairs,  # per pass: read and write 8 B key + 4 B value

@@ -326,70 +326,79 @@ __device__ __forceinline__ unsigned char to_unorm8(float v) {
   return (unsigned char)__float2uint_rn(clampf(v, 0.0f, 1.0f) * 255.0f);
 }
 
-// src/shaders/rasterize.wgsl:32-100: one CTA per 16x16 tile, one thread per pixel,
-// each warp an 8x4 block that walks the tile's list on its own (no CTA barriers,
-// so a warp whose pixels are all done stops without waiting for the others). The
-// list is staged 32 entries at a time into the warp's slice of shared memory,
-// keeping only splats that can reach the block: a splat rejected there has alpha
-// below 1/255 at every pixel of the block, so skipping it changes nothing. At a
-// pixel, a power under the splat's cutoff skips the exp with the same outcome. A
-// pixel stops before the splat that would take its transmittance below 1e-4.
-// Results are bit-identical to the plain loop over every list entry.
+// src/shaders/rasterize.wgsl:32-100. The work is split into independent items,
+// one per (tile, 8x4 pixel block): 8 per 16x16 tile. Each warp is persistent and
+// takes items from a counter, so no warp ever waits for another (a warp whose
+// pixels are all done moves on at once) and the last items spread over every SM.
+// For an item, the warp walks the tile's list, staging 32 entries at a time into
+// its own slice of shared memory and keeping only splats that can reach its block:
+// a splat rejected there has alpha below 1/255 at every pixel of the block, so
+// skipping it changes nothing. At a pixel, a power under the splat's cutoff skips
+// the exp with the same outcome. A pixel stops before the splat that would take
+// its transmittance below 1e-4. Results are bit-identical to the plain loop over
+// every list entry.
 __global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict__ camera,
                                                         const float4* __restrict__ raster_params,
                                                         const float* __restrict__ splats,
                                                         const uint32_t* __restrict__ pair_splats,
                                                         const uint2* __restrict__ ranges, uchar4* __restrict__ target,
                                                         float4* __restrict__ pixel_color,
-                                                        uint32_t* __restrict__ pixel_last) {
+                                                        uint32_t* __restrict__ pixel_last,
+                                                        uint32_t* __restrict__ work_counter) {
   __shared__ WarpStage stages[8];
-  const uint32_t tid = threadIdx.x;
-  WarpStage& st = stages[tid >> 5];
+  const uint32_t lane = threadIdx.x & 31u;
+  WarpStage& st = stages[threadIdx.x >> 5];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
-  const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
-  const uint32_t px = blockIdx.x * TILE + tile_pixel_x(tid), py = blockIdx.y * TILE + tile_pixel_y(tid);
-  const bool inside = (float)px < vpx && (float)py < vpy;
-  const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-  // The warp block's first pixel center.
-  const float x0 = (float)(blockIdx.x * TILE + tile_pixel_x(tid & ~31u)) + 0.5f;
-  const float y0 = (float)(blockIdx.y * TILE + tile_pixel_y(tid & ~31u)) + 0.5f;
-  const uint2 run = ranges[tile];
-  float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
-  bool done = !inside;
-  uint32_t last = 0;
-  for (uint32_t start = run.x; start < run.y; start += 32) {
-    if (__all_sync(0xffffffffu, done)) break;
-    const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, start, run.y, x0, y0);
-    for (uint32_t j = 0; j < staged && !done; j++) {
-      const float2 m = st.mean[j];
-      const float4 q = st.quad[j];
-      const float power = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
-      if (power < q.w) continue;  // alpha < 1/255 for certain
-      if (power > 0.0f) continue;
-      const float4 c = st.color[j];
-      const float alpha = fminf(0.99f, c.w * exp_blend(power));
-      if (alpha < 1.0f / 255.0f) continue;
-      const float remaining = T * (1.0f - alpha);
-      if (remaining < 0.0001f) {
-        done = true;
-        continue;
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE, tiles_y = ((uint32_t)vpy + TILE - 1u) / TILE;
+  const uint32_t items = tiles_x * tiles_y * 8u;
+  const float4 bg = raster_params[0];
+  while (true) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(work_counter, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= items) break;
+    const uint32_t tile = item >> 3, block = item & 7u;
+    const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
+    const uint32_t px = bx + (lane & 7u), py = by + (lane >> 3);
+    const bool inside = (float)px < vpx && (float)py < vpy;
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    const float x0 = (float)bx + 0.5f, y0 = (float)by + 0.5f;  // the block's first pixel center
+    const uint2 run = ranges[tile];
+    float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
+    bool done = !inside;
+    uint32_t last = 0;
+    for (uint32_t start = run.x; start < run.y; start += 32) {
+      if (__all_sync(0xffffffffu, done)) break;
+      const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, start, run.y, x0, y0);
+      for (uint32_t j = 0; j < staged && !done; j++) {
+        const float2 m = st.mean[j];
+        const float4 q = st.quad[j];
+        const float power = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
+        if (power < q.w) continue;  // alpha < 1/255 for certain
+        if (power > 0.0f) continue;
+        const float4 c = st.color[j];
+        const float alpha = fminf(0.99f, c.w * exp_blend(power));
+        if (alpha < 1.0f / 255.0f) continue;
+        const float remaining = T * (1.0f - alpha);
+        if (remaining < 0.0001f) {
+          done = true;
+          continue;
+        }
+        r = r + c.x * alpha * T;
+        g = g + c.y * alpha * T;
+        b = b + c.z * alpha * T;
+        T = remaining;
+        last = st.pos[j] + 1;
       }
-      r = r + c.x * alpha * T;
-      g = g + c.y * alpha * T;
-      b = b + c.z * alpha * T;
-      T = remaining;
-      last = st.pos[j] + 1;
+      __syncwarp();
     }
-    __syncwarp();
-  }
-  if (inside) {
-    const float4 bg = raster_params[0];
-    const float fr = r + T * bg.x, fg = g + T * bg.y, fb = b + T * bg.z;
-    const uint32_t p = py * (uint32_t)vpx + px;
-    pixel_color[p] = make_float4(fr, fg, fb, T);
-    pixel_last[p] = last;
-    if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
+    if (inside) {
+      const float fr = r + T * bg.x, fg = g + T * bg.y, fb = b + T * bg.z;
+      const uint32_t p = py * (uint32_t)vpx + px;
+      pixel_color[p] = make_float4(fr, fg, fb, T);
+      pixel_last[p] = last;
+      if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
+    }
   }
 }
 
@@ -436,6 +445,7 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
   if (st == DG_OK) st = alloc_buffer(ctx, 4, &tr->scan_total);
   if (st == DG_OK) st = alloc_buffer(ctx, scan_scratch_bytes(std::max(count, 1u)), &tr->scan_scratch);
   if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->raster_params);
+  if (st == DG_OK) st = alloc_buffer(ctx, 8, &tr->work);
   if (st == DG_OK && cudaMallocHost(&tr->pinned_total, 4) != cudaSuccess) st = fail(DG_ERROR_OUT_OF_MEMORY, "pinned");
   if (st == DG_OK && cudaEventCreateWithFlags(&tr->readback_event, cudaEventDisableTiming) != cudaSuccess)
     st = fail(DG_ERROR_CUDA, "event");
@@ -551,12 +561,25 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
 
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   dg_context* ctx = tr->ctx;
+  DG_CUDA(cudaMemsetAsync(tr->work->ptr, 0, 4, ctx->stream));
   DG_LAUNCH(ctx, "rasterize",
-            rasterize_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
+            rasterize_kernel<<<blend_grid(tr, (const void*)rasterize_kernel), 256, 0, ctx->stream>>>(
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr,
-                typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last)));
+                typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last), typed<uint32_t>(tr->work)));
   return DG_OK;
+}
+
+uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel) {
+  // As many 8-warp CTAs as can be resident at once; each warp then keeps taking
+  // items, so a CTA that could not start until another finished would find none.
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  const uint32_t items = tr->tiles_x * tr->tiles_y * 8u;
+  return std::max(1u, std::min(ceil_div(items, 8), (uint32_t)(tr->ctx->sm_count * per_sm)));
 }
 
 // The sorted keys in the reference's 64-bit form, rebuilt if the last frame took
@@ -731,7 +754,7 @@ dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
   for (dg_buffer* b : {tr->tile_offsets, tr->scan_total, tr->scan_scratch, tr->raster_params, tr->keys, tr->values,
                        tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last,
                        tr->depth_keys, tr->depth_values, tr->depth_keys_alt, tr->depth_values_alt, tr->depth_scratch,
-                       tr->counts_sorted, tr->keys64})
+                       tr->counts_sorted, tr->keys64, tr->work})
     free_buffer(b);
   if (tr->readback_event) {
     cudaEventSynchronize(tr->readback_event);

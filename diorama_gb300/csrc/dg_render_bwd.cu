@@ -68,130 +68,114 @@ __device__ __forceinline__ int reduce9_slot(int lane) {
   return slot == 15 ? -1 : slot;
 }
 
-// src/shaders/rasterizeBackward.wgsl:50-163. One CTA per 16x16 tile; each warp
-// is an 8x4 pixel block and walks the tile's list on its own, back to front from
-// the largest `last` among its pixels, with no CTA barrier until the end: each
-// pixel recovers the transmittance in front of each splat by dividing the final
-// one by (1 - alpha). The list is staged 32 entries at a time into the warp's
-// slice of shared memory, keeping only splats that can reach the block. A splat's
-// 9 gradient shares are summed over the warp's 32 pixels with shuffles and added
-// into a per-tile accumulator indexed by list position (shared memory for the
-// first ACC_CAP positions, global memory past that); at the end the tile's totals
-// go to global memory with one atomic add per nonzero value.
-constexpr uint32_t ACC_CAP = 1536;
-
+// src/shaders/rasterizeBackward.wgsl:50-163. Like the forward pass, the work is
+// split into independent items, one per (tile, 8x4 pixel block), taken by
+// persistent warps from a counter, so no warp waits for another. For an item, the
+// warp walks the tile's list back to front from the largest `last` among its
+// pixels, staging 32 entries at a time into its own slice of shared memory and
+// keeping only splats that can reach its block; each pixel recovers the
+// transmittance in front of each splat by dividing the final one by (1 - alpha).
+// A splat's 9 gradient shares are summed over the warp's 32 pixels with shuffles
+// and added to its global gradient, one atomic add per nonzero value.
 __global__ void __launch_bounds__(256) rasterize_backward_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const float4* __restrict__ pixel_color,
-    const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads) {
+    const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads,
+    uint32_t* __restrict__ work_counter) {
   __shared__ WarpStage stages[8];
-  __shared__ float s_acc[ACC_CAP * SPLAT_GRADS];
-  __shared__ uint32_t s_max_last;
-  const uint32_t tid = threadIdx.x;
-  const int lane = tid & 31;
-  WarpStage& st = stages[tid >> 5];
+  const int lane = threadIdx.x & 31;
+  WarpStage& st = stages[threadIdx.x >> 5];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
-  const uint32_t tile = blockIdx.y * tiles_x + blockIdx.x;
-  const uint32_t px = blockIdx.x * TILE + tile_pixel_x(tid), py = blockIdx.y * TILE + tile_pixel_y(tid);
-  const bool inside = (float)px < vpx && (float)py < vpy;
-  const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-  const float x0 = (float)(blockIdx.x * TILE + tile_pixel_x(tid & ~31u)) + 0.5f;
-  const float y0 = (float)(blockIdx.y * TILE + tile_pixel_y(tid & ~31u)) + 0.5f;
-  const uint2 run = ranges[tile];
-  float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
-  uint32_t last = 0;
-  if (inside) {
-    const uint32_t p = py * (uint32_t)vpx + px;
-    Tf = pixel_color[p].w;
-    last = pixel_last[p];
-    const float4 pg = pixel_grads[p];
-    pgx = pg.x;
-    pgy = pg.y;
-    pgz = pg.z;
-  }
-  if (tid == 0) s_max_last = 0;
-  __syncthreads();
-  if (last) atomicMax(&s_max_last, last);
-  // Splats at or past a warp's largest `last` contribute nothing to that warp.
-  const uint32_t warp_last = __reduce_max_sync(0xffffffffu, last);
-  __syncthreads();
-  const uint32_t held = min(s_max_last, ACC_CAP);
-  for (uint32_t k = tid; k < held * SPLAT_GRADS; k += 256) s_acc[k] = 0.0f;
-  __syncthreads();
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE, tiles_y = ((uint32_t)vpy + TILE - 1u) / TILE;
+  const uint32_t items = tiles_x * tiles_y * 8u;
+  const float4 bg = raster_params[0];
   // The even lane of each pair adds the value its pair holds after the reduction.
   const int my_slot = (lane & 1) ? -1 : reduce9_slot(lane);
-  const float4 bg = raster_params[0];
-  const float bg_grad = bg.x * pgx + bg.y * pgy + bg.z * pgz;
-  float T = Tf;
-  float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
-  float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
-  for (uint32_t end = run.x + warp_last; end > run.x;) {
-    const uint32_t lo = end - run.x > 32u ? end - 32u : run.x;
-    const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, lo, end, x0, y0);
-    for (uint32_t slot = staged; slot > 0; slot--) {
-      const uint32_t j = slot - 1;
-      const uint32_t pos = st.pos[j];
-      float v[9];
+  while (true) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(work_counter, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= items) break;
+    const uint32_t tile = item >> 3, block = item & 7u;
+    const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
+    const uint32_t px = bx + (lane & 7u), py = by + (lane >> 3);
+    const bool inside = (float)px < vpx && (float)py < vpy;
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    const float x0 = (float)bx + 0.5f, y0 = (float)by + 0.5f;
+    const uint2 run = ranges[tile];
+    float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
+    uint32_t last = 0;
+    if (inside) {
+      const uint32_t p = py * (uint32_t)vpx + px;
+      Tf = pixel_color[p].w;
+      last = pixel_last[p];
+      const float4 pg = pixel_grads[p];
+      pgx = pg.x;
+      pgy = pg.y;
+      pgz = pg.z;
+    }
+    // Splats at or past the warp's largest `last` contribute nothing to it.
+    const uint32_t warp_last = __reduce_max_sync(0xffffffffu, last);
+    const float bg_grad = bg.x * pgx + bg.y * pgy + bg.z * pgz;
+    float T = Tf;
+    float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
+    float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
+    for (uint32_t end = run.x + warp_last; end > run.x;) {
+      const uint32_t lo = end - run.x > 32u ? end - 32u : run.x;
+      const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, lo, end, x0, y0);
+      for (uint32_t slot = staged; slot > 0; slot--) {
+        const uint32_t j = slot - 1;
+        float v[9];
 #pragma unroll
-      for (int q = 0; q < 9; q++) v[q] = 0.0f;
-      bool contributes = false;
-      if (inside && pos < last) {
-        const float2 m = st.mean[j];
-        const float4 q = st.quad[j];
-        const float dx = cx - m.x, dy = cy - m.y;
-        const float power = blend_power(q.x, q.y, q.z, dx, dy);
-        if (power >= q.w && power <= 0.0f) {
-          const float4 c = st.color[j];
-          const float G = exp_blend(power);
-          const float alpha = fminf(0.99f, __fmul_rn(c.w, G));
-          if (alpha >= 1.0f / 255.0f) {
-            contributes = true;
-            const float inv = __frcp_rn(1.0f - alpha);  // 1 / (1 - alpha), used twice
-            T = T * inv;
-            bhx = na * ncx + (1.0f - na) * bhx;
-            bhy = na * ncy + (1.0f - na) * bhy;
-            bhz = na * ncz + (1.0f - na) * bhz;
-            na = alpha;
-            ncx = c.x;
-            ncy = c.y;
-            ncz = c.z;
-            const float dotv = (c.x - bhx) * pgx + (c.y - bhy) * pgy + (c.z - bhz) * pgz;
-            const float alpha_grad = T * dotv - Tf * inv * bg_grad;
-            const float power_grad = alpha_grad * c.w * G;
-            // The conic is (a, b, c) = (-2A, b, -2C).
-            const float ca = -2.0f * q.x, cb = q.y, cc = -2.0f * q.z;
-            v[0] = power_grad * (ca * dx + cb * dy);
-            v[1] = power_grad * (cb * dx + cc * dy);
-            v[2] = power_grad * (-0.5f * dx * dx);
-            v[3] = power_grad * (-dx * dy);
-            v[4] = power_grad * (-0.5f * dy * dy);
-            v[5] = alpha_grad * G;
-            const float w = alpha * T;
-            v[6] = w * pgx;
-            v[7] = w * pgy;
-            v[8] = w * pgz;
+        for (int q = 0; q < 9; q++) v[q] = 0.0f;
+        bool contributes = false;
+        if (inside && st.pos[j] < last) {
+          const float2 m = st.mean[j];
+          const float4 q = st.quad[j];
+          const float dx = cx - m.x, dy = cy - m.y;
+          const float power = blend_power(q.x, q.y, q.z, dx, dy);
+          if (power >= q.w && power <= 0.0f) {
+            const float4 c = st.color[j];
+            const float G = exp_blend(power);
+            const float alpha = fminf(0.99f, __fmul_rn(c.w, G));
+            if (alpha >= 1.0f / 255.0f) {
+              contributes = true;
+              const float inv = __frcp_rn(1.0f - alpha);  // 1 / (1 - alpha), used twice
+              T = T * inv;
+              bhx = na * ncx + (1.0f - na) * bhx;
+              bhy = na * ncy + (1.0f - na) * bhy;
+              bhz = na * ncz + (1.0f - na) * bhz;
+              na = alpha;
+              ncx = c.x;
+              ncy = c.y;
+              ncz = c.z;
+              const float dotv = (c.x - bhx) * pgx + (c.y - bhy) * pgy + (c.z - bhz) * pgz;
+              const float alpha_grad = T * dotv - Tf * inv * bg_grad;
+              const float power_grad = alpha_grad * c.w * G;
+              // The conic is (a, b, c) = (-2A, b, -2C).
+              const float ca = -2.0f * q.x, cb = q.y, cc = -2.0f * q.z;
+              v[0] = power_grad * (ca * dx + cb * dy);
+              v[1] = power_grad * (cb * dx + cc * dy);
+              v[2] = power_grad * (-0.5f * dx * dx);
+              v[3] = power_grad * (-dx * dy);
+              v[4] = power_grad * (-0.5f * dy * dy);
+              v[5] = alpha_grad * G;
+              const float w = alpha * T;
+              v[6] = w * pgx;
+              v[7] = w * pgy;
+              v[8] = w * pgz;
+            }
           }
         }
-      }
-      if (__any_sync(0xffffffffu, contributes)) {
-        const float total = warp_reduce9(v, lane);
-        if (my_slot >= 0 && total != 0.0f) {
-          if (pos < ACC_CAP)
-            atomicAdd(&s_acc[pos * SPLAT_GRADS + my_slot], total);
-          else
+        if (__any_sync(0xffffffffu, contributes)) {
+          const float total = warp_reduce9(v, lane);
+          if (my_slot >= 0 && total != 0.0f)
             atomicAdd(&splat_grads[(size_t)st.index[j] * SPLAT_GRADS + my_slot], total);
         }
       }
+      __syncwarp();
+      end = lo;
     }
-    __syncwarp();
-    end = lo;
-  }
-  __syncthreads();
-  for (uint32_t k = tid; k < held * SPLAT_GRADS; k += 256) {
-    const float total = s_acc[k];
-    if (total != 0.0f)
-      atomicAdd(&splat_grads[(size_t)pair_splats[run.x + k / SPLAT_GRADS] * SPLAT_GRADS + k % SPLAT_GRADS], total);
   }
 }
 
@@ -415,11 +399,13 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(
 
 dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads) {
   dg_context* ctx = tr->ctx;
+  uint32_t* counter = typed<uint32_t>(tr->work) + 1;
+  DG_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), ctx->stream));
   DG_LAUNCH(ctx, "rasterize_backward",
-            rasterize_backward_kernel<<<dim3(tr->tiles_x, tr->tiles_y), 256, 0, ctx->stream>>>(
+            rasterize_backward_kernel<<<blend_grid(tr, (const void*)rasterize_backward_kernel), 256, 0, ctx->stream>>>(
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads)));
+                typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads), counter));
   return DG_OK;
 }
 

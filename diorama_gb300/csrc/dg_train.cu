@@ -23,7 +23,8 @@ struct AdamParams {
   float bias_correction1, bias_correction2;
   float position_lr, opacity_lr, scale_lr, rotation_lr, color_lr, sh_lr;
   float viewport[2];
-  float pad[2];
+  // Reciprocals of the bias corrections (and of the second's square root), from the host.
+  float inv_bias_correction1, inv_sqrt_bias_correction2;
 };
 
 // DensifyParams (src/shaders/densify.wgsl:149-161)
@@ -42,92 +43,74 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
   return raw;
 }
 
-// src/shaders/adam.wgsl:80-107, one warp per Gaussian: lanes 0-31 take moment
-// slots 0-31 (the 16 raw parameters, then SH coefficients 0-15) and lanes 0-28
-// slots 32-60 (SH 16-44). A Gaussian's moments are 488 contiguous bytes and its
-// parameters, SH coefficients and gradients are contiguous runs too, so every
-// access coalesces, and the per-slot chain rule is written without branches so
-// the warp never splits. Slots 7 and 15 (padding, which holds densification
-// stamps) are left alone.
-// Adam's update with the bias corrections applied as reciprocals computed once:
-// within two ulps of value - lr (m/bc1) / (sqrt(v/bc2) + eps).
-__device__ __forceinline__ float adam_step_fast(float value, float grad, float2& m, float lr, float inv_bc1,
-                                                float inv_bc2) {
-  m.x = 0.9f * m.x + 0.1f * grad;
-  m.y = 0.999f * m.y + 0.001f * grad * grad;
-  return value - lr * (m.x * inv_bc1) * __frcp_rn(sqrtf(m.y * inv_bc2) + 1e-15f);
+// src/shaders/adam.wgsl:80-107 as two flat elementwise kernels over Adam's slots:
+// adam_sh_kernel over the 45 SH coefficients of every Gaussian (moment slots
+// 16-60) and adam_param_kernel over the 16 raw parameters (slots 0-15). Each
+// thread takes one slot, so parameters, gradients and moments are read in
+// consecutive runs and no thread waits on another. Slots 7 and 15 (padding, which
+// holds densification stamps) are left alone.
+//
+// The step uses the host's reciprocals of the bias corrections and approximate
+// square root and division: within a few ulps of
+// value - lr (m / bc1) / (sqrt(v / bc2) + eps).
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
-__global__ void __launch_bounds__(256) adam_kernel(const AdamParams* __restrict__ ap, float* __restrict__ params,
-                                                   float* __restrict__ sh, float2* __restrict__ moments,
-                                                   const float* __restrict__ ggrad, const float* __restrict__ sgrad,
-                                                   float* __restrict__ gaussians, uint32_t count) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= count) return;
-  const float inv_bc1 = 1.0f / ap->bias_correction1, inv_bc2 = 1.0f / ap->bias_correction2;
-  // Round 1: lane k < 16 holds raw parameter k (its group's learning rate and chain
-  // rule), lanes 16-31 SH coefficients 0-15. Round 2: lanes 0-28 SH 16-44.
-  // kind: 0 position/rotation, 1 opacity, 2 scale, 3 colour, 4 padding, 5 SH.
-  const uint32_t kind = lane >= 16  ? 5u
-                        : lane < 3  ? 0u
-                        : lane == 3 ? 1u
-                        : lane < 7  ? 2u
-                        : lane == 7 ? 4u
-                        : lane < 12 ? 0u
-                        : lane < 15 ? 3u
-                                    : 4u;
-  const float lr1 = kind == 5   ? ap->sh_lr
-                    : lane < 3  ? ap->position_lr
-                    : lane == 3 ? ap->opacity_lr
-                    : lane < 7  ? ap->scale_lr
-                    : lane < 12 ? ap->rotation_lr
-                                : ap->color_lr;
-  const float sh_lr = ap->sh_lr;
-  const size_t slot0 = (size_t)i * MOMENT_SLOTS;
-  const bool param = lane < FLOATS_PER_GAUSSIAN;
-  const bool second = lane < MOMENT_SLOTS - 32;
-  float* p1 = param ? params + (size_t)i * FLOATS_PER_GAUSSIAN + lane : sh + (size_t)i * SH_REST_FLOATS + (lane - 16);
-  const float* g1 = param ? ggrad + (size_t)i * FLOATS_PER_GAUSSIAN + lane : sgrad + (size_t)i * SH_REST_FLOATS + (lane - 16);
-  const size_t s2 = (size_t)i * SH_REST_FLOATS + 16 + lane;
-  // Every load of both rounds is in flight before any arithmetic.
-  float2 m1 = moments[slot0 + lane];
-  const float x1 = *p1, d1 = *g1;
-  float2 m2 = make_float2(0.f, 0.f);
-  float x2 = 0.f, d2 = 0.f;
-  if (second) {
-    m2 = moments[slot0 + 32 + lane];
-    x2 = sh[s2];
-    d2 = sgrad[s2];
+__device__ __forceinline__ float adam_step_fast(float value, float grad, float2& m, float lr, float inv_bc1,
+                                                float inv_sqrt_bc2) {
+  m.x = 0.9f * m.x + 0.1f * grad;
+  m.y = 0.999f * m.y + 0.001f * grad * grad;
+  return value - __fdividef(lr * (m.x * inv_bc1), sqrt_approx(m.y) * inv_sqrt_bc2 + 1e-15f);
+}
+
+__global__ void __launch_bounds__(256) adam_sh_kernel(const AdamParams* __restrict__ ap, float* __restrict__ sh,
+                                                      float2* __restrict__ moments, const float* __restrict__ sgrad,
+                                                      uint32_t count) {
+  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= count * SH_REST_FLOATS) return;
+  const uint32_t i = e / SH_REST_FLOATS, j = e - i * SH_REST_FLOATS;
+  const size_t slot = (size_t)i * MOMENT_SLOTS + FLOATS_PER_GAUSSIAN + j;
+  float2 m = moments[slot];
+  const float x = sh[e], g = sgrad[e];
+  sh[e] = adam_step_fast(x, g, m, ap->sh_lr, ap->inv_bias_correction1, ap->inv_sqrt_bias_correction2);
+  moments[slot] = m;
+}
+
+__global__ void __launch_bounds__(256) adam_param_kernel(const AdamParams* __restrict__ ap,
+                                                         float* __restrict__ params, float2* __restrict__ moments,
+                                                         const float* __restrict__ ggrad,
+                                                         float* __restrict__ gaussians, uint32_t count) {
+  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
+  if (e >= count * FLOATS_PER_GAUSSIAN) return;
+  const uint32_t i = e >> 4, k = e & 15u;
+  if (k == 7 || k == 15) return;
+  const size_t slot = (size_t)i * MOMENT_SLOTS + k;
+  float2 m = moments[slot];
+  const float x = params[e];
+  float grad = ggrad[e];
+  float lr;
+  if (k < 3) {
+    lr = ap->position_lr;
+  } else if (k == 3) {
+    const float opacity = sigmoidf_(x);
+    grad = grad * opacity * (1.0f - opacity);
+    lr = ap->opacity_lr;
+  } else if (k < 7) {
+    grad = grad * expf(x);
+    lr = ap->scale_lr;
+  } else if (k < 12) {
+    lr = ap->rotation_lr;
+  } else {
+    grad = grad * SH_C0;
+    lr = ap->color_lr;
   }
-  if (kind != 4) {
-    // One exp serves both chain rules: exp(value) for a scale, exp(-value) for the opacity's sigmoid.
-    float grad = d1;
-    if (kind == 1 || kind == 2) {
-      const float e = expf(kind == 1 ? -x1 : x1);
-      const float opacity = 1.0f / (1.0f + e);
-      grad = kind == 2 ? grad * e : grad * opacity * (1.0f - opacity);
-    } else if (kind == 3) {
-      grad = grad * SH_C0;
-    }
-    const float n1 = adam_step_fast(x1, grad, m1, lr1, inv_bc1, inv_bc2);
-    *p1 = n1;
-    moments[slot0 + lane] = m1;
-    if (param) {
-      float act = n1;
-      if (kind == 1 || kind == 2) {
-        const float e = expf(kind == 1 ? -n1 : n1);
-        act = kind == 2 ? e : 1.0f / (1.0f + e);
-      } else if (kind == 3) {
-        act = 0.5f + SH_C0 * n1;
-      }
-      gaussians[(size_t)i * FLOATS_PER_GAUSSIAN + lane] = act;
-    }
-  }
-  if (second) {
-    sh[s2] = adam_step_fast(x2, d2, m2, sh_lr, inv_bc1, inv_bc2);
-    moments[slot0 + 32 + lane] = m2;
-  }
+  const float next = adam_step_fast(x, grad, m, lr, ap->inv_bias_correction1, ap->inv_sqrt_bias_correction2);
+  params[e] = next;
+  moments[slot] = m;
+  gaussians[e] = activated(k, next);
 }
 
 // src/shaders/adam.wgsl:74-77, one thread per raw float.
@@ -375,11 +358,14 @@ static dg_status launch_stats(dg_trainer* t) {
 
 static dg_status launch_adam(dg_trainer* t) {
   dg_renderer* r = t->renderer;
-  DG_LAUNCH(t->ctx, "adam",
-            adam_kernel<<<ceil_div(t->count, 8), 256, 0, t->ctx->stream>>>(
-                typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float>(r->sh),
-                typed<float2>(t->moments), typed<float>(r->grad_gaussians), typed<float>(r->grad_sh),
-                typed<float>(r->gaussians), t->count));
+  DG_LAUNCH(t->ctx, "adam_sh",
+            adam_sh_kernel<<<ceil_div((uint64_t)t->count * SH_REST_FLOATS, 256), 256, 0, t->ctx->stream>>>(
+                typed<AdamParams>(t->adam_params), typed<float>(r->sh), typed<float2>(t->moments),
+                typed<float>(r->grad_sh), t->count));
+  DG_LAUNCH(t->ctx, "adam_param",
+            adam_param_kernel<<<ceil_div((uint64_t)t->count * FLOATS_PER_GAUSSIAN, 256), 256, 0, t->ctx->stream>>>(
+                typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float2>(t->moments),
+                typed<float>(r->grad_gaussians), typed<float>(r->gaussians), t->count));
   return DG_OK;
 }
 
@@ -529,6 +515,8 @@ dg_status dg_trainer_optimize(dg_trainer* t) {
   AdamParams ap{};
   ap.bias_correction1 = (float)(1 - std::pow(0.9, t->adam_steps));
   ap.bias_correction2 = (float)(1 - std::pow(0.999, t->adam_steps));
+  ap.inv_bias_correction1 = (float)(1.0 / (double)ap.bias_correction1);
+  ap.inv_sqrt_bias_correction2 = (float)(1.0 / std::sqrt((double)ap.bias_correction2));
   ap.position_lr = (float)position_lr;
   ap.opacity_lr = (float)s.opacity_lr;
   ap.scale_lr = (float)s.scale_lr;
