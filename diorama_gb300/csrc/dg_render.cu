@@ -326,79 +326,325 @@ __device__ __forceinline__ unsigned char to_unorm8(float v) {
   return (unsigned char)__float2uint_rn(clampf(v, 0.0f, 1.0f) * 255.0f);
 }
 
-// src/shaders/rasterize.wgsl:32-100. The work is split into independent items,
-// one per (tile, 8x4 pixel block): 8 per 16x16 tile. Each warp is persistent and
-// takes items from a counter, so no warp ever waits for another (a warp whose
-// pixels are all done moves on at once) and the last items spread over every SM.
-// For an item, the warp walks the tile's list, staging 32 entries at a time into
-// its own slice of shared memory and keeping only splats that can reach its block:
-// a splat rejected there has alpha below 1/255 at every pixel of the block, so
-// skipping it changes nothing. At a pixel, a power under the splat's cutoff skips
-// the exp with the same outcome. A pixel stops before the splat that would take
-// its transmittance below 1e-4. Results are bit-identical to the plain loop over
-// every list entry.
-__global__ void __launch_bounds__(256) rasterize_kernel(const Camera* __restrict__ camera,
-                                                        const float4* __restrict__ raster_params,
-                                                        const float* __restrict__ splats,
-                                                        const uint32_t* __restrict__ pair_splats,
-                                                        const uint2* __restrict__ ranges, uchar4* __restrict__ target,
-                                                        float4* __restrict__ pixel_color,
-                                                        uint32_t* __restrict__ pixel_last,
-                                                        uint32_t* __restrict__ work_counter) {
-  __shared__ WarpStage stages[8];
-  const uint32_t lane = threadIdx.x & 31u;
-  WarpStage& st = stages[threadIdx.x >> 5];
+// ------------------------------------------------------------------ work plan
+// Orders the frame's blend work; one CTA. The forward pass takes tiles with more
+// than COOP_MIN entries first, longest first by powers of two, then the rest; the
+// backward pass takes the (tile, chunk) pairs of tiles with several chunks first.
+// Order within a group follows atomics and does not change any result.
+constexpr uint32_t PLAN_THREADS = 1024;
+
+__global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(const uint2* __restrict__ ranges, uint32_t tiles,
+                                                            uint32_t* __restrict__ plan, uint2* __restrict__ chunks) {
+  __shared__ uint32_t s_bucket[32];  // cooperative tiles by floor(log2(length)); then write cursors
+  __shared__ uint32_t s_light, s_multi, s_single;
+  const uint32_t tid = threadIdx.x;
+  if (tid < 32) s_bucket[tid] = 0;
+  if (tid == 0) s_multi = 0;
+  __syncthreads();
+  for (uint32_t t = tid; t < tiles; t += PLAN_THREADS) {
+    const uint2 r = ranges[t];
+    const uint32_t len = r.y - r.x;
+    if (len > COOP_MIN) atomicAdd(&s_bucket[31 - __clz(len)], 1u);
+    const uint32_t nb = (len + CHUNK - 1) / CHUNK;
+    if (nb > 1) atomicAdd(&s_multi, nb);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t at = 0;
+    for (int k = 31; k >= 0; k--) {
+      const uint32_t c = s_bucket[k];
+      s_bucket[k] = at;
+      at += c;
+    }
+    plan[0] = at;
+    plan[1] = tiles;
+    s_light = at;
+    s_single = s_multi;
+    s_multi = 0;
+  }
+  __syncthreads();
+  uint32_t* order = plan + PLAN_HEADER;
+  for (uint32_t t = tid; t < tiles; t += PLAN_THREADS) {
+    const uint2 r = ranges[t];
+    const uint32_t len = r.y - r.x;
+    order[len > COOP_MIN ? atomicAdd(&s_bucket[31 - __clz(len)], 1u) : atomicAdd(&s_light, 1u)] = t;
+    const uint32_t nb = (len + CHUNK - 1) / CHUNK;
+    if (nb > 1) {
+      const uint32_t at = atomicAdd(&s_multi, nb);
+      for (uint32_t k = 0; k < nb; k++) chunks[at + k] = make_uint2(t, k);
+    } else if (nb == 1) {
+      chunks[atomicAdd(&s_single, 1u)] = make_uint2(t, 0u);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    plan[2] = s_single;
+    plan[3] = 0;
+  }
+}
+
+// Writes the checkpoints of boundaries [k_from, k_to) of a tile with one pixel state.
+__device__ __forceinline__ void save_checkpoints(float4* __restrict__ checkpoints, uint32_t run_x, uint32_t k_from,
+                                                 uint32_t k_to, uint32_t block, uint32_t lane, float T, float r,
+                                                 float g, float b) {
+  for (uint32_t k = k_from; k < k_to; k++) checkpoints[checkpoint_at(run_x, k, block, lane)] = make_float4(T, r, g, b);
+}
+
+// One pixel's front-to-back blend (src/shaders/rasterize.wgsl:62-92), the lane's
+// pixel of a warp's 8x4 block.
+struct PixelBlend {
+  float cx, cy;
+  float T, r, g, b;
+  uint32_t last;
+  bool done;
+
+  // The alphas of up to 4 staged entries e[0..n) of `st` at this pixel, 0 where
+  // the pixel does not blend the splat (alpha under 1/255; a power under the
+  // splat's cutoff skips the exp with the same outcome). Computed together:
+  // independent work the SM can overlap. Returns false, with all alphas 0, when
+  // no lane reaches any of the 4 cutoffs.
+  __device__ __forceinline__ bool alphas4(const WarpStage& st, const uint32_t (&e)[4], uint32_t n, bool active,
+                                          float (&alpha)[4]) const {
+    float power[4];
+    bool need[4], any = false;
+#pragma unroll
+    for (uint32_t u = 0; u < 4; u++) {
+      const float2 m = st.mean[e[u]];
+      const float4 q = st.quad[e[u]];
+      power[u] = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
+      need[u] = active && u < n && power[u] >= q.w && power[u] <= 0.0f;
+      any |= need[u];
+    }
+    if (!__any_sync(0xffffffffu, any)) {
+#pragma unroll
+      for (uint32_t u = 0; u < 4; u++) alpha[u] = 0.0f;
+      return false;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < 4; u++) {
+      const float a = fminf(0.99f, st.color[e[u]].w * exp_blend(need[u] ? power[u] : 0.0f));
+      alpha[u] = need[u] && a >= 1.0f / 255.0f ? a : 0.0f;
+    }
+    return true;
+  }
+
+  // Blends one splat of alpha `alpha` (0: not blended here) and colour c at list
+  // position pos; stops before the splat that would take the transmittance
+  // below 1e-4.
+  __device__ __forceinline__ void blend(float alpha, float4 c, uint32_t pos) {
+    if (alpha == 0.0f || done) return;
+    const float remaining = T * (1.0f - alpha);
+    if (remaining < 0.0001f) {
+      done = true;
+      return;
+    }
+    r = r + c.x * alpha * T;
+    g = g + c.y * alpha * T;
+    b = b + c.z * alpha * T;
+    T = remaining;
+    last = pos + 1;
+  }
+
+  // Applies up to 4 staged entries e[0..n) of `st` in list order.
+  __device__ __forceinline__ void apply4(const WarpStage& st, const uint32_t (&e)[4], uint32_t n) {
+    float alpha[4];
+    if (!alphas4(st, e, n, !done, alpha)) return;
+#pragma unroll
+    for (uint32_t u = 0; u < 4; u++)
+      if (alpha[u] != 0.0f) blend(alpha[u], st.color[e[u]], st.pos[e[u]]);
+  }
+};
+
+// The geometry of a blend item: tile `tile`, 8x4 block `block`, this lane's pixel.
+struct BlendItem {
+  uint32_t px, py;
+  bool inside;
+  float x0, y0;  // the block's first pixel center
+  uint2 run;
+  __device__ __forceinline__ BlendItem(uint32_t tile, uint32_t block, uint32_t lane, uint32_t tiles_x, float vpx,
+                                       float vpy, const uint2* __restrict__ ranges) {
+    const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
+    px = bx + (lane & 7u);
+    py = by + (lane >> 3);
+    inside = (float)px < vpx && (float)py < vpy;
+    x0 = (float)bx + 0.5f;
+    y0 = (float)by + 0.5f;
+    run = ranges[tile];
+  }
+};
+
+__device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlend& pb, float4 bg, uint32_t width,
+                                            uchar4* __restrict__ target, float4* __restrict__ pixel_color,
+                                            uint32_t* __restrict__ pixel_last) {
+  if (!it.inside) return;
+  const float fr = pb.r + pb.T * bg.x, fg = pb.g + pb.T * bg.y, fb = pb.b + pb.T * bg.z;
+  const uint32_t p = it.py * width + it.px;
+  pixel_color[p] = make_float4(fr, fg, fb, pb.T);
+  pixel_last[p] = pb.last;
+  if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
+}
+
+// src/shaders/rasterize.wgsl:32-100. The work is split into items, one per (tile,
+// 8x4 pixel block): 8 per 16x16 tile, taken from counters by persistent CTAs and
+// warps in the plan's order. Whatever the split, each pixel blends the tile's list
+// front to back exactly as the plain loop over every entry does, so results are
+// bit-identical to it; the split only decides who does the work:
+//
+// - Tiles with more than COOP_MIN entries come first, each block blended by a
+//   whole CTA. Its warps take consecutive 32-entry windows, keep the splats that
+//   can reach the block and compute their alphas at the block's pixels, queueing
+//   those some pixel blends; warp 0 then applies the queued alphas of all the
+//   windows in list order. The costly part of each splat (power, exp, alpha) is
+//   spread over the CTA; only the short transmittance update stays serial.
+// - Every warp then takes the other blocks on its own, walking the list 32
+//   entries at a time.
+//
+// In both, a window's splat records are copied into shared memory while the
+// previous one blends, a splat rejected for the block has alpha below 1/255 at
+// all of its pixels, and a power under the splat's cutoff skips the exp: none of
+// these changes a result. The pixel state at each CHUNK boundary of the list is
+// saved for the backward pass.
+__global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
+    const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
+    const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
+    uchar4* __restrict__ target, float4* __restrict__ pixel_color, uint32_t* __restrict__ pixel_last,
+    float4* __restrict__ checkpoints, uint32_t* __restrict__ counters) {
+  __shared__ WarpStage stages[FWD_WARPS];
+  __shared__ float s_alpha[FWD_WARPS][32][32];  // cooperative: alphas of each warp's queued entries
+  __shared__ uint32_t s_item, s_stop;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  WarpStage& st = stages[warp];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE, tiles_y = ((uint32_t)vpy + TILE - 1u) / TILE;
-  const uint32_t items = tiles_x * tiles_y * 8u;
+  const uint32_t width = (uint32_t)vpx;
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
   const float4 bg = raster_params[0];
+  const uint32_t cooperative = plan[0], tiles = plan[1];
+  const uint32_t* order = plan + PLAN_HEADER;
+
+  // Cooperative items: one block of a long tile per CTA.
+  while (true) {
+    __syncthreads();  // everyone has read the previous s_item
+    if (threadIdx.x == 0) s_item = atomicAdd(&counters[0], 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= cooperative * 8u) break;
+    const uint32_t block = item & 7u;
+    const BlendItem it(order[item >> 3], block, lane, tiles_x, vpx, vpy, ranges);
+    const uint2 run = it.run;
+    PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
+    uint32_t next_k = 1;  // the next checkpoint boundary (warp 0)
+    // Warp w takes windows w, w + FWD_WARPS, ...: this lane's entry of the window
+    // in flight and of the one after it.
+    uint32_t index = 0, next_index = 0;
+    {
+      const uint32_t k = run.x + 32u * warp + lane;
+      if (k < run.y) index = pair_splats[k];
+      stage_issue(st, splats, index, k < run.y);
+      if (k + 32u * FWD_WARPS < run.y) next_index = pair_splats[k + 32u * FWD_WARPS];
+    }
+    for (uint32_t round = run.x; round < run.y; round += 32u * FWD_WARPS) {
+      const uint32_t start = round + 32u * warp;
+      if (start < run.y) {
+        const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
+        {
+          const uint32_t k = start + 32u * FWD_WARPS + lane;
+          stage_issue(st, splats, next_index, k < run.y);
+          index = next_index;
+          next_index = k + 32u * FWD_WARPS < run.y ? pair_splats[k + 32u * FWD_WARPS] : 0u;
+        }
+        // The alphas of the kept entries at the block's pixels; entries no pixel
+        // blends are dropped, the others queued with their alphas for warp 0.
+        uint32_t live = 0;
+        for (uint32_t j = 0; j < staged; j += 4) {
+          const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
+          float alpha[4];
+          if (!pb.alphas4(st, e, staged - j, it.inside, alpha)) continue;
+#pragma unroll
+          for (uint32_t u = 0; u < 4; u++) {
+            if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
+              if (lane == 0) st.live[live] = (uint8_t)(j + u);
+              s_alpha[warp][live][lane] = alpha[u];
+              live++;
+            }
+          }
+        }
+        if (lane == 0) st.live_count = live;
+      } else if (lane == 0) {
+        st.live_count = 0;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        for (uint32_t w = 0; w < FWD_WARPS; w++) {
+          const uint32_t ws = round + 32u * w;
+          if (ws >= run.y) break;
+          if (ws - run.x == next_k * CHUNK) {
+            save_checkpoints(checkpoints, run.x, next_k, next_k + 1, block, lane, pb.T, pb.r, pb.g, pb.b);
+            next_k++;
+          }
+          const WarpStage& sw = stages[w];
+          const uint32_t n = sw.live_count;
+#pragma unroll 4
+          for (uint32_t m = 0; m < n; m++) {
+            const uint32_t e = sw.live[m];
+            pb.blend(s_alpha[w][m][lane], sw.color[e], sw.pos[e]);
+          }
+        }
+        const bool stop = __all_sync(0xffffffffu, pb.done);
+        if (lane == 0) s_stop = stop;
+      }
+      __syncthreads();
+      if (s_stop) break;
+    }
+    cp_async_wait_all();
+    if (warp == 0) {
+      save_checkpoints(checkpoints, run.x, next_k, (run.y - run.x + CHUNK - 1) / CHUNK, block, lane, pb.T, pb.r, pb.g,
+                       pb.b);
+      write_pixel(it, pb, bg, width, target, pixel_color, pixel_last);
+    }
+  }
+
+  // Independent items: one block per warp.
   while (true) {
     uint32_t item = 0;
-    if (lane == 0) item = atomicAdd(work_counter, 1u);
+    if (lane == 0) item = atomicAdd(&counters[1], 1u);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= items) break;
-    const uint32_t tile = item >> 3, block = item & 7u;
-    const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
-    const uint32_t px = bx + (lane & 7u), py = by + (lane >> 3);
-    const bool inside = (float)px < vpx && (float)py < vpy;
-    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-    const float x0 = (float)bx + 0.5f, y0 = (float)by + 0.5f;  // the block's first pixel center
-    const uint2 run = ranges[tile];
-    float T = 1.0f, r = 0.0f, g = 0.0f, b = 0.0f;
-    bool done = !inside;
-    uint32_t last = 0;
+    if (item >= (tiles - cooperative) * 8u) break;
+    const uint32_t block = item & 7u;
+    const BlendItem it(order[cooperative + (item >> 3)], block, lane, tiles_x, vpx, vpy, ranges);
+    const uint2 run = it.run;
+    PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
+    uint32_t next_k = 1;
+    uint32_t index = 0, next_index = 0;
+    {
+      const uint32_t k = run.x + lane;
+      if (k < run.y) index = pair_splats[k];
+      stage_issue(st, splats, index, k < run.y);
+      if (k + 32u < run.y) next_index = pair_splats[k + 32u];
+    }
     for (uint32_t start = run.x; start < run.y; start += 32) {
-      if (__all_sync(0xffffffffu, done)) break;
-      const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, start, run.y, x0, y0);
-      for (uint32_t j = 0; j < staged && !done; j++) {
-        const float2 m = st.mean[j];
-        const float4 q = st.quad[j];
-        const float power = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
-        if (power < q.w) continue;  // alpha < 1/255 for certain
-        if (power > 0.0f) continue;
-        const float4 c = st.color[j];
-        const float alpha = fminf(0.99f, c.w * exp_blend(power));
-        if (alpha < 1.0f / 255.0f) continue;
-        const float remaining = T * (1.0f - alpha);
-        if (remaining < 0.0001f) {
-          done = true;
-          continue;
-        }
-        r = r + c.x * alpha * T;
-        g = g + c.y * alpha * T;
-        b = b + c.z * alpha * T;
-        T = remaining;
-        last = st.pos[j] + 1;
+      if (__all_sync(0xffffffffu, pb.done)) break;
+      if (start - run.x == next_k * CHUNK) {
+        save_checkpoints(checkpoints, run.x, next_k, next_k + 1, block, lane, pb.T, pb.r, pb.g, pb.b);
+        next_k++;
+      }
+      const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
+      {
+        const uint32_t k = start + 32u + lane;
+        stage_issue(st, splats, next_index, k < run.y);
+        index = next_index;
+        next_index = k + 32u < run.y ? pair_splats[k + 32u] : 0u;
+      }
+      for (uint32_t j = 0; j < staged; j += 4) {
+        if (__all_sync(0xffffffffu, pb.done)) break;
+        const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
+        pb.apply4(st, e, staged - j);
       }
       __syncwarp();
     }
-    if (inside) {
-      const float fr = r + T * bg.x, fg = g + T * bg.y, fb = b + T * bg.z;
-      const uint32_t p = py * (uint32_t)vpx + px;
-      pixel_color[p] = make_float4(fr, fg, fb, T);
-      pixel_last[p] = last;
-      if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
-    }
+    cp_async_wait_all();  // a window may still be in flight after an early stop
+    save_checkpoints(checkpoints, run.x, next_k, (run.y - run.x + CHUNK - 1) / CHUNK, block, lane, pb.T, pb.r, pb.g,
+                     pb.b);
+    write_pixel(it, pb, bg, width, target, pixel_color, pixel_last);
   }
 }
 
@@ -411,6 +657,8 @@ __global__ void clear_target_kernel(uchar4* __restrict__ target, uint32_t pixels
 }  // namespace
 
 // ------------------------------------------------------------ TileRasterizer
+
+static dg_status ensure_plan(dg_tile_rasterizer* tr);
 
 static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
   dg_context* ctx = tr->ctx;
@@ -429,7 +677,7 @@ static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
   DG_TRY(alloc_buffer(ctx, (size_t)capacity * 4, &tr->values_alt));
   DG_TRY(alloc_buffer(ctx, std::max(sort_scratch_bytes(tr->plan), sort_scratch_bytes(tr->tile_plan)),
                       &tr->sort_scratch));
-  return DG_OK;
+  return ensure_plan(tr);
 }
 
 dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity) { return make_pairs(tr, capacity); }
@@ -445,7 +693,7 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
   if (st == DG_OK) st = alloc_buffer(ctx, 4, &tr->scan_total);
   if (st == DG_OK) st = alloc_buffer(ctx, scan_scratch_bytes(std::max(count, 1u)), &tr->scan_scratch);
   if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->raster_params);
-  if (st == DG_OK) st = alloc_buffer(ctx, 8, &tr->work);
+  if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->work);
   if (st == DG_OK && cudaMallocHost(&tr->pinned_total, 4) != cudaSuccess) st = fail(DG_ERROR_OUT_OF_MEMORY, "pinned");
   if (st == DG_OK && cudaEventCreateWithFlags(&tr->readback_event, cudaEventDisableTiming) != cudaSuccess)
     st = fail(DG_ERROR_CUDA, "event");
@@ -486,6 +734,7 @@ dg_status rasterizer_prepare(dg_tile_rasterizer* tr, const float viewport[2], co
     tr->ranges = nullptr;
     DG_TRY(alloc_buffer(tr->ctx, (size_t)std::max(tiles, 1u) * 8, &tr->ranges));
     tr->ranges_tiles = tiles;
+    DG_TRY(ensure_plan(tr));
   }
   const uint32_t pixels = (uint32_t)viewport[0] * (uint32_t)viewport[1];
   if (!tr->pixel_color || tr->pixel_count < pixels) {
@@ -561,25 +810,51 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
 
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   dg_context* ctx = tr->ctx;
-  DG_CUDA(cudaMemsetAsync(tr->work->ptr, 0, 4, ctx->stream));
+  const uint32_t tiles = tr->tiles_x * tr->tiles_y;
+  DG_CUDA(cudaMemsetAsync(tr->work->ptr, 0, 16, ctx->stream));
+  DG_LAUNCH(ctx, "plan",
+            plan_kernel<<<1, PLAN_THREADS, 0, ctx->stream>>>(typed<uint2>(tr->ranges), tiles, typed<uint32_t>(tr->work_plan),
+                                                             typed<uint2>(tr->chunks)));
   DG_LAUNCH(ctx, "rasterize",
-            rasterize_kernel<<<blend_grid(tr, (const void*)rasterize_kernel), 256, 0, ctx->stream>>>(
+            rasterize_kernel<<<blend_grid(tr, (const void*)rasterize_kernel, FWD_THREADS), FWD_THREADS, 0,
+                               ctx->stream>>>(
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
-                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), target ? typed<uchar4>(target) : nullptr,
-                typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last), typed<uint32_t>(tr->work)));
+                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
+                target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
+                typed<uint32_t>(tr->pixel_last), typed<float4>(tr->checkpoints), typed<uint32_t>(tr->work)));
   return DG_OK;
 }
 
-uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel) {
-  // As many 8-warp CTAs as can be resident at once; each warp then keeps taking
-  // items, so a CTA that could not start until another finished would find none.
+uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel, uint32_t threads) {
+  // As many CTAs as can be resident at once; each keeps taking items, so a CTA
+  // that could not start until another finished would find none.
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)threads, 0) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();
     per_sm = 1;
   }
   const uint32_t items = tr->tiles_x * tr->tiles_y * 8u;
-  return std::max(1u, std::min(ceil_div(items, 8), (uint32_t)(tr->ctx->sm_count * per_sm)));
+  return std::max(1u, std::min(ceil_div(items, threads / 32u), (uint32_t)(tr->ctx->sm_count * per_sm)));
+}
+
+// The work plan, the backward's chunk list and the checkpoints, sized for the
+// allocated tiles and pair capacity.
+static dg_status ensure_plan(dg_tile_rasterizer* tr) {
+  const size_t tiles = std::max(tr->ranges_tiles, 1u);
+  const size_t slots = (size_t)tr->pair_capacity / CHUNK + 1;
+  struct Need {
+    dg_buffer** buf;
+    size_t bytes;
+  } needs[] = {{&tr->work_plan, (PLAN_HEADER + tiles) * 4},
+               {&tr->chunks, (tiles + slots) * 8},
+               {&tr->checkpoints, slots * 8 * 32 * 16}};
+  for (const Need& n : needs) {
+    if (*n.buf && (*n.buf)->bytes >= n.bytes) continue;
+    free_buffer(*n.buf);
+    *n.buf = nullptr;
+    DG_TRY(alloc_buffer(tr->ctx, n.bytes, n.buf));
+  }
+  return DG_OK;
 }
 
 // The sorted keys in the reference's 64-bit form, rebuilt if the last frame took
@@ -754,7 +1029,7 @@ dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
   for (dg_buffer* b : {tr->tile_offsets, tr->scan_total, tr->scan_scratch, tr->raster_params, tr->keys, tr->values,
                        tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last,
                        tr->depth_keys, tr->depth_values, tr->depth_keys_alt, tr->depth_values_alt, tr->depth_scratch,
-                       tr->counts_sorted, tr->keys64, tr->work})
+                       tr->counts_sorted, tr->keys64, tr->work, tr->work_plan, tr->chunks, tr->checkpoints})
     free_buffer(b);
   if (tr->readback_event) {
     cudaEventSynchronize(tr->readback_event);

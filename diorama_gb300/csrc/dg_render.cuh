@@ -45,7 +45,12 @@ struct dg_tile_rasterizer {
   dg_buffer* depth_scratch;
   dg_buffer* counts_sorted;  // tile counts in depth order, then their scan
   dg_buffer* keys64;         // the reference's 64-bit sorted keys, rebuilt on request
-  dg_buffer* work;           // item counters of the blend kernels (forward, backward)
+  dg_buffer* work;           // item counters of the blend kernels
+  // The blend kernels' work plan (plan_kernel, dg_render.cu): tile order, the
+  // backward's (tile, chunk) pairs and the forward's per-chunk pixel states.
+  dg_buffer* work_plan;
+  dg_buffer* chunks;
+  dg_buffer* checkpoints;
 };
 
 namespace dg {
@@ -60,8 +65,8 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
                             uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);
 dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity);
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
-// Grid of a persistent blend kernel (256 threads per CTA).
-uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel);
+// Grid of a persistent blend kernel.
+uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel, uint32_t threads);
 dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr);
 }  // namespace dg
 

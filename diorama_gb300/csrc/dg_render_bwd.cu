@@ -18,164 +18,254 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
   for (int k = threadIdx.x; k < 36; k += blockDim.x) d[k] = s[k];
 }
 
-// Sums 9 values over the warp with 12 shuffles instead of 45. Each halving step
-// swaps half of a lane's values with its partner's, so the set a lane holds
-// halves each time: values 0-4 / 5-8 at distance 16, then 3 / 2 of those at 8,
-// 2 / 1 at 4, 1 / 1 at 2, and a plain add at 1. Afterwards the lanes 2p and
-// 2p+1 of pair p hold the total of value reduce9_slot(2p), or padding when that is -1.
-__device__ __forceinline__ float warp_reduce9(const float v[9], int lane) {
-  float w[5];
-  {
-    const bool upper = lane & 16;
+// One halving step of a reduce-scatter over the warp: a lane holding M partial
+// sums keeps the lower or the upper half of them (by bit D of its lane index) and
+// adds its partner's copy of that half. With M == 1 both lanes keep the sum.
+template <int M, int D>
+__device__ __forceinline__ void reduce_half(float* v, uint32_t lane) {
+  if constexpr (M == 1) {
+    v[0] = v[0] + __shfl_xor_sync(0xffffffffu, v[0], D);
+  } else {
+    constexpr int H = (M + 1) / 2;
+    const bool upper = lane & D;
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-      const float lo = v[k], hi = k < 4 ? v[5 + k] : 0.0f;
-      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 16);
-      w[k] = (upper ? hi : lo) + got;
+    for (int k = 0; k < H; k++) {
+      const float lo = v[k], hi = H + k < M ? v[H + k] : 0.0f;
+      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, D);
+      v[k] = (upper ? hi : lo) + got;
     }
   }
-  float x[3];
-  {
-    const bool upper = lane & 8;
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const float lo = w[k], hi = k < 2 ? w[3 + k] : 0.0f;
-      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 8);
-      x[k] = (upper ? hi : lo) + got;
-    }
-  }
-  float y[2];
-  {
-    const bool upper = lane & 4;
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-      const float lo = x[k], hi = k < 1 ? x[2] : 0.0f;
-      const float got = __shfl_xor_sync(0xffffffffu, upper ? lo : hi, 4);
-      y[k] = (upper ? hi : lo) + got;
-    }
-  }
-  const bool upper = lane & 2;
-  const float z = (upper ? y[1] : y[0]) + __shfl_xor_sync(0xffffffffu, upper ? y[0] : y[1], 2);
-  return z + __shfl_xor_sync(0xffffffffu, z, 1);
 }
 
-// Which value lane pair p = lane >> 1 ends up holding (bits of p: 16-, 8-, 4-, 2-lane
-// halves), packed 4 bits per pair with 15 meaning padding. Each lane extracts its
-// entry once; an indexed constant-memory table would serialize across the warp.
-__device__ __forceinline__ int reduce9_slot(int lane) {
-  const uint64_t table = 0xFFF8F765FF43F210ull;  // nibble p = slot of pair p (0xF: padding)
-  const int slot = (int)((table >> (4 * (lane >> 1))) & 0xFull);
-  return slot == 15 ? -1 : slot;
+// Sums N <= 32 values over the warp's 32 lanes with about N shuffles (N = 18:
+// 20 shuffles in 5 dependent steps, against 5 N in 5 N steps for N separate
+// butterflies). Afterwards lane l holds the total of value reduce_slot<N>(l), or
+// a copy or padding where that is -1. Clobbers v.
+template <int N>
+__device__ __forceinline__ float warp_reduce_scatter(float (&v)[N], uint32_t lane) {
+  static_assert(N <= 32, "one value per lane at most");
+  constexpr int M2 = (N + 1) / 2, M3 = (M2 + 1) / 2, M4 = (M3 + 1) / 2, M5 = (M4 + 1) / 2;
+  static_assert(M5 == 1 || (M5 == 2 && N > 16), "the last step leaves one value per lane");
+  reduce_half<N, 16>(v, lane);
+  reduce_half<M2, 8>(v, lane);
+  reduce_half<M3, 4>(v, lane);
+  reduce_half<M4, 2>(v, lane);
+  reduce_half<M5, 1>(v, lane);
+  return v[0];
 }
 
-// src/shaders/rasterizeBackward.wgsl:50-163. Like the forward pass, the work is
-// split into independent items, one per (tile, 8x4 pixel block), taken by
-// persistent warps from a counter, so no warp waits for another. For an item, the
-// warp walks the tile's list back to front from the largest `last` among its
-// pixels, staging 32 entries at a time into its own slice of shared memory and
-// keeping only splats that can reach its block; each pixel recovers the
-// transmittance in front of each splat by dividing the final one by (1 - alpha).
-// A splat's 9 gradient shares are summed over the warp's 32 pixels with shuffles
-// and added to its global gradient, one atomic add per nonzero value.
-__global__ void __launch_bounds__(256) rasterize_backward_kernel(
+// Which of the N values lane `lane` holds after warp_reduce_scatter<N>: the index
+// ranges each step keeps, followed for this lane's bits; -1 for padding or for the
+// upper lane of a pair that holds the same sum.
+template <int N>
+__device__ __forceinline__ int reduce_slot(uint32_t lane) {
+  int base = 0, real = N, m = N;
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    if (m == 1) {
+      if (lane & d) real = 0;
+      continue;
+    }
+    const int h = (m + 1) / 2;
+    if (lane & d) {
+      base += h;
+      real = real > h ? real - h : 0;
+    } else {
+      real = real < h ? real : h;
+    }
+    m = h;
+  }
+  return real > 0 ? base : -1;
+}
+
+// The exponent, Gaussian and alpha of a splat at this lane's pixel, and whether
+// the forward pass blended it there (the same decisions, made with the same
+// non-fusing arithmetic).
+struct BlendTerm {
+  float dx, dy, G, alpha;
+  bool blended;
+};
+
+__device__ __forceinline__ BlendTerm blend_term(const WarpStage& st, uint32_t e, bool eligible, float cx, float cy) {
+  BlendTerm t;
+  const float2 m = st.mean[e];
+  const float4 q = st.quad[e];
+  t.dx = cx - m.x;
+  t.dy = cy - m.y;
+  const float power = blend_power(q.x, q.y, q.z, t.dx, t.dy);
+  const bool need = eligible && power >= q.w && power <= 0.0f;
+  t.G = exp_blend(need ? power : 0.0f);
+  t.alpha = fminf(0.99f, __fmul_rn(st.color[e].w, t.G));
+  t.blended = need && t.alpha >= 1.0f / 255.0f;
+  return t;
+}
+
+// A pixel's state on its back-to-front walk: the transmittance in front of the
+// current splat, the colour composited behind it and the last splat passed.
+struct PixelBackward {
+  float Tf, T, pgx, pgy, pgz, bg_grad;
+  float bhx, bhy, bhz;  // colour of everything behind
+  float na, ncx, ncy, ncz;
+
+  // Starts the walk at a point where the transmittance is T0 and the colour
+  // composited behind, relative to T0, is `behind`.
+  __device__ __forceinline__ void begin(float final_T, float T0, float3 behind, float gx, float gy, float gz,
+                                        float4 bg) {
+    Tf = final_T;
+    T = T0;
+    pgx = gx;
+    pgy = gy;
+    pgz = gz;
+    bg_grad = bg.x * gx + bg.y * gy + bg.z * gz;
+    bhx = behind.x;
+    bhy = behind.y;
+    bhz = behind.z;
+    na = ncx = ncy = ncz = 0.0f;
+  }
+
+  // Steps in front of a splat this pixel blended and writes its 9 gradient shares.
+  __device__ __forceinline__ void shares(const BlendTerm& t, float4 q, float4 c, float* w) {
+    const float alpha = t.alpha, G = t.G, dx = t.dx, dy = t.dy;
+    const float inv = __frcp_rn(1.0f - alpha);  // 1 / (1 - alpha), used twice
+    T = T * inv;
+    bhx = na * ncx + (1.0f - na) * bhx;
+    bhy = na * ncy + (1.0f - na) * bhy;
+    bhz = na * ncz + (1.0f - na) * bhz;
+    na = alpha;
+    ncx = c.x;
+    ncy = c.y;
+    ncz = c.z;
+    const float dotv = (c.x - bhx) * pgx + (c.y - bhy) * pgy + (c.z - bhz) * pgz;
+    const float alpha_grad = T * dotv - Tf * inv * bg_grad;
+    const float power_grad = alpha_grad * c.w * G;
+    // The conic is (a, b, c) = (-2A, b, -2C).
+    const float ca = -2.0f * q.x, cb = q.y, cc = -2.0f * q.z;
+    w[0] = power_grad * (ca * dx + cb * dy);
+    w[1] = power_grad * (cb * dx + cc * dy);
+    w[2] = power_grad * (-0.5f * dx * dx);
+    w[3] = power_grad * (-dx * dy);
+    w[4] = power_grad * (-0.5f * dy * dy);
+    w[5] = alpha_grad * G;
+    const float wt = alpha * T;
+    w[6] = wt * pgx;
+    w[7] = wt * pgy;
+    w[8] = wt * pgz;
+  }
+};
+
+// src/shaders/rasterizeBackward.wgsl:50-163. The work is split into independent
+// items, one per (tile, CHUNK-entry chunk of its list, 8x4 pixel block), taken by
+// persistent warps from a counter in the plan's order, so no warp waits for
+// another and a long list is spread over many warps. For an item, the warp walks
+// its chunk back to front from the largest `last` among its pixels, keeping in its
+// own slice of shared memory, 32 entries at a time, only the splats that can reach
+// its block (the records of the next window are copied in meanwhile). Each pixel
+// starts from its state behind the chunk: the transmittance the forward pass saved
+// at the chunk's end, and the colour behind it, (final colour - colour saved) /
+// that transmittance; behind its last splat (the whole list for most tiles) these
+// are the final transmittance and nothing. Splats are then taken two at a time:
+// their alphas are computed together, then each pixel recovers the transmittance
+// in front of each splat by dividing by (1 - alpha), in list order. The 18
+// gradient shares of the pair are summed over the warp's 32 pixels in one
+// reduce-scatter and added to the splats' global gradients, one atomic add per
+// nonzero total.
+__global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
-    const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const float4* __restrict__ pixel_color,
-    const uint32_t* __restrict__ pixel_last, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads,
+    const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
+    const uint2* __restrict__ chunks, const float4* __restrict__ pixel_color, const uint32_t* __restrict__ pixel_last,
+    const float4* __restrict__ checkpoints, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads,
     uint32_t* __restrict__ work_counter) {
-  __shared__ WarpStage stages[8];
-  const int lane = threadIdx.x & 31;
+  __shared__ WarpStage stages[BWD_WARPS];
+  const uint32_t lane = threadIdx.x & 31u;
   WarpStage& st = stages[threadIdx.x >> 5];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE, tiles_y = ((uint32_t)vpy + TILE - 1u) / TILE;
-  const uint32_t items = tiles_x * tiles_y * 8u;
+  const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
+  const uint32_t items = plan[2] * 8u;
   const float4 bg = raster_params[0];
-  // The even lane of each pair adds the value its pair holds after the reduction.
-  const int my_slot = (lane & 1) ? -1 : reduce9_slot(lane);
+  const int my_slot = reduce_slot<2 * SPLAT_GRADS>(lane);
+  // Value my_slot belongs to the pair's first (further back) splat when below 9.
+  const uint32_t my_entry = my_slot >= (int)SPLAT_GRADS ? 1u : 0u;
+  const uint32_t my_grad = my_slot >= 0 ? (uint32_t)my_slot - my_entry * SPLAT_GRADS : 0u;
   while (true) {
     uint32_t item = 0;
     if (lane == 0) item = atomicAdd(work_counter, 1u);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= items) break;
-    const uint32_t tile = item >> 3, block = item & 7u;
+    const uint2 chunk = chunks[item >> 3];
+    const uint32_t tile = chunk.x, block = item & 7u;
     const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
     const uint32_t px = bx + (lane & 7u), py = by + (lane >> 3);
     const bool inside = (float)px < vpx && (float)py < vpy;
     const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
     const float x0 = (float)bx + 0.5f, y0 = (float)by + 0.5f;
     const uint2 run = ranges[tile];
-    float Tf = 0.0f, pgx = 0.0f, pgy = 0.0f, pgz = 0.0f;
+    const uint32_t chunk_lo = run.x + chunk.y * CHUNK, chunk_hi = min(chunk_lo + CHUNK, run.y);
+    const uint32_t boundary = (chunk.y + 1u) * CHUNK;  // the chunk's end, relative to run.x
+    float4 color = make_float4(0.f, 0.f, 0.f, 0.f), pg = color;
     uint32_t last = 0;
     if (inside) {
       const uint32_t p = py * (uint32_t)vpx + px;
-      Tf = pixel_color[p].w;
+      color = pixel_color[p];
       last = pixel_last[p];
-      const float4 pg = pixel_grads[p];
-      pgx = pg.x;
-      pgy = pg.y;
-      pgz = pg.z;
+      pg = pixel_grads[p];
     }
     // Splats at or past the warp's largest `last` contribute nothing to it.
-    const uint32_t warp_last = __reduce_max_sync(0xffffffffu, last);
-    const float bg_grad = bg.x * pgx + bg.y * pgy + bg.z * pgz;
-    float T = Tf;
-    float bhx = 0.0f, bhy = 0.0f, bhz = 0.0f;  // colour of everything behind
-    float na = 0.0f, ncx = 0.0f, ncy = 0.0f, ncz = 0.0f;
-    for (uint32_t end = run.x + warp_last; end > run.x;) {
-      const uint32_t lo = end - run.x > 32u ? end - 32u : run.x;
-      const uint32_t staged = stage_warp_window(st, splats, pair_splats, run.x, lo, end, x0, y0);
-      for (uint32_t slot = staged; slot > 0; slot--) {
-        const uint32_t j = slot - 1;
-        float v[9];
+    const uint32_t end_all = min(chunk_hi, run.x + __reduce_max_sync(0xffffffffu, last));
+    if (end_all <= chunk_lo) continue;
+    float T0 = color.w;
+    float3 behind = make_float3(0.f, 0.f, 0.f);
+    if (last > boundary) {  // the pixel blends splats behind this chunk
+      const float4 ck = checkpoints[checkpoint_at(run.x, chunk.y + 1u, block, lane)];
+      const float inv = 1.0f / ck.x;
+      T0 = ck.x;
+      behind = make_float3((color.x - color.w * bg.x - ck.y) * inv, (color.y - color.w * bg.y - ck.z) * inv,
+                           (color.z - color.w * bg.z - ck.w) * inv);
+    }
+    PixelBackward px_state;
+    px_state.begin(color.w, T0, behind, pg.x, pg.y, pg.z, bg);
+    // Windows run back to front: [lo, end) with lo = max(chunk_lo, end - 32).
+    uint32_t end = end_all;
+    uint32_t index = 0, next_index = 0;
+    {
+      const uint32_t lo = end - chunk_lo > 32u ? end - 32u : chunk_lo;
+      const uint32_t k = lo + lane;
+      if (k < end) index = pair_splats[k];
+      stage_issue(st, splats, index, k < end);
+      const uint32_t lo2 = lo - chunk_lo > 32u ? lo - 32u : chunk_lo;
+      if (lo2 + lane < lo) next_index = pair_splats[lo2 + lane];
+    }
+    while (end > chunk_lo) {
+      const uint32_t lo = end - chunk_lo > 32u ? end - 32u : chunk_lo;
+      const uint32_t staged = stage_commit(st, run.x, lo, end, index, x0, y0);
+      {
+        const uint32_t lo2 = lo - chunk_lo > 32u ? lo - 32u : chunk_lo;
+        stage_issue(st, splats, next_index, lo2 + lane < lo);
+        index = next_index;
+        const uint32_t lo3 = lo2 - chunk_lo > 32u ? lo2 - 32u : chunk_lo;
+        next_index = lo3 + lane < lo2 ? pair_splats[lo3 + lane] : 0u;
+      }
+      for (uint32_t slot = staged; slot > 0;) {
+        // Entries j0 (further back, taken first) and j1 = j0 - 1 when there is one.
+        const uint32_t j0 = slot - 1, j1 = slot >= 2 ? slot - 2 : j0;
+        const bool pair = slot >= 2;
+        slot = pair ? slot - 2 : 0;
+        const BlendTerm t0 = blend_term(st, j0, inside && st.pos[j0] < last, cx, cy);
+        const BlendTerm t1 = blend_term(st, j1, pair && inside && st.pos[j1] < last, cx, cy);
+        if (!__any_sync(0xffffffffu, t0.blended || t1.blended)) continue;
+        float v[2 * SPLAT_GRADS];
 #pragma unroll
-        for (int q = 0; q < 9; q++) v[q] = 0.0f;
-        bool contributes = false;
-        if (inside && st.pos[j] < last) {
-          const float2 m = st.mean[j];
-          const float4 q = st.quad[j];
-          const float dx = cx - m.x, dy = cy - m.y;
-          const float power = blend_power(q.x, q.y, q.z, dx, dy);
-          if (power >= q.w && power <= 0.0f) {
-            const float4 c = st.color[j];
-            const float G = exp_blend(power);
-            const float alpha = fminf(0.99f, __fmul_rn(c.w, G));
-            if (alpha >= 1.0f / 255.0f) {
-              contributes = true;
-              const float inv = __frcp_rn(1.0f - alpha);  // 1 / (1 - alpha), used twice
-              T = T * inv;
-              bhx = na * ncx + (1.0f - na) * bhx;
-              bhy = na * ncy + (1.0f - na) * bhy;
-              bhz = na * ncz + (1.0f - na) * bhz;
-              na = alpha;
-              ncx = c.x;
-              ncy = c.y;
-              ncz = c.z;
-              const float dotv = (c.x - bhx) * pgx + (c.y - bhy) * pgy + (c.z - bhz) * pgz;
-              const float alpha_grad = T * dotv - Tf * inv * bg_grad;
-              const float power_grad = alpha_grad * c.w * G;
-              // The conic is (a, b, c) = (-2A, b, -2C).
-              const float ca = -2.0f * q.x, cb = q.y, cc = -2.0f * q.z;
-              v[0] = power_grad * (ca * dx + cb * dy);
-              v[1] = power_grad * (cb * dx + cc * dy);
-              v[2] = power_grad * (-0.5f * dx * dx);
-              v[3] = power_grad * (-dx * dy);
-              v[4] = power_grad * (-0.5f * dy * dy);
-              v[5] = alpha_grad * G;
-              const float w = alpha * T;
-              v[6] = w * pgx;
-              v[7] = w * pgy;
-              v[8] = w * pgz;
-            }
-          }
-        }
-        if (__any_sync(0xffffffffu, contributes)) {
-          const float total = warp_reduce9(v, lane);
-          if (my_slot >= 0 && total != 0.0f)
-            atomicAdd(&splat_grads[(size_t)st.index[j] * SPLAT_GRADS + my_slot], total);
-        }
+        for (int q = 0; q < 2 * (int)SPLAT_GRADS; q++) v[q] = 0.0f;
+        // Back to front: j0, then j1.
+        if (t0.blended) px_state.shares(t0, st.quad[j0], st.color[j0], v);
+        if (t1.blended) px_state.shares(t1, st.quad[j1], st.color[j1], v + SPLAT_GRADS);
+        const float total = warp_reduce_scatter(v, lane);
+        if (my_slot >= 0 && total != 0.0f && (my_entry == 0 || pair))
+          atomicAdd(&splat_grads[(size_t)st.index[my_entry ? j1 : j0] * SPLAT_GRADS + my_grad], total);
       }
       __syncwarp();
       end = lo;
     }
+    cp_async_wait_all();
   }
 }
 
@@ -399,13 +489,15 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(
 
 dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads) {
   dg_context* ctx = tr->ctx;
-  uint32_t* counter = typed<uint32_t>(tr->work) + 1;
+  uint32_t* counter = typed<uint32_t>(tr->work) + 2;
   DG_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), ctx->stream));
   DG_LAUNCH(ctx, "rasterize_backward",
-            rasterize_backward_kernel<<<blend_grid(tr, (const void*)rasterize_backward_kernel), 256, 0, ctx->stream>>>(
+            rasterize_backward_kernel<<<blend_grid(tr, (const void*)rasterize_backward_kernel, BWD_THREADS),
+                                        BWD_THREADS, 0, ctx->stream>>>(
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
-                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last), typed<float4>(pixel_grads), typed<float>(splat_grads), counter));
+                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
+                typed<uint2>(tr->chunks), typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last),
+                typed<float4>(tr->checkpoints), typed<float4>(pixel_grads), typed<float>(splat_grads), counter));
   return DG_OK;
 }
 

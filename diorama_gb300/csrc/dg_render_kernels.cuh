@@ -239,38 +239,82 @@ __device__ __forceinline__ bool rect_reachable(float A, float b, float C, float 
   return qmax + 1e-6f * terms + 1e-6f >= cut;
 }
 
-// The pixel blocks of a 16x16 tile: warp w covers the 8x4 block at
-// (8 * (w & 1), 4 * (w >> 1)); lane l is pixel (l & 7, l >> 3) of it.
-__device__ __forceinline__ uint32_t tile_pixel_x(uint32_t tid) { return ((tid >> 5) & 1u) * 8u + (tid & 7u); }
-__device__ __forceinline__ uint32_t tile_pixel_y(uint32_t tid) { return (tid >> 6) * 4u + ((tid >> 3) & 3u); }
+// CTA sizes of the blend kernels. The forward's 8 warps blend a long tile list
+// together; otherwise every warp takes items of its own.
+constexpr uint32_t FWD_THREADS = 128;
+constexpr uint32_t FWD_WARPS = FWD_THREADS / 32;
+constexpr uint32_t BWD_THREADS = 128;
+constexpr uint32_t BWD_WARPS = BWD_THREADS / 32;
+// The backward pass walks a tile's list in chunks of CHUNK entries, each starting
+// from the state the forward pass saved at the chunk's end (a checkpoint per
+// CHUNK entries). A multiple of the 32-entry window.
+constexpr uint32_t CHUNK = 512;
+// Tiles with more entries than this are blended by a whole CTA in the forward pass.
+constexpr uint32_t COOP_MIN = 512;
+// The frame's work plan (dg_render.cu, plan_kernel): a header of PLAN_HEADER
+// words (cooperative tiles, tiles, backward chunks, spare), the tiles in the
+// order the forward pass takes them, then the backward's (tile, chunk) pairs.
+constexpr uint32_t PLAN_HEADER = 4;
 
 // A warp's own window of up to 32 list entries, staged in its slice of shared
-// memory: only the splats that can reach the warp's 8x4 pixel block, in list order.
+// memory: only the splats that can reach the warp's 8x4 pixel block, in list
+// order. `raw` receives the splat records of the next window by cp.async while
+// the current one blends.
 struct WarpStage {
   float2 mean[32];
   float4 quad[32];   // A = -0.5 a, b, C = -0.5 c, cutoff
   float4 color[32];  // rgb, opacity
   uint32_t pos[32];  // position in the tile's list
   uint32_t index[32];
+  float4 raw[32][3];  // lane l: the 48-byte record of its entry of the window in flight
+  uint8_t live[32];   // cooperative blending: the kept entries some pixel blends
+  uint32_t live_count;
 };
 
-// Stages list entries [lo, min(lo + 32, hi)) for the calling warp, whose pixel
-// centers span [x0, x0 + 7] x [y0, y0 + 3]; returns how many were kept. All 32
-// lanes must call it.
-__device__ __forceinline__ uint32_t stage_warp_window(WarpStage& st, const float* __restrict__ splats,
-                                                      const uint32_t* __restrict__ pair_splats, uint32_t run_x,
-                                                      uint32_t lo, uint32_t hi, float x0, float y0) {
+// A pixel's state at the start of chunk boundary k of a tile (after every entry
+// before position k * CHUNK): transmittance and the colour blended so far. One
+// slot of 8 blocks x 32 pixels per CHUNK entries of the pair list; boundary k of
+// the tile whose list starts at run_x has slot (run_x + k * CHUNK) / CHUNK, which
+// no other boundary of any tile shares.
+__device__ __forceinline__ size_t checkpoint_at(uint32_t run_x, uint32_t k, uint32_t block, uint32_t lane) {
+  const size_t slot = (run_x + k * CHUNK) / CHUNK;
+  return (slot * 8u + block) * 32u + lane;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Starts copying the splat record of this lane's entry of a window into `raw`.
+__device__ __forceinline__ void stage_issue(WarpStage& st, const float* __restrict__ splats, uint32_t index,
+                                            bool valid) {
+  if (valid) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
+    cp_async16(&st.raw[lane][0], s);
+    cp_async16(&st.raw[lane][1], s + 1);
+    cp_async16(&st.raw[lane][2], s + 2);
+  }
+}
+
+// Waits for the window [lo, min(lo + 32, hi)) issued by stage_issue (lane l holds
+// entry lo + l, splat `index`) and keeps, in list order, the splats that can reach
+// the warp's block, whose pixel centers span [x0, x0 + 7] x [y0, y0 + 3]. Returns
+// how many were kept. All 32 lanes must call it. Every value read from `raw` is
+// consumed before this returns, so the caller may issue the next window at once.
+__device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, uint32_t lo, uint32_t hi,
+                                                 uint32_t index, float x0, float y0) {
+  cp_async_wait_all();
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t k = lo + lane;
   bool keep = false;
   float2 mean = make_float2(0.f, 0.f);
   float4 quad = make_float4(0.f, 0.f, 0.f, 0.f), color = quad;
-  uint32_t index = 0;
   if (k < hi) {
-    index = pair_splats[k];
-    const float4* s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT);
-    const float4 s0 = s[0], s1 = s[1];
-    color = s[2];
+    const float4 s0 = st.raw[lane][0], s1 = st.raw[lane][1];
+    color = st.raw[lane][2];
     mean = make_float2(s0.x, s0.y);
     const float A = -0.5f * s1.x, b = s1.y, C = -0.5f * s1.z;
     const float cut = blend_cutoff(color.w);
