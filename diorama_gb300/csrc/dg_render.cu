@@ -430,30 +430,53 @@ struct PixelBlend {
 
   // Blends one splat of alpha `alpha` (0: not blended here) and colour c at list
   // position pos; stops before the splat that would take the transmittance
-  // below 1e-4.
-  __device__ __forceinline__ void blend(float alpha, float4 c, uint32_t pos) {
-    if (alpha == 0.0f || done) return;
+  // below 1e-4. Returns whether the pixel blended it.
+  __device__ __forceinline__ bool blend(float alpha, float4 c, uint32_t pos) {
+    if (alpha == 0.0f || done) return false;
     const float remaining = T * (1.0f - alpha);
     if (remaining < 0.0001f) {
       done = true;
-      return;
+      return false;
     }
     r = r + c.x * alpha * T;
     g = g + c.y * alpha * T;
     b = b + c.z * alpha * T;
     T = remaining;
     last = pos + 1;
+    return true;
   }
 
-  // Applies up to 4 staged entries e[0..n) of `st` in list order.
-  __device__ __forceinline__ void apply4(const WarpStage& st, const uint32_t (&e)[4], uint32_t n) {
+  // Applies up to 4 staged entries e[0..n) of `st` in list order. Sets bit
+  // (position - base) of `blended` for each entry with a nonzero alpha at some
+  // pixel of the warp that had not stopped: every entry a pixel blends, and at
+  // most a last one it stopped at.
+  __device__ __forceinline__ void apply4(const WarpStage& st, const uint32_t (&e)[4], uint32_t n, uint32_t base,
+                                         uint32_t& blended) {
     float alpha[4];
     if (!alphas4(st, e, n, !done, alpha)) return;
+    const uint32_t mine = (alpha[0] != 0.0f ? 1u : 0u) | (alpha[1] != 0.0f ? 2u : 0u) |
+                          (alpha[2] != 0.0f ? 4u : 0u) | (alpha[3] != 0.0f ? 8u : 0u);
+    const uint32_t any = __reduce_or_sync(0xffffffffu, mine);
 #pragma unroll
-    for (uint32_t u = 0; u < 4; u++)
+    for (uint32_t u = 0; u < 4; u++) {
+      if ((any >> u) & 1u) blended |= 1u << (st.pos[e[u]] - base);
       if (alpha[u] != 0.0f) blend(alpha[u], st.color[e[u]], st.pos[e[u]]);
+    }
   }
 };
+
+// The blend mask: bit p % 32 of word (p / 32) * 8 + block is set when some pixel
+// of 8x4 block `block` of the tile holding pair p blended that pair's splat. The
+// forward pass sets the bits, the backward pass walks only those entries. Both
+// helpers take the 32 bits of positions [p0, p0 + 32) of the pair list.
+__device__ __forceinline__ void publish_blended(uint32_t* __restrict__ mask, uint32_t p0, uint32_t block,
+                                                uint32_t bits) {
+  if (bits == 0) return;
+  const uint32_t w = p0 >> 5, shift = p0 & 31u;
+  const uint32_t lo = bits << shift, hi = shift ? bits >> (32u - shift) : 0u;
+  if (lo) atomicOr(&mask[(size_t)w * 8u + block], lo);
+  if (hi) atomicOr(&mask[(size_t)(w + 1) * 8u + block], hi);
+}
 
 // The geometry of a blend item: tile `tile`, 8x4 block `block`, this lane's pixel.
 struct BlendItem {
@@ -503,15 +526,15 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 // previous one blends, a splat rejected for the block has alpha below 1/255 at
 // all of its pixels, and a power under the splat's cutoff skips the exp: none of
 // these changes a result. The pixel state at each CHUNK boundary of the list is
-// saved for the backward pass.
+// saved for the backward pass, and which entries each block blended.
 __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
     uchar4* __restrict__ target, float4* __restrict__ pixel_color, uint32_t* __restrict__ pixel_last,
-    float4* __restrict__ checkpoints, uint32_t* __restrict__ counters) {
+    float4* __restrict__ checkpoints, uint32_t* __restrict__ blend_mask, uint32_t* __restrict__ counters) {
   __shared__ WarpStage stages[FWD_WARPS];
   __shared__ float s_alpha[FWD_WARPS][32][32];  // cooperative: alphas of each warp's queued entries
-  __shared__ uint32_t s_item, s_stop;
+  __shared__ uint32_t s_item, s_stop, s_done;  // s_done: warp 0's pixels that have stopped
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   WarpStage& st = stages[warp];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
@@ -524,7 +547,10 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
   // Cooperative items: one block of a long tile per CTA.
   while (true) {
     __syncthreads();  // everyone has read the previous s_item
-    if (threadIdx.x == 0) s_item = atomicAdd(&counters[0], 1u);
+    if (threadIdx.x == 0) {
+      s_item = atomicAdd(&counters[0], 1u);
+      s_done = 0;
+    }
     __syncthreads();
     const uint32_t item = s_item;
     if (item >= cooperative * 8u) break;
@@ -553,22 +579,28 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
           next_index = k + 32u * FWD_WARPS < run.y ? pair_splats[k + 32u * FWD_WARPS] : 0u;
         }
         // The alphas of the kept entries at the block's pixels; entries no pixel
-        // blends are dropped, the others queued with their alphas for warp 0.
-        uint32_t live = 0;
+        // blends are dropped, the others queued with their alphas for warp 0 and
+        // marked in the blend mask (pixels warp 0 had stopped by the last round
+        // take no part).
+        uint32_t live = 0, blended = 0;
         for (uint32_t j = 0; j < staged; j += 4) {
           const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
           float alpha[4];
-          if (!pb.alphas4(st, e, staged - j, it.inside, alpha)) continue;
+          if (!pb.alphas4(st, e, staged - j, it.inside && !((s_done >> lane) & 1u), alpha)) continue;
 #pragma unroll
           for (uint32_t u = 0; u < 4; u++) {
             if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
               if (lane == 0) st.live[live] = (uint8_t)(j + u);
               s_alpha[warp][live][lane] = alpha[u];
+              blended |= 1u << (st.pos[j + u] - (start - run.x));
               live++;
             }
           }
         }
-        if (lane == 0) st.live_count = live;
+        if (lane == 0) {
+          st.live_count = live;
+          publish_blended(blend_mask, start, block, blended);
+        }
       } else if (lane == 0) {
         st.live_count = 0;
       }
@@ -589,8 +621,11 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
             pb.blend(s_alpha[w][m][lane], sw.color[e], sw.pos[e]);
           }
         }
-        const bool stop = __all_sync(0xffffffffu, pb.done);
-        if (lane == 0) s_stop = stop;
+        const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
+        if (lane == 0) {
+          s_stop = done == 0xffffffffu;
+          s_done = done;
+        }
       }
       __syncthreads();
       if (s_stop) break;
@@ -634,11 +669,13 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
         index = next_index;
         next_index = k + 32u < run.y ? pair_splats[k + 32u] : 0u;
       }
+      uint32_t blended = 0;
       for (uint32_t j = 0; j < staged; j += 4) {
         if (__all_sync(0xffffffffu, pb.done)) break;
         const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
-        pb.apply4(st, e, staged - j);
+        pb.apply4(st, e, staged - j, start - run.x, blended);
       }
+      if (lane == 0) publish_blended(blend_mask, start, block, blended);
       __syncwarp();
     }
     cp_async_wait_all();  // a window may still be in flight after an early stop
@@ -812,6 +849,7 @@ dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   dg_context* ctx = tr->ctx;
   const uint32_t tiles = tr->tiles_x * tr->tiles_y;
   DG_CUDA(cudaMemsetAsync(tr->work->ptr, 0, 16, ctx->stream));
+  DG_CUDA(cudaMemsetAsync(tr->blend_mask->ptr, 0, tr->blend_mask->bytes, ctx->stream));
   DG_LAUNCH(ctx, "plan",
             plan_kernel<<<1, PLAN_THREADS, 0, ctx->stream>>>(typed<uint2>(tr->ranges), tiles, typed<uint32_t>(tr->work_plan),
                                                              typed<uint2>(tr->chunks)));
@@ -821,7 +859,8 @@ dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
                 target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last), typed<float4>(tr->checkpoints), typed<uint32_t>(tr->work)));
+                typed<uint32_t>(tr->pixel_last), typed<float4>(tr->checkpoints), typed<uint32_t>(tr->blend_mask),
+                typed<uint32_t>(tr->work)));
   return DG_OK;
 }
 
@@ -847,7 +886,8 @@ static dg_status ensure_plan(dg_tile_rasterizer* tr) {
     size_t bytes;
   } needs[] = {{&tr->work_plan, (PLAN_HEADER + tiles) * 4},
                {&tr->chunks, (tiles + slots) * 8},
-               {&tr->checkpoints, slots * 8 * 32 * 16}};
+               {&tr->checkpoints, slots * 8 * 32 * 16},
+               {&tr->blend_mask, ((size_t)tr->pair_capacity / 32 + 2) * 8 * 4}};
   for (const Need& n : needs) {
     if (*n.buf && (*n.buf)->bytes >= n.bytes) continue;
     free_buffer(*n.buf);
@@ -1029,7 +1069,8 @@ dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
   for (dg_buffer* b : {tr->tile_offsets, tr->scan_total, tr->scan_scratch, tr->raster_params, tr->keys, tr->values,
                        tr->keys_alt, tr->values_alt, tr->sort_scratch, tr->ranges, tr->pixel_color, tr->pixel_last,
                        tr->depth_keys, tr->depth_values, tr->depth_keys_alt, tr->depth_values_alt, tr->depth_scratch,
-                       tr->counts_sorted, tr->keys64, tr->work, tr->work_plan, tr->chunks, tr->checkpoints})
+                       tr->counts_sorted, tr->keys64, tr->work, tr->work_plan, tr->chunks, tr->checkpoints,
+                       tr->blend_mask})
     free_buffer(b);
   if (tr->readback_event) {
     cudaEventSynchronize(tr->readback_event);

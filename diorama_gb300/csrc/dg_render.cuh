@@ -51,6 +51,7 @@ struct dg_tile_rasterizer {
   dg_buffer* work_plan;
   dg_buffer* chunks;
   dg_buffer* checkpoints;
+  dg_buffer* blend_mask;  // which entries each 8x4 block blended (dg_render.cu, publish_blended)
 };
 
 namespace dg {

@@ -153,13 +153,27 @@ struct PixelBackward {
   }
 };
 
+// The start of the back-to-front window that ends at `end`: max(floor, end - 32).
+__device__ __forceinline__ uint32_t window_start(uint32_t end, uint32_t floor) {
+  return end - floor > 32u ? end - 32u : floor;
+}
+
+// The blend mask bits of window [lo, hi) for `block` (none when the window is empty).
+__device__ __forceinline__ uint32_t window_blended(const uint32_t* __restrict__ mask, uint32_t lo, uint32_t hi,
+                                                   uint32_t block) {
+  if (hi <= lo) return 0u;
+  const uint32_t bits = read_blended(mask, lo, block);
+  return hi - lo >= 32u ? bits : bits & ((1u << (hi - lo)) - 1u);
+}
+
 // src/shaders/rasterizeBackward.wgsl:50-163. The work is split into independent
 // items, one per (tile, CHUNK-entry chunk of its list, 8x4 pixel block), taken by
 // persistent warps from a counter in the plan's order, so no warp waits for
 // another and a long list is spread over many warps. For an item, the warp walks
 // its chunk back to front from the largest `last` among its pixels, keeping in its
-// own slice of shared memory, 32 entries at a time, only the splats that can reach
-// its block (the records of the next window are copied in meanwhile). Each pixel
+// own slice of shared memory, 32 entries at a time, only the splats some pixel of
+// its block blended in the forward pass (the forward's blend mask; the records of
+// the next window are copied in meanwhile). Each pixel
 // starts from its state behind the chunk: the transmittance the forward pass saved
 // at the chunk's end, and the colour behind it, (final colour - colour saved) /
 // that transmittance; behind its last splat (the whole list for most tiles) these
@@ -173,8 +187,8 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
     const uint2* __restrict__ chunks, const float4* __restrict__ pixel_color, const uint32_t* __restrict__ pixel_last,
-    const float4* __restrict__ checkpoints, const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads,
-    uint32_t* __restrict__ work_counter) {
+    const float4* __restrict__ checkpoints, const uint32_t* __restrict__ blend_mask,
+    const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads, uint32_t* __restrict__ work_counter) {
   __shared__ WarpStage stages[BWD_WARPS];
   const uint32_t lane = threadIdx.x & 31u;
   WarpStage& st = stages[threadIdx.x >> 5];
@@ -197,7 +211,6 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     const uint32_t px = bx + (lane & 7u), py = by + (lane >> 3);
     const bool inside = (float)px < vpx && (float)py < vpy;
     const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-    const float x0 = (float)bx + 0.5f, y0 = (float)by + 0.5f;
     const uint2 run = ranges[tile];
     const uint32_t chunk_lo = run.x + chunk.y * CHUNK, chunk_hi = min(chunk_lo + CHUNK, run.y);
     const uint32_t boundary = (chunk.y + 1u) * CHUNK;  // the chunk's end, relative to run.x
@@ -223,26 +236,28 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     }
     PixelBackward px_state;
     px_state.begin(color.w, T0, behind, pg.x, pg.y, pg.z, bg);
-    // Windows run back to front: [lo, end) with lo = max(chunk_lo, end - 32).
+    // Windows run back to front: [lo, end) with lo = max(chunk_lo, end - 32). Only
+    // the entries some pixel of the block blended (the forward pass's mask) are
+    // staged. This lane's entry of the window in flight and of the next one.
     uint32_t end = end_all;
-    uint32_t index = 0, next_index = 0;
-    {
-      const uint32_t lo = end - chunk_lo > 32u ? end - 32u : chunk_lo;
-      const uint32_t k = lo + lane;
-      if (k < end) index = pair_splats[k];
-      stage_issue(st, splats, index, k < end);
-      const uint32_t lo2 = lo - chunk_lo > 32u ? lo - 32u : chunk_lo;
-      if (lo2 + lane < lo) next_index = pair_splats[lo2 + lane];
-    }
+    uint32_t lo = window_start(end, chunk_lo);
+    uint32_t bits = window_blended(blend_mask, lo, end, block);
+    uint32_t index = (bits >> lane) & 1u ? pair_splats[lo + lane] : 0u;
+    stage_issue(st, splats, index, (bits >> lane) & 1u);
+    uint32_t next_lo = window_start(lo, chunk_lo);
+    uint32_t next_bits = window_blended(blend_mask, next_lo, lo, block);
+    uint32_t next_index = (next_bits >> lane) & 1u ? pair_splats[next_lo + lane] : 0u;
     while (end > chunk_lo) {
-      const uint32_t lo = end - chunk_lo > 32u ? end - 32u : chunk_lo;
-      const uint32_t staged = stage_commit(st, run.x, lo, end, index, x0, y0);
+      const uint32_t staged = stage_commit_blended(st, run.x, lo, index, bits);
       {
-        const uint32_t lo2 = lo - chunk_lo > 32u ? lo - 32u : chunk_lo;
-        stage_issue(st, splats, next_index, lo2 + lane < lo);
+        stage_issue(st, splats, next_index, (next_bits >> lane) & 1u);
+        end = lo;
+        lo = next_lo;
+        bits = next_bits;
         index = next_index;
-        const uint32_t lo3 = lo2 - chunk_lo > 32u ? lo2 - 32u : chunk_lo;
-        next_index = lo3 + lane < lo2 ? pair_splats[lo3 + lane] : 0u;
+        next_lo = window_start(lo, chunk_lo);
+        next_bits = window_blended(blend_mask, next_lo, lo, block);
+        next_index = (next_bits >> lane) & 1u ? pair_splats[next_lo + lane] : 0u;
       }
       for (uint32_t slot = staged; slot > 0;) {
         // Entries j0 (further back, taken first) and j1 = j0 - 1 when there is one.
@@ -263,36 +278,41 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
           atomicAdd(&splat_grads[(size_t)st.index[my_entry ? j1 : j0] * SPLAT_GRADS + my_grad], total);
       }
       __syncwarp();
-      end = lo;
     }
     cp_async_wait_all();
   }
 }
 
-// src/shaders/preprocessBackward.wgsl:28-181: one thread per Gaussian. Writes the
-// 16-float Gaussian gradient (slots 7 and 15 zero) and the 45 SH gradients.
-__global__ void __launch_bounds__(128) preprocess_backward_kernel(
-    const Camera* __restrict__ camera, const float* __restrict__ gaussians, const float* __restrict__ sh,
-    uint32_t count, const uint32_t* __restrict__ scene_params, const float* __restrict__ splats,
-    const float* __restrict__ splat_grads, float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
-  __shared__ Camera s_cam;
-  load_camera(s_cam, camera);
-  __syncthreads();
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const Camera& cam = s_cam;
-  const uint32_t degree = scene_params[0];
-  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
-  float* gg = gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN;
-  float* sg = sh_grads + (size_t)i * SH_REST_FLOATS;
+constexpr uint32_t PBWD_THREADS = 128;
+
+// Copies n floats between global and shared memory, 16 bytes at a time where both
+// ends allow it; all threads of the CTA take part.
+__device__ __forceinline__ void copy_floats(float* __restrict__ dst, const float* __restrict__ src, uint32_t n) {
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+    const uint32_t vecs = n / 4;
+    for (uint32_t k = threadIdx.x; k < vecs; k += blockDim.x)
+      reinterpret_cast<float4*>(dst)[k] = reinterpret_cast<const float4*>(src)[k];
+    for (uint32_t k = vecs * 4 + threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+  } else {
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+  }
+}
+
+// src/shaders/preprocessBackward.wgsl:28-181 for one Gaussian: the 16-float
+// Gaussian gradient (slots 7 and 15 zero) to gg, and the 45 SH gradients over
+// its 45 SH coefficients in shv (shared memory).
+__device__ __forceinline__ void preprocess_backward_one(const Camera& cam, uint32_t i, const float* __restrict__ gaussians,
+                                                        float* shv, uint32_t basis_count,
+                                                        const float* __restrict__ splats,
+                                                        const float* __restrict__ splat_grads, float* __restrict__ gg) {
   float out[16];
 #pragma unroll
   for (int k = 0; k < 16; k++) out[k] = 0.0f;
-  bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
+  const bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
   if (!visible) {
 #pragma unroll
     for (int k = 0; k < 4; k++) reinterpret_cast<float4*>(gg)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (uint32_t k = 0; k < SH_REST_FLOATS; k++) sg[k] = 0.0f;
+    for (uint32_t k = 0; k < SH_REST_FLOATS; k++) shv[k] = 0.0f;
     return;
   }
   float grad[9];
@@ -399,7 +419,7 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(
   off[2] = g[2] - campos[2];
   const float dist = normalize3(off, dir);
   sh_basis(dir, basis);
-  const float* coef = sh + (size_t)i * SH_REST_FLOATS;
+  const float* coef = shv;
   float raw_color[3] = {g[12], g[13], g[14]};
   for (uint32_t k = 0; k < basis_count; k++)
 #pragma unroll
@@ -411,18 +431,19 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(
   {
     float bgrad[15][3];
     sh_basis_gradient(dir, bgrad);
+    // Each coefficient is read before its slot of shv takes the gradient.
     for (uint32_t k = 0; k < SH_REST_FLOATS / 3; k++) {
       if (k < basis_count) {
-#pragma unroll
-        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = basis[k] * raw_grad[ch];
         float d = coef[k * 3] * raw_grad[0];
         d = d + coef[k * 3 + 1] * raw_grad[1];
         d = d + coef[k * 3 + 2] * raw_grad[2];
 #pragma unroll
+        for (int ch = 0; ch < 3; ch++) shv[k * 3 + ch] = basis[k] * raw_grad[ch];
+#pragma unroll
         for (int ax = 0; ax < 3; ax++) dgrad[ax] = dgrad[ax] + bgrad[k][ax] * d;
       } else {
 #pragma unroll
-        for (int ch = 0; ch < 3; ch++) sg[k * 3 + ch] = 0.0f;
+        for (int ch = 0; ch < 3; ch++) shv[k * 3 + ch] = 0.0f;
       }
     }
   }
@@ -484,6 +505,30 @@ __global__ void __launch_bounds__(128) preprocess_backward_kernel(
     reinterpret_cast<float4*>(gg)[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
 }
 
+// One thread per Gaussian. The CTA's SH coefficients are staged in shared memory
+// and its SH gradients written back from there, both as contiguous copies (a
+// thread's own 45 floats would otherwise be 180 bytes apart from its neighbour's).
+__global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
+    const Camera* __restrict__ camera, const float* __restrict__ gaussians, const float* __restrict__ sh,
+    uint32_t count, const uint32_t* __restrict__ scene_params, const float* __restrict__ splats,
+    const float* __restrict__ splat_grads, float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
+  __shared__ Camera s_cam;
+  __shared__ __align__(16) float s_sh[PBWD_THREADS * SH_REST_FLOATS];
+  load_camera(s_cam, camera);
+  const uint32_t block_start = blockIdx.x * PBWD_THREADS;
+  const uint32_t here = min(PBWD_THREADS, count - block_start);
+  copy_floats(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  __syncthreads();
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  const uint32_t i = block_start + threadIdx.x;
+  if (i < count)
+    preprocess_backward_one(s_cam, i, gaussians, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count, splats, splat_grads,
+                            gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN);
+  __syncthreads();
+  copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
+}
+
 
 }  // namespace
 
@@ -497,13 +542,14 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
                 typed<uint2>(tr->chunks), typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last),
-                typed<float4>(tr->checkpoints), typed<float4>(pixel_grads), typed<float>(splat_grads), counter));
+                typed<float4>(tr->checkpoints), typed<uint32_t>(tr->blend_mask), typed<float4>(pixel_grads),
+                typed<float>(splat_grads), counter));
   return DG_OK;
 }
 
 dg_status launch_preprocess_backward(dg_renderer* r) {
   DG_LAUNCH(r->ctx, "preprocess_backward",
-            preprocess_backward_kernel<<<ceil_div(r->count, 128), 128, 0, r->ctx->stream>>>(
+            preprocess_backward_kernel<<<ceil_div(r->count, PBWD_THREADS), PBWD_THREADS, 0, r->ctx->stream>>>(
                 typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                 typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats),
                 typed<float>(r->grad_gaussians), typed<float>(r->grad_sh)));

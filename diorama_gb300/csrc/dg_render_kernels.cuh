@@ -335,6 +335,38 @@ __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, 
   return __popc(kept);
 }
 
+// The bits of positions [p0, p0 + 32) of the pair list in the blend mask of
+// 8x4 block `block`: bit p % 32 of word (p / 32) * 8 + block is set when some
+// pixel of the block blended pair p's splat in the forward pass.
+__device__ __forceinline__ uint32_t read_blended(const uint32_t* __restrict__ mask, uint32_t p0, uint32_t block) {
+  const uint32_t w = p0 >> 5, shift = p0 & 31u;
+  const uint32_t lo = mask[(size_t)w * 8u + block];
+  if (!shift) return lo;
+  const uint32_t hi = mask[(size_t)(w + 1) * 8u + block];
+  return (lo >> shift) | (hi << (32u - shift));
+}
+
+// Like stage_commit for a window whose entries the block blended are known:
+// lane l keeps entry lo + l when bit l of `blended` is set (lanes past hi must
+// have it clear), with no rectangle test.
+__device__ __forceinline__ uint32_t stage_commit_blended(WarpStage& st, uint32_t run_x, uint32_t lo, uint32_t index,
+                                                         uint32_t blended) {
+  cp_async_wait_all();
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool keep = (blended >> lane) & 1u;
+  if (keep) {
+    const uint32_t at = __popc(blended & ((1u << lane) - 1u));
+    const float4 s0 = st.raw[lane][0], s1 = st.raw[lane][1], color = st.raw[lane][2];
+    st.mean[at] = make_float2(s0.x, s0.y);
+    st.quad[at] = make_float4(-0.5f * s1.x, s1.y, -0.5f * s1.z, blend_cutoff(color.w));
+    st.color[at] = color;
+    st.pos[at] = lo + lane - run_x;
+    st.index[at] = index;
+  }
+  __syncwarp();
+  return __popc(blended);
+}
+
 // tile_count / tile_rect (src/shaders/common.wgsl:31-42).
 __device__ __forceinline__ uint2 tile_grid(const Camera& cam) {
   return make_uint2(((uint32_t)cam.viewport[0] + TILE - 1u) / TILE, ((uint32_t)cam.viewport[1] + TILE - 1u) / TILE);

@@ -47,8 +47,10 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
 // adam_sh_kernel over the 45 SH coefficients of every Gaussian (moment slots
 // 16-60) and adam_param_kernel over the 16 raw parameters (slots 0-15). Each
 // thread takes one slot, so parameters, gradients and moments are read in
-// consecutive runs and no thread waits on another. Slots 7 and 15 (padding, which
-// holds densification stamps) are left alone.
+// consecutive runs and no thread waits on another. (One kernel over all 61 slots
+// of each moment record measured slower: its warps mix the two paths and seven
+// streams.) Slots 7 and 15 (padding, which holds densification stamps) are left
+// alone.
 //
 // The step uses the host's reciprocals of the bias corrections and approximate
 // square root and division: within a few ulps of
@@ -90,27 +92,25 @@ __global__ void __launch_bounds__(256) adam_param_kernel(const AdamParams* __res
   const size_t slot = (size_t)i * MOMENT_SLOTS + k;
   float2 m = moments[slot];
   const float x = params[e];
-  float grad = ggrad[e];
-  float lr;
-  if (k < 3) {
-    lr = ap->position_lr;
-  } else if (k == 3) {
-    const float opacity = sigmoidf_(x);
-    grad = grad * opacity * (1.0f - opacity);
-    lr = ap->opacity_lr;
-  } else if (k < 7) {
-    grad = grad * expf(x);
-    lr = ap->scale_lr;
-  } else if (k < 12) {
-    lr = ap->rotation_lr;
-  } else {
-    grad = grad * SH_C0;
-    lr = ap->color_lr;
-  }
+  // The chain rule through the activation and the learning rate of slot k,
+  // without branches: the 16 slots of a Gaussian share a warp, and each would
+  // otherwise take its own path. One expf serves the sigmoid (k = 3) and the
+  // exponential (k = 4-6); the values equal the per-slot formulas bit for bit.
+  const bool opacity = k == 3, scale = k >= 4 && k <= 6, color = k >= 12;
+  const float ex = expf(opacity ? -x : x);
+  const float sig = 1.0f / (1.0f + ex);
+  const float g0 = ggrad[e];
+  const float grad = opacity ? g0 * sig * (1.0f - sig) : scale ? g0 * ex : color ? g0 * SH_C0 : g0;
+  const float lr = k < 3 ? ap->position_lr
+                 : opacity ? ap->opacity_lr
+                 : scale ? ap->scale_lr
+                 : color ? ap->color_lr
+                         : ap->rotation_lr;
   const float next = adam_step_fast(x, grad, m, lr, ap->inv_bias_correction1, ap->inv_sqrt_bias_correction2);
   params[e] = next;
   moments[slot] = m;
-  gaussians[e] = activated(k, next);
+  const float ey = expf(opacity ? -next : next);
+  gaussians[e] = opacity ? 1.0f / (1.0f + ey) : scale ? ey : color ? 0.5f + SH_C0 * next : next;
 }
 
 // src/shaders/adam.wgsl:74-77, one thread per raw float.
@@ -585,6 +585,12 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
     free_buffer(counters);
     free_buffer(scratch);
     return fail(DG_ERROR_STATE, "Densification removed every Gaussian.");
+  }
+  if (new_count >= (1u << 26)) {
+    free_buffer(outputs);
+    free_buffer(counters);
+    free_buffer(scratch);
+    return fail(DG_ERROR_STATE, "Densification would exceed 2^26 Gaussians (Adam indexes slots with 32 bits).");
   }
   t->densifications.push_back(
       {t->iteration, count, new_count, readback[2], readback[3], readback[4], readback[1]});
