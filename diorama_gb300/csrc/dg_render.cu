@@ -587,15 +587,30 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
           const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
           float alpha[4];
           if (!pb.alphas4(st, e, staged - j, it.inside && !((s_done >> lane) & 1u), alpha)) continue;
+          float4 color[4];
+          uint32_t pos[4];
+#pragma unroll
+          for (uint32_t u = 0; u < 4; u++) {
+            color[u] = st.color[e[u]];
+            pos[u] = st.pos[e[u]];
+          }
+          __syncwarp();
+          // Queued entries are compacted in place (slot live <= j + u, whose own
+          // entry has been read): colour and position in list order, so warp 0
+          // reads them without going through an index.
 #pragma unroll
           for (uint32_t u = 0; u < 4; u++) {
             if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
-              if (lane == 0) st.live[live] = (uint8_t)(j + u);
+              if (lane == 0) {
+                st.color[live] = color[u];
+                st.pos[live] = pos[u];
+              }
               s_alpha[warp][live][lane] = alpha[u];
-              blended |= 1u << (st.pos[j + u] - (start - run.x));
+              blended |= 1u << (pos[u] - (start - run.x));
               live++;
             }
           }
+          __syncwarp();
         }
         if (lane == 0) {
           st.live_count = live;
@@ -616,10 +631,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
           const WarpStage& sw = stages[w];
           const uint32_t n = sw.live_count;
 #pragma unroll 4
-          for (uint32_t m = 0; m < n; m++) {
-            const uint32_t e = sw.live[m];
-            pb.blend(s_alpha[w][m][lane], sw.color[e], sw.pos[e]);
-          }
+          for (uint32_t m = 0; m < n; m++) pb.blend(s_alpha[w][m][lane], sw.color[m], sw.pos[m]);
         }
         const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
         if (lane == 0) {

@@ -267,8 +267,7 @@ struct WarpStage {
   uint32_t pos[32];  // position in the tile's list
   uint32_t index[32];
   float4 raw[32][3];  // lane l: the 48-byte record of its entry of the window in flight
-  uint8_t live[32];   // cooperative blending: the kept entries some pixel blends
-  uint32_t live_count;
+  uint32_t live_count;  // cooperative blending: entries queued for warp 0
 };
 
 // A pixel's state at the start of chunk boundary k of a tile (after every entry
