@@ -139,6 +139,12 @@ SIGNATURES = {
     "dg_renderer_tiles": (_P, [_P]),
     "dg_renderer_draw_tiles": (_P, [_P]),
     "dg_renderer_destroy": (None, [_P]),
+    "dg_renderer_render_views": (None, [_P, POINTER(Camera), c_uint32, _fp, _P, _P]),
+    "dg_renderer_set_view_batching": (None, [_P, c_uint32, c_uint32, c_int32]),
+    "dg_renderer_view_batching": (None, [_P, POINTER(c_uint32), POINTER(c_uint32)]),
+    "dg_renderer_tune_views": (None, [_P, POINTER(Camera), c_uint32, _fp, _P, POINTER(c_uint32), POINTER(c_uint32),
+                                      POINTER(c_double), POINTER(c_uint32)]),
+    "dg_renderer_views_pixel_last": (c_void_p, [_P]),
     "dg_training_loss_create": (None, [_P, c_uint32, c_uint32, POINTER(_P)]),
     "dg_training_loss_encode": (None, [_P, _P, _P]),
     "dg_training_loss_pixel_grads": (_P, [_P]),

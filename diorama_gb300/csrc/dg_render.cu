@@ -24,61 +24,22 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
 }
 
 // ------------------------------------------------------------------ preprocess
-// One thread per Gaussian: src/shaders/preprocess.wgsl:21-88. The CTA's SH
-// coefficients are staged through shared memory with coalesced loads (45 floats
-// per Gaussian; the odd stride makes the per-thread reads conflict-free). When
-// tile_counts is given, the tiles each splat touches are written too
-// (src/shaders/tiles.wgsl:24-35, fused); when depth_keys is given, the depth's
-// bits (0 when culled) and the splat's index, the input of the depth sort.
-__global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* __restrict__ camera,
-                                                                 const float* __restrict__ gaussians,
-                                                                 const float* __restrict__ sh, uint32_t count,
-                                                                 const uint32_t* __restrict__ scene_params,
-                                                                 float* __restrict__ splats,
-                                                                 uint32_t* __restrict__ tile_counts,
-                                                                 uint32_t* __restrict__ depth_keys,
-                                                                 uint32_t* __restrict__ depth_order) {
-  __shared__ Camera s_cam;
-  __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
-  load_camera(s_cam, camera);
-  const uint32_t degree = scene_params[0];
-  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
-  const uint32_t block_start = blockIdx.x * PRE_THREADS;
-  const uint32_t here = min((uint32_t)PRE_THREADS, count - block_start);
-  if (basis_count > 0) {
-    const float* src = sh + (size_t)block_start * SH_REST_FLOATS;
-    const uint32_t floats = here * SH_REST_FLOATS;
-    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-      const uint32_t vecs = floats / 4;
-      for (uint32_t k = threadIdx.x; k < vecs; k += PRE_THREADS)
-        reinterpret_cast<float4*>(s_sh)[k] = reinterpret_cast<const float4*>(src)[k];
-      for (uint32_t k = vecs * 4 + threadIdx.x; k < floats; k += PRE_THREADS) s_sh[k] = src[k];
-    } else {
-      for (uint32_t k = threadIdx.x; k < floats; k += PRE_THREADS) s_sh[k] = src[k];
-    }
-  }
-  __syncthreads();
-  const uint32_t i = block_start + threadIdx.x;
-  if (i >= count) return;
-  const Camera& cam = s_cam;
-  float g[16];
-  {
-    const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      float4 q = gp[k];
-      g[4 * k] = q.x; g[4 * k + 1] = q.y; g[4 * k + 2] = q.z; g[4 * k + 3] = q.w;
-    }
-  }
-  float4* out = reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT);
+// src/shaders/preprocess.wgsl:21-88 for one Gaussian g (16 activated floats)
+// seen by camera cam, its SH coefficients at shv: writes the 48-byte splat to out
+// (zeros when culled) and returns the tiles it touches
+// (src/shaders/tiles.wgsl:24-35) and its depth's bits (0 when culled).
+struct Projected {
+  uint32_t tiles, depth_bits;
+};
+
+__device__ __forceinline__ Projected preprocess_one(const Camera& cam, const float (&g)[16], const float* shv,
+                                                    uint32_t basis_count, float4* __restrict__ out) {
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (depth_order) depth_order[i] = i;
   auto culled = [&]() {
     out[0] = zero;
     out[1] = zero;
     out[2] = zero;
-    if (tile_counts) tile_counts[i] = 0;
-    if (depth_keys) depth_keys[i] = 0;
+    return Projected{0u, 0u};
   };
   if (-view_z(cam, g) <= 0.2f) return culled();
   Projection p;
@@ -109,21 +70,105 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
     off[2] = g[2] - campos[2];
     normalize3(off, dir);
     sh_basis(dir, basis);
-    const float* c = s_sh + threadIdx.x * SH_REST_FLOATS;
     for (uint32_t k = 0; k < basis_count; k++) {
-      color[0] = color[0] + basis[k] * c[k * 3 + 0];
-      color[1] = color[1] + basis[k] * c[k * 3 + 1];
-      color[2] = color[2] + basis[k] * c[k * 3 + 2];
+      color[0] = color[0] + basis[k] * shv[k * 3 + 0];
+      color[1] = color[1] + basis[k] * shv[k * 3 + 1];
+      color[2] = color[2] + basis[k] * shv[k * 3 + 2];
     }
   }
   out[0] = make_float4(mx, my, p.depth, radius);
   out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, 0.0f);
   out[2] = make_float4(fmaxf(color[0], 0.0f), fmaxf(color[1], 0.0f), fmaxf(color[2], 0.0f), g[3]);
-  if (tile_counts) {
-    uint4 rect = tile_rect(mx, my, radius, tile_grid(cam));
-    tile_counts[i] = (rect.z - rect.x) * (rect.w - rect.y);
+  const uint4 rect = tile_rect(mx, my, radius, tile_grid(cam));
+  return Projected{(rect.z - rect.x) * (rect.w - rect.y), __float_as_uint(p.depth)};
+}
+
+// Stages the SH coefficients of Gaussians [first, first + n) into shared memory
+// with coalesced loads (45 floats per Gaussian; the odd stride makes the
+// per-thread reads conflict-free). All threads of the CTA take part.
+__device__ __forceinline__ void stage_sh(float* s_sh, const float* __restrict__ sh, uint32_t first, uint32_t n) {
+  const float* src = sh + (size_t)first * SH_REST_FLOATS;
+  const uint32_t floats = n * SH_REST_FLOATS;
+  if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    const uint32_t vecs = floats / 4;
+    for (uint32_t k = threadIdx.x; k < vecs; k += blockDim.x)
+      reinterpret_cast<float4*>(s_sh)[k] = reinterpret_cast<const float4*>(src)[k];
+    for (uint32_t k = vecs * 4 + threadIdx.x; k < floats; k += blockDim.x) s_sh[k] = src[k];
+  } else {
+    for (uint32_t k = threadIdx.x; k < floats; k += blockDim.x) s_sh[k] = src[k];
   }
-  if (depth_keys) depth_keys[i] = __float_as_uint(p.depth);
+}
+
+__device__ __forceinline__ void load_gaussian(const float* __restrict__ gaussians, uint32_t i, float (&g)[16]) {
+  const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float4 q = gp[k];
+    g[4 * k] = q.x;
+    g[4 * k + 1] = q.y;
+    g[4 * k + 2] = q.z;
+    g[4 * k + 3] = q.w;
+  }
+}
+
+// One thread per Gaussian, one view. When tile_counts is given, the tiles each
+// splat touches are written too (src/shaders/tiles.wgsl:24-35, fused); when
+// depth_keys is given, the depth's bits (0 when culled) and the splat's index,
+// the input of the depth sort.
+__global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* __restrict__ camera,
+                                                                 const float* __restrict__ gaussians,
+                                                                 const float* __restrict__ sh, uint32_t count,
+                                                                 const uint32_t* __restrict__ scene_params,
+                                                                 float* __restrict__ splats,
+                                                                 uint32_t* __restrict__ tile_counts,
+                                                                 uint32_t* __restrict__ depth_keys,
+                                                                 uint32_t* __restrict__ depth_order) {
+  __shared__ Camera s_cam;
+  __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
+  load_camera(s_cam, camera);
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  const uint32_t block_start = blockIdx.x * PRE_THREADS;
+  if (basis_count > 0) stage_sh(s_sh, sh, block_start, min((uint32_t)PRE_THREADS, count - block_start));
+  __syncthreads();
+  const uint32_t i = block_start + threadIdx.x;
+  if (i >= count) return;
+  float g[16];
+  load_gaussian(gaussians, i, g);
+  const Projected pr = preprocess_one(s_cam, g, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count,
+                                      reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT));
+  if (tile_counts) tile_counts[i] = pr.tiles;
+  if (depth_keys) depth_keys[i] = pr.depth_bits;
+  if (depth_order) depth_order[i] = i;
+}
+
+// The same for a batch of views sharing one viewport: each CTA stages its
+// Gaussians and their SH coefficients once and projects them into every view.
+// Splat (view v, Gaussian i) is number v * count + i; its depth-sort key puts
+// the view above the depth's bits, so one sort orders every view by depth.
+__global__ void __launch_bounds__(PRE_THREADS) preprocess_views_kernel(
+    const Camera* __restrict__ cameras, uint32_t views, const float* __restrict__ gaussians,
+    const float* __restrict__ sh, uint32_t count, const uint32_t* __restrict__ scene_params,
+    float* __restrict__ splats, uint32_t* __restrict__ tile_counts, uint2* __restrict__ depth_keys,
+    uint32_t* __restrict__ depth_order) {
+  __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  const uint32_t block_start = blockIdx.x * PRE_THREADS;
+  if (basis_count > 0) stage_sh(s_sh, sh, block_start, min((uint32_t)PRE_THREADS, count - block_start));
+  __syncthreads();
+  const uint32_t i = block_start + threadIdx.x;
+  if (i >= count) return;
+  float g[16];
+  load_gaussian(gaussians, i, g);
+  for (uint32_t v = 0; v < views; v++) {
+    const size_t at = (size_t)v * count + i;
+    const Projected pr = preprocess_one(cameras[v], g, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count,
+                                        reinterpret_cast<float4*>(splats + at * FLOATS_PER_SPLAT));
+    tile_counts[at] = pr.tiles;
+    depth_keys[at] = make_uint2(pr.depth_bits, v);
+    depth_order[at] = (uint32_t)at;
+  }
 }
 
 // The depth-first tile sort (the renderer's path). The reference sorts 64-bit
@@ -143,12 +188,15 @@ __global__ void gather_counts_kernel(const uint32_t* __restrict__ order, const u
 
 // duplicate_kernel's warp-cooperative emission over splats in depth order: the
 // pairs of 32 consecutive sorted splats are one contiguous run of slots. Keys are
-// the tile index alone (u32), values the splat index.
+// the tile index alone (u32), values the splat index. For a batch of views
+// (splat v * per_view + i is Gaussian i in view v), the tiles of view v are
+// numbered after those of the views before it.
 __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Camera* __restrict__ camera,
                                                                        const float* __restrict__ splats,
                                                                        const uint32_t* __restrict__ order,
                                                                        const uint32_t* __restrict__ offsets,
-                                                                       uint32_t count, uint32_t capacity,
+                                                                       uint32_t count, uint32_t per_view,
+                                                                       uint32_t capacity,
                                                                        uint32_t* __restrict__ keys,
                                                                        uint32_t* __restrict__ values) {
   __shared__ uint32_t s_excl[DUP_THREADS];
@@ -156,6 +204,7 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   __shared__ uint32_t s_y0[DUP_THREADS];
   __shared__ uint32_t s_w[DUP_THREADS];
   __shared__ uint32_t s_index[DUP_THREADS];
+  __shared__ uint32_t s_base[DUP_THREADS];  // the first tile number of the splat's view
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t j = blockIdx.x * DUP_THREADS + threadIdx.x;
   const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
@@ -186,6 +235,7 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   s_y0[threadIdx.x] = rect.y;
   s_w[threadIdx.x] = rect.z - rect.x;
   s_index[threadIdx.x] = index;
+  s_base[threadIdx.x] = (index / per_view) * (tiles.x * tiles.y);
   __syncwarp();
   for (uint32_t k = lane; k < total; k += 32) {
     int lo = 0;
@@ -199,7 +249,7 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
     const uint32_t x = s_x0[src] + local % w;
     const uint32_t slot = slot0 + k;
     if (slot < capacity) {
-      keys[slot] = y * tiles.x + x;
+      keys[slot] = s_base[src] + y * tiles.x + x;
       values[slot] = s_index[src];
     }
   }
@@ -328,13 +378,15 @@ __device__ __forceinline__ unsigned char to_unorm8(float v) {
 
 // ------------------------------------------------------------------ work plan
 // Orders the frame's blend work; one CTA. The forward pass takes tiles with more
-// than COOP_MIN entries first, longest first by powers of two, then the rest; the
-// backward pass takes the (tile, chunk) pairs of tiles with several chunks first.
-// Order within a group follows atomics and does not change any result.
+// than coop_min entries first, longest first by powers of two, then the rest; the
+// backward pass (when chunks is given) takes the (tile, chunk) pairs of tiles
+// with several chunks first. Order within a group follows atomics and does not
+// change any result.
 constexpr uint32_t PLAN_THREADS = 1024;
 
 __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(const uint2* __restrict__ ranges, uint32_t tiles,
-                                                            uint32_t* __restrict__ plan, uint2* __restrict__ chunks) {
+                                                            uint32_t coop_min, uint32_t* __restrict__ plan,
+                                                            uint2* __restrict__ chunks) {
   __shared__ uint32_t s_bucket[32];  // cooperative tiles by floor(log2(length)); then write cursors
   __shared__ uint32_t s_light, s_multi, s_single;
   const uint32_t tid = threadIdx.x;
@@ -344,7 +396,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(const uint2* __restr
   for (uint32_t t = tid; t < tiles; t += PLAN_THREADS) {
     const uint2 r = ranges[t];
     const uint32_t len = r.y - r.x;
-    if (len > COOP_MIN) atomicAdd(&s_bucket[31 - __clz(len)], 1u);
+    if (len > coop_min) atomicAdd(&s_bucket[31 - __clz(len)], 1u);
     const uint32_t nb = (len + CHUNK - 1) / CHUNK;
     if (nb > 1) atomicAdd(&s_multi, nb);
   }
@@ -367,7 +419,8 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(const uint2* __restr
   for (uint32_t t = tid; t < tiles; t += PLAN_THREADS) {
     const uint2 r = ranges[t];
     const uint32_t len = r.y - r.x;
-    order[len > COOP_MIN ? atomicAdd(&s_bucket[31 - __clz(len)], 1u) : atomicAdd(&s_light, 1u)] = t;
+    order[len > coop_min ? atomicAdd(&s_bucket[31 - __clz(len)], 1u) : atomicAdd(&s_light, 1u)] = t;
+    if (!chunks) continue;
     const uint32_t nb = (len + CHUNK - 1) / CHUNK;
     if (nb > 1) {
       const uint32_t at = atomicAdd(&s_multi, nb);
@@ -387,6 +440,7 @@ __global__ void __launch_bounds__(PLAN_THREADS) plan_kernel(const uint2* __restr
 __device__ __forceinline__ void save_checkpoints(float4* __restrict__ checkpoints, uint32_t run_x, uint32_t k_from,
                                                  uint32_t k_to, uint32_t block, uint32_t lane, float T, float r,
                                                  float g, float b) {
+  if (!checkpoints) return;
   for (uint32_t k = k_from; k < k_to; k++) checkpoints[checkpoint_at(run_x, k, block, lane)] = make_float4(T, r, g, b);
 }
 
@@ -471,40 +525,44 @@ struct PixelBlend {
 // helpers take the 32 bits of positions [p0, p0 + 32) of the pair list.
 __device__ __forceinline__ void publish_blended(uint32_t* __restrict__ mask, uint32_t p0, uint32_t block,
                                                 uint32_t bits) {
-  if (bits == 0) return;
+  if (bits == 0 || !mask) return;
   const uint32_t w = p0 >> 5, shift = p0 & 31u;
   const uint32_t lo = bits << shift, hi = shift ? bits >> (32u - shift) : 0u;
   if (lo) atomicOr(&mask[(size_t)w * 8u + block], lo);
   if (hi) atomicOr(&mask[(size_t)(w + 1) * 8u + block], hi);
 }
 
-// The geometry of a blend item: tile `tile`, 8x4 block `block`, this lane's pixel.
+// The geometry of a blend item: tile `tile` (of the view tile / tiles_per_view
+// when several views are blended together), 8x4 block `block`, this lane's pixel.
 struct BlendItem {
   uint32_t px, py;
+  size_t pixel;  // index in the views' stacked pixel buffers
   bool inside;
   float x0, y0;  // the block's first pixel center
   uint2 run;
-  __device__ __forceinline__ BlendItem(uint32_t tile, uint32_t block, uint32_t lane, uint32_t tiles_x, float vpx,
-                                       float vpy, const uint2* __restrict__ ranges) {
-    const uint32_t bx = (tile % tiles_x) * TILE + (block & 1u) * 8u, by = (tile / tiles_x) * TILE + (block >> 1) * 4u;
+  __device__ __forceinline__ BlendItem(uint32_t tile, uint32_t block, uint32_t lane, uint32_t tiles_x,
+                                       uint32_t tiles_per_view, float vpx, float vpy, const uint2* __restrict__ ranges) {
+    const uint32_t view = tile / tiles_per_view, local = tile - view * tiles_per_view;
+    const uint32_t bx = (local % tiles_x) * TILE + (block & 1u) * 8u, by = (local / tiles_x) * TILE + (block >> 1) * 4u;
     px = bx + (lane & 7u);
     py = by + (lane >> 3);
     inside = (float)px < vpx && (float)py < vpy;
+    const uint32_t width = (uint32_t)vpx, height = (uint32_t)vpy;
+    pixel = (size_t)view * width * height + (size_t)py * width + px;
     x0 = (float)bx + 0.5f;
     y0 = (float)by + 0.5f;
     run = ranges[tile];
   }
 };
 
-__device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlend& pb, float4 bg, uint32_t width,
+__device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlend& pb, float4 bg,
                                             uchar4* __restrict__ target, float4* __restrict__ pixel_color,
                                             uint32_t* __restrict__ pixel_last) {
   if (!it.inside) return;
   const float fr = pb.r + pb.T * bg.x, fg = pb.g + pb.T * bg.y, fb = pb.b + pb.T * bg.z;
-  const uint32_t p = it.py * width + it.px;
-  pixel_color[p] = make_float4(fr, fg, fb, pb.T);
-  pixel_last[p] = pb.last;
-  if (target) target[p] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
+  pixel_color[it.pixel] = make_float4(fr, fg, fb, pb.T);
+  pixel_last[it.pixel] = pb.last;
+  if (target) target[it.pixel] = make_uchar4(to_unorm8(fr), to_unorm8(fg), to_unorm8(fb), 255);
 }
 
 // src/shaders/rasterize.wgsl:32-100. The work is split into items, one per (tile,
@@ -513,11 +571,11 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 // front to back exactly as the plain loop over every entry does, so results are
 // bit-identical to it; the split only decides who does the work:
 //
-// - Tiles with more than COOP_MIN entries come first, each block blended by a
-//   whole CTA. Its warps take consecutive 32-entry windows, keep the splats that
-//   can reach the block and compute their alphas at the block's pixels, queueing
-//   those some pixel blends; warp 0 then applies the queued alphas of all the
-//   windows in list order. The costly part of each splat (power, exp, alpha) is
+// - Tiles with more entries than the plan's threshold (COOP_MIN unless tuned)
+//   come first, each block blended by a whole CTA. Its warps take consecutive
+//   32-entry windows, keep the splats that can reach the block and compute their
+//   alphas at the block's pixels, queueing those some pixel blends; warp 0 then
+//   applies the queued alphas of all the windows in list order. The costly part of each splat (power, exp, alpha) is
 //   spread over the CTA; only the short transmittance update stays serial.
 // - Every warp then takes the other blocks on its own, walking the list 32
 //   entries at a time.
@@ -530,15 +588,15 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
-    uchar4* __restrict__ target, float4* __restrict__ pixel_color, uint32_t* __restrict__ pixel_last,
-    float4* __restrict__ checkpoints, uint32_t* __restrict__ blend_mask, uint32_t* __restrict__ counters) {
+    uint32_t tiles_per_view, uchar4* __restrict__ target, float4* __restrict__ pixel_color,
+    uint32_t* __restrict__ pixel_last, float4* __restrict__ checkpoints, uint32_t* __restrict__ blend_mask,
+    uint32_t* __restrict__ counters) {
   __shared__ WarpStage stages[FWD_WARPS];
   __shared__ float s_alpha[FWD_WARPS][32][32];  // cooperative: alphas of each warp's queued entries
   __shared__ uint32_t s_item, s_stop, s_done;  // s_done: warp 0's pixels that have stopped
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   WarpStage& st = stages[warp];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
-  const uint32_t width = (uint32_t)vpx;
   const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
   const float4 bg = raster_params[0];
   const uint32_t cooperative = plan[0], tiles = plan[1];
@@ -555,7 +613,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const uint32_t item = s_item;
     if (item >= cooperative * 8u) break;
     const uint32_t block = item & 7u;
-    const BlendItem it(order[item >> 3], block, lane, tiles_x, vpx, vpy, ranges);
+    const BlendItem it(order[item >> 3], block, lane, tiles_x, tiles_per_view, vpx, vpy, ranges);
     const uint2 run = it.run;
     PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
     uint32_t next_k = 1;  // the next checkpoint boundary (warp 0)
@@ -646,7 +704,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     if (warp == 0) {
       save_checkpoints(checkpoints, run.x, next_k, (run.y - run.x + CHUNK - 1) / CHUNK, block, lane, pb.T, pb.r, pb.g,
                        pb.b);
-      write_pixel(it, pb, bg, width, target, pixel_color, pixel_last);
+      write_pixel(it, pb, bg, target, pixel_color, pixel_last);
     }
   }
 
@@ -657,7 +715,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= (tiles - cooperative) * 8u) break;
     const uint32_t block = item & 7u;
-    const BlendItem it(order[cooperative + (item >> 3)], block, lane, tiles_x, vpx, vpy, ranges);
+    const BlendItem it(order[cooperative + (item >> 3)], block, lane, tiles_x, tiles_per_view, vpx, vpy, ranges);
     const uint2 run = it.run;
     PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
     uint32_t next_k = 1;
@@ -693,7 +751,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     cp_async_wait_all();  // a window may still be in flight after an early stop
     save_checkpoints(checkpoints, run.x, next_k, (run.y - run.x + CHUNK - 1) / CHUNK, block, lane, pb.T, pb.r, pb.g,
                      pb.b);
-    write_pixel(it, pb, bg, width, target, pixel_color, pixel_last);
+    write_pixel(it, pb, bg, target, pixel_color, pixel_last);
   }
 }
 
@@ -749,6 +807,7 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
   uint32_t capacity = initial_pair_capacity ? initial_pair_capacity : std::max(1u << 16, count * 8u);
   if (st == DG_OK) st = make_pairs(tr, capacity);
   tr->depth_first = depth_first;
+  tr->coop_min = COOP_MIN;
   if (st == DG_OK && depth_first) {
     const size_t n = std::max(count, 1u);
     tr->depth_plan = sort_plan_low_bits(std::max(count, 1u), 32);
@@ -820,7 +879,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
     if (count > 0) {
       DG_LAUNCH(ctx, "duplicate",
                 duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
-                    cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count,
+                    cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count, count,
                     tr->pair_capacity, typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values)));
     }
     DG_TRY(sort_launch(ctx, tr->tile_plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
@@ -859,24 +918,39 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
 
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   dg_context* ctx = tr->ctx;
-  const uint32_t tiles = tr->tiles_x * tr->tiles_y;
-  DG_CUDA(cudaMemsetAsync(tr->work->ptr, 0, 16, ctx->stream));
   DG_CUDA(cudaMemsetAsync(tr->blend_mask->ptr, 0, tr->blend_mask->bytes, ctx->stream));
+  BlendForward f{};
+  f.camera = typed<const Camera>(tr->camera);
+  f.raster_params = typed<float4>(tr->raster_params);
+  f.splats = typed<float>(tr->splats);
+  f.pair_splats = typed<uint32_t>(tr->values);
+  f.ranges = typed<uint2>(tr->ranges);
+  f.tiles = f.tiles_per_view = tr->tiles_x * tr->tiles_y;
+  f.coop_min = tr->coop_min;
+  f.plan = typed<uint32_t>(tr->work_plan);
+  f.chunks = typed<uint2>(tr->chunks);
+  f.target = target ? typed<uchar4>(target) : nullptr;
+  f.pixel_color = typed<float4>(tr->pixel_color);
+  f.pixel_last = typed<uint32_t>(tr->pixel_last);
+  f.checkpoints = typed<float4>(tr->checkpoints);
+  f.blend_mask = typed<uint32_t>(tr->blend_mask);
+  f.counters = typed<uint32_t>(tr->work);
+  return blend_forward(ctx, f);
+}
+
+dg_status blend_forward(dg_context* ctx, const BlendForward& f) {
+  DG_CUDA(cudaMemsetAsync(f.counters, 0, 16, ctx->stream));
   DG_LAUNCH(ctx, "plan",
-            plan_kernel<<<1, PLAN_THREADS, 0, ctx->stream>>>(typed<uint2>(tr->ranges), tiles, typed<uint32_t>(tr->work_plan),
-                                                             typed<uint2>(tr->chunks)));
+            plan_kernel<<<1, PLAN_THREADS, 0, ctx->stream>>>(f.ranges, f.tiles, f.coop_min, f.plan, f.chunks));
   DG_LAUNCH(ctx, "rasterize",
-            rasterize_kernel<<<blend_grid(tr, (const void*)rasterize_kernel, FWD_THREADS), FWD_THREADS, 0,
-                               ctx->stream>>>(
-                typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
-                typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
-                target ? typed<uchar4>(target) : nullptr, typed<float4>(tr->pixel_color),
-                typed<uint32_t>(tr->pixel_last), typed<float4>(tr->checkpoints), typed<uint32_t>(tr->blend_mask),
-                typed<uint32_t>(tr->work)));
+            rasterize_kernel<<<blend_grid(ctx, (const void*)rasterize_kernel, FWD_THREADS, f.tiles * 8u), FWD_THREADS,
+                               0, ctx->stream>>>(f.camera, f.raster_params, f.splats, f.pair_splats, f.ranges, f.plan,
+                                                 f.tiles_per_view, f.target, f.pixel_color, f.pixel_last,
+                                                 f.checkpoints, f.blend_mask, f.counters));
   return DG_OK;
 }
 
-uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel, uint32_t threads) {
+uint32_t blend_grid(dg_context* ctx, const void* kernel, uint32_t threads, uint32_t items) {
   // As many CTAs as can be resident at once; each keeps taking items, so a CTA
   // that could not start until another finished would find none.
   int per_sm = 0;
@@ -884,8 +958,40 @@ uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel, uint32_t threads
     cudaGetLastError();
     per_sm = 1;
   }
-  const uint32_t items = tr->tiles_x * tr->tiles_y * 8u;
-  return std::max(1u, std::min(ceil_div(items, threads / 32u), (uint32_t)(tr->ctx->sm_count * per_sm)));
+  return std::max(1u, std::min(ceil_div(items, threads / 32u), (uint32_t)(ctx->sm_count * per_sm)));
+}
+
+dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32_t views, const float* gaussians,
+                                  const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
+                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order) {
+  DG_LAUNCH(ctx, "preprocess",
+            preprocess_views_kernel<<<ceil_div(count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
+                cameras, views, gaussians, sh, count, scene_params, splats, tile_counts, depth_keys, order));
+  return DG_OK;
+}
+
+dg_status gather_counts_launch(dg_context* ctx, const uint32_t* order, const uint32_t* counts, uint32_t n,
+                               uint32_t* out) {
+  DG_LAUNCH(ctx, "gather_counts",
+            gather_counts_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(order, counts, n, out));
+  return DG_OK;
+}
+
+dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
+                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,
+                                  uint32_t* keys, uint32_t* values) {
+  DG_LAUNCH(ctx, "duplicate",
+            duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, ctx->stream>>>(
+                camera, splats, order, offsets, count, per_view, capacity, keys, values));
+  return DG_OK;
+}
+
+dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
+                             uint32_t tiles, uint2* ranges) {
+  DG_LAUNCH(ctx, "find_ranges",
+            find_ranges_kernel<1><<<std::max(1u, ceil_div(capacity, RANGE_THREADS)), RANGE_THREADS, 0, ctx->stream>>>(
+                tile_keys, pair_total, capacity, tiles, ranges));
+  return DG_OK;
 }
 
 // The work plan, the backward's chunk list and the checkpoints, sized for the
@@ -1098,6 +1204,8 @@ dg_status dg_renderer_create(dg_context* ctx, uint32_t initial_pair_capacity, dg
   auto* r = new dg_renderer();
   r->ctx = ctx;
   r->initial_pair_capacity = initial_pair_capacity;
+  r->view_coop_min = COOP_MIN;
+  r->view_graph = true;
   dg_status st = alloc_buffer(ctx, sizeof(Camera), &r->camera);
   if (st != DG_OK) {
     delete r;
@@ -1215,6 +1323,7 @@ dg_status dg_renderer_destroy(dg_renderer* r) {
   if (!r) return DG_OK;
   destroy_scene(r);
   if (r->draw_rasterizer) dg_tile_rasterizer_destroy(r->draw_rasterizer);
+  view_batch_destroy(r->views);
   free_buffer(r->camera);
   delete r;
   return DG_OK;

@@ -52,6 +52,7 @@ struct dg_tile_rasterizer {
   dg_buffer* chunks;
   dg_buffer* checkpoints;
   dg_buffer* blend_mask;  // which entries each 8x4 block blended (dg_render.cu, publish_blended)
+  uint32_t coop_min;      // tiles with more entries are blended by a whole CTA
 };
 
 namespace dg {
@@ -66,10 +67,45 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
                             uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);
 dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity);
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
-// Grid of a persistent blend kernel.
-uint32_t blend_grid(dg_tile_rasterizer* tr, const void* kernel, uint32_t threads);
+// Grid of a persistent blend kernel of `threads` threads per CTA over `items`
+// warp items.
+uint32_t blend_grid(dg_context* ctx, const void* kernel, uint32_t threads, uint32_t items);
+
+// The forward blend (plan + rasterize kernels) over `tiles` tiles of
+// tiles_per_view each; checkpoints, blend_mask and chunks may be NULL when no
+// backward pass follows.
+struct BlendForward {
+  const Camera* camera;
+  const float4* raster_params;
+  const float* splats;
+  const uint32_t* pair_splats;
+  const uint2* ranges;
+  uint32_t tiles, tiles_per_view, coop_min;
+  uint32_t* plan;
+  uint2* chunks;
+  uchar4* target;
+  float4* pixel_color;
+  uint32_t* pixel_last;
+  float4* checkpoints;
+  uint32_t* blend_mask;
+  uint32_t* counters;  // 4 words, cleared here
+};
+dg_status blend_forward(dg_context* ctx, const BlendForward& f);
+// The batched views' stages (dg_render.cu; used by dg_views.cu).
+dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32_t views, const float* gaussians,
+                                  const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
+                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order);
+dg_status gather_counts_launch(dg_context* ctx, const uint32_t* order, const uint32_t* counts, uint32_t n,
+                               uint32_t* out);
+dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
+                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,
+                                  uint32_t* keys, uint32_t* values);
+dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
+                             uint32_t tiles, uint2* ranges);
 dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr);
 }  // namespace dg
+
+struct dg_view_batch;
 
 // GaussianRenderer (src/gaussianRenderer.ts:55-311).
 struct dg_renderer {
@@ -89,6 +125,12 @@ struct dg_renderer {
   dg_buffer* grad_gaussians;
   dg_buffer* grad_sh;
   dg_tile_rasterizer* draw_rasterizer;
+  // Batched views (dg_views.cu): buffers, views per batch (0: all), the blend's
+  // cooperative threshold, and whether a batch is replayed as a CUDA graph.
+  dg_view_batch* views;
+  uint32_t view_batch;
+  uint32_t view_coop_min;
+  bool view_graph;
 };
 
 namespace dg {
@@ -101,4 +143,10 @@ const Camera* renderer_camera(dg_renderer* r);
 // The backward kernels (dg_render_bwd.cu).
 dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status launch_preprocess_backward(dg_renderer* r);
+// Batched views (dg_views.cu): renders count views in batches of `batch` into
+// targets (count rgba8 images, may be NULL) and pixel_colors (count vec4 images,
+// may be NULL).
+dg_status views_render(dg_renderer* r, const dg_camera* cams, uint32_t count, const float bg[3], uchar4* targets,
+                       float4* pixel_colors, uint32_t batch, uint32_t coop_min);
+void view_batch_destroy(dg_view_batch* b);
 }  // namespace dg

@@ -537,7 +537,8 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
   uint32_t* counter = typed<uint32_t>(tr->work) + 2;
   DG_CUDA(cudaMemsetAsync(counter, 0, sizeof(uint32_t), ctx->stream));
   DG_LAUNCH(ctx, "rasterize_backward",
-            rasterize_backward_kernel<<<blend_grid(tr, (const void*)rasterize_backward_kernel, BWD_THREADS),
+            rasterize_backward_kernel<<<blend_grid(ctx, (const void*)rasterize_backward_kernel, BWD_THREADS,
+                                                    tr->tiles_x * tr->tiles_y * 8u),
                                         BWD_THREADS, 0, ctx->stream>>>(
                 typed<const Camera>(tr->camera), typed<float4>(tr->raster_params), typed<float>(tr->splats),
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),

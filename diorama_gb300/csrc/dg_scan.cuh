@@ -19,12 +19,16 @@ struct SortPlan {
   uint32_t capacity;
   uint32_t key_words;
   uint32_t high_bits;
-  uint32_t passes;     // always even, so the result lands back in keys/values
+  uint32_t passes;     // even in the reference's plans, so the result lands back in keys/values
   uint32_t shift[8];   // bit offset of each pass's 8-bit digit within the key
 };
 SortPlan sort_plan(uint32_t capacity, uint32_t high_bits);
 // u32 keys of which only the low `bits` bits vary (bits a multiple of 16).
 SortPlan sort_plan_low_bits(uint32_t capacity, uint32_t bits);
+// The fewest 8-bit passes for keys whose varying bits are the low `bits` (u32
+// keys) or all 32 low-word bits plus `bits` high-word bits (u64 keys). With an
+// odd number of passes the result lands in keys_alt/values_alt.
+SortPlan sort_plan_digits(uint32_t capacity, uint32_t key_words, uint32_t bits);
 // Per-device kernel attributes; called once when a context is created.
 dg_status sort_init();
 size_t sort_scratch_bytes(const SortPlan& plan);

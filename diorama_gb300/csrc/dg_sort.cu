@@ -311,6 +311,16 @@ SortPlan sort_plan_low_bits(uint32_t capacity, uint32_t bits) {
   return p;
 }
 
+SortPlan sort_plan_digits(uint32_t capacity, uint32_t key_words, uint32_t bits) {
+  SortPlan p{};
+  p.capacity = capacity;
+  p.key_words = key_words;
+  p.high_bits = key_words == 2 ? bits : 0;
+  p.passes = key_words == 2 ? 4 + (bits + 7) / 8 : std::max(1u, (bits + 7) / 8);
+  for (uint32_t k = 0; k < p.passes; k++) p.shift[k] = k * 8;
+  return p;
+}
+
 size_t sort_scratch_bytes(const SortPlan& plan) { return layout_of(plan).total; }
 
 dg_status sort_launch(dg_context* ctx, const SortPlan& plan, void* keys, uint32_t* values, void* keys_alt,

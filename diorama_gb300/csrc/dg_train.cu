@@ -655,18 +655,33 @@ dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint
   DG_REQUIRE(t && views && psnr && ssim, "NULL argument");
   DG_REQUIRE(view_count > 0, "no views");
   dg_context* ctx = t->ctx;
-  dg_buffer *sums = nullptr, *slot = nullptr;
+  for (uint32_t k = 1; k < view_count; k++)
+    DG_REQUIRE(views[k].camera.viewport[0] == views[0].camera.viewport[0] &&
+                   views[k].camera.viewport[1] == views[0].camera.viewport[1],
+               "All evaluated views must be the same size.");
+  const uint32_t w = (uint32_t)views[0].camera.viewport[0], h = (uint32_t)views[0].camera.viewport[1];
+  const size_t pixels = (size_t)w * h;
+  for (uint32_t k = 0; k < view_count; k++)
+    DG_REQUIRE(views[k].image && views[k].image->bytes >= pixels * 4, "a view's image is too small");
+  dg_buffer *sums = nullptr, *slot = nullptr, *rendered = nullptr;
   DG_TRY(alloc_buffer(ctx, view_count * 16, &sums));
   DG_TRY(alloc_buffer(ctx, 8 * view_count, &slot));
+  DG_TRY(alloc_buffer(ctx, pixels * 16 * view_count, &rendered));
   std::vector<const void*> photos(view_count);
-  for (uint32_t k = 0; k < view_count; k++) photos[k] = views[k].image->ptr;
-  DG_TRY(write_async(ctx, slot->ptr, photos.data(), 8 * view_count));
+  std::vector<dg_camera> cameras(view_count);
   for (uint32_t k = 0; k < view_count; k++) {
-    const dg_camera& cam = views[k].camera;
-    DG_TRY(dg_renderer_encode(t->renderer, t->target, &cam, t->settings.background));
+    photos[k] = views[k].image->ptr;
+    cameras[k] = views[k].camera;
+  }
+  DG_TRY(write_async(ctx, slot->ptr, photos.data(), 8 * view_count));
+  // Every view rendered in batches (dg_views.cu), then scored on the GPU.
+  dg_renderer* r = t->renderer;
+  DG_TRY(views_render(r, cameras.data(), view_count, t->settings.background, nullptr, typed<float4>(rendered),
+                      r->view_batch, r->view_coop_min));
+  for (uint32_t k = 0; k < view_count; k++) {
+    dg_buffer view_rendered{ctx, static_cast<char*>(rendered->ptr) + pixels * 16 * k, pixels * 16, false};
     dg_buffer view_slot{ctx, static_cast<char*>(slot->ptr) + 8 * k, 8, false};
-    DG_TRY(metrics_launch(ctx, t->renderer->rasterizer->pixel_color, &view_slot, (uint32_t)cam.viewport[0],
-                          (uint32_t)cam.viewport[1], typed<double>(sums) + 2 * k));
+    DG_TRY(metrics_launch(ctx, &view_rendered, &view_slot, w, h, typed<double>(sums) + 2 * k));
   }
   std::vector<double> host(2 * view_count);
   DG_CUDA(cudaMemcpyAsync(host.data(), sums->ptr, 16 * view_count, cudaMemcpyDeviceToHost, ctx->stream));
@@ -679,6 +694,7 @@ dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint
   }
   free_buffer(sums);
   free_buffer(slot);
+  free_buffer(rendered);
   *psnr = psnr_total / view_count;
   *ssim = with_ssim ? ssim_total / view_count : NAN;
   return DG_OK;

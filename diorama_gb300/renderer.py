@@ -6,7 +6,7 @@ is enqueued on the device's stream as it is encoded)."""
 from __future__ import annotations
 
 import ctypes
-from ctypes import c_void_p
+from ctypes import c_double, c_uint32, c_void_p
 from dataclasses import dataclass
 
 import numpy as np
@@ -201,10 +201,52 @@ class GaussianRenderer:
     def afterSubmit(self, wait: bool = True) -> None:
         _lib.call("dg_renderer_after_submit", self.handle, int(wait))
 
+    # Batched views: no reference counterpart (the reference renders held-out
+    # views one at a time); images are bit-identical to encode()'s.
+    def renderViews(self, cameras: list[CameraData], background, targets: Buffer | None = None,
+                    pixelColors: Buffer | None = None) -> None:
+        """Renders every camera's view (all one size) into targets (rgba8 images
+        back to back) and pixelColors (vec4 images), each optional."""
+        arr = _cameras_c(cameras)
+        _lib.call("dg_renderer_render_views", self.handle, arr, len(cameras), _lib.floats(background),
+                  targets.handle if targets is not None else None,
+                  pixelColors.handle if pixelColors is not None else None)
+
+    def setViewBatching(self, batch: int = 0, coopMin: int = 0, graph: bool = True) -> None:
+        _lib.call("dg_renderer_set_view_batching", self.handle, batch, coopMin, int(graph))
+
+    @property
+    def viewBatching(self) -> dict:
+        batch, coop = c_uint32(), c_uint32()
+        _lib.call("dg_renderer_view_batching", self.handle, ctypes.byref(batch), ctypes.byref(coop))
+        return {"batch": batch.value, "coopMin": coop.value}
+
+    def tuneViews(self, cameras: list[CameraData], background, targets: Buffer | None = None) -> dict:
+        """Times the (views per batch, cooperative threshold) candidates on these
+        views and keeps the fastest; returns it and every candidate's seconds."""
+        arr = _cameras_c(cameras)
+        batch, coop, tried = c_uint32(), c_uint32(), c_uint32()
+        seconds = (c_double * 32)()
+        _lib.call("dg_renderer_tune_views", self.handle, arr, len(cameras), _lib.floats(background),
+                  targets.handle if targets is not None else None, ctypes.byref(batch), ctypes.byref(coop),
+                  seconds, ctypes.byref(tried))
+        return {"batch": batch.value, "coopMin": coop.value, "seconds": list(seconds[: tried.value])}
+
+    @property
+    def viewsPixelLast(self) -> Buffer | None:
+        return self._buffer("dg_renderer_views_pixel_last")
+
     def destroy(self) -> None:
         if self.owned and self.handle:
             _lib.call("dg_renderer_destroy", self.handle)
         self.handle = None
+
+
+def _cameras_c(cameras: list[CameraData]):
+    arr = (_lib.Camera * len(cameras))()
+    for k, cam in enumerate(cameras):
+        arr[k] = cam.to_c()
+    return arr
 
 
 def shRestFloats(count: int) -> int:

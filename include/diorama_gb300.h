@@ -189,6 +189,27 @@ dg_tile_rasterizer* dg_renderer_tiles(dg_renderer* r);
 dg_tile_rasterizer* dg_renderer_draw_tiles(dg_renderer* r);
 dg_status dg_renderer_destroy(dg_renderer* r);
 
+/* ---- Batched views. No reference counterpart: the reference renders held-out
+ * views one at a time (src/trainer.ts:371-386); these render many views of the
+ * scene together, each stage once per batch, with images bit-identical to
+ * dg_renderer_encode's. All views must share one viewport. */
+/* Renders count views: targets (NULL or count rgba8 images of the viewport,
+ * back to back) and pixel_colors (NULL or count vec4 images: rgb, final T). */
+dg_status dg_renderer_render_views(dg_renderer* r, const dg_camera* cameras, uint32_t count, const float background[3],
+                                   dg_buffer* targets, dg_buffer* pixel_colors);
+/* Views per batch (0: all at once), the blend's cooperative threshold (0: the
+ * default) and whether a batch replays as one CUDA graph. */
+dg_status dg_renderer_set_view_batching(dg_renderer* r, uint32_t batch, uint32_t coop_min, int32_t graph);
+dg_status dg_renderer_view_batching(const dg_renderer* r, uint32_t* batch, uint32_t* coop_min);
+/* The autotuner: times each (views per batch, cooperative threshold) candidate on
+ * these views and keeps the fastest. seconds (NULL or room for 32) receives each
+ * candidate's time in the order tried; tried, how many were tried. */
+dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint32_t count, const float background[3],
+                                 dg_buffer* targets, uint32_t* best_batch, uint32_t* best_coop_min, double* seconds,
+                                 uint32_t* tried);
+/* The last batch's pixel_last (views x pixels u32), for inspection. */
+dg_buffer* dg_renderer_views_pixel_last(dg_renderer* r);
+
 /* ---- TrainingLoss (src/trainingLoss.ts:16-130): 0.8 L1 + 0.2 (1 - SSIM). */
 dg_status dg_training_loss_create(dg_context* ctx, uint32_t width, uint32_t height, dg_training_loss** out);
 /* encode(encoder, rendered, target): rendered vec4 per pixel, target rgba8 bytes. */

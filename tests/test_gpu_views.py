@@ -1,0 +1,78 @@
+"""Batched views on the GPU (no reference counterpart: the reference renders
+held-out views one at a time, src/trainer.ts:371-386).
+
+Held-out views of the planes-and-boxes scene rendered together must give, view
+by view, the same pixel colours, last indices and rgba8 images as
+GaussianRenderer.encode, bit for bit: in one batch, in several, with and
+without graph replay, and with whatever the autotuner picks."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from diorama_gb300 import GaussianRenderer, activate, scenes
+
+pytestmark = pytest.mark.gpu
+
+BG = (0.1, 0.2, 0.3)
+
+
+@pytest.fixture(scope="module")
+def scene(device):
+    raw, sh = scenes.surface_scene(200_000, 22, noise=0.01)
+    _train, held = scenes.ring_cameras()
+    r = GaussianRenderer(device)
+    r.setGaussians(activate(raw), {"rest": sh.reshape(-1), "degree": 3})
+    cams = held[:6]
+    W, H = cams[0].viewport
+    colors, lasts, images = [], [], []
+    tex = device.createTexture(W, H)
+    for cam in cams:
+        for _ in range(2):  # the first frame may grow the pair buffers
+            r.encode(None, tex, cam, BG)
+            r.afterSubmit()
+        colors.append(r.pixelBuffer.read(np.float32)[: W * H * 4].copy())
+        lasts.append(r.pixelLastBuffer.read(np.uint32)[: W * H].copy())
+        images.append(tex.buffer.read(np.uint8)[: W * H * 4].copy())
+    tex.destroy()
+    yield r, cams, colors, lasts, images
+    r.destroy()
+
+
+def _check(device, r, cams, colors, lasts, images, batch):
+    W, H = cams[0].viewport
+    n = len(cams)
+    targets = device.createBuffer(n * W * H * 4)
+    pixel_colors = device.createBuffer(n * W * H * 16)
+    r.renderViews(cams, BG, targets, pixel_colors)
+    got_color = pixel_colors.read(np.float32).reshape(n, -1)
+    got_image = targets.read(np.uint8).reshape(n, -1)
+    for k in range(n):
+        assert np.array_equal(got_color[k].view(np.uint32), colors[k].view(np.uint32)), (batch, k)
+        assert np.array_equal(got_image[k], images[k]), (batch, k)
+    # pixel_last of the last batch: its views are the last `size` ones.
+    size = n - (batch * ((n - 1) // batch) if batch else 0)
+    last = r.viewsPixelLast.read(np.uint32)[: size * W * H].reshape(size, -1)
+    for j in range(size):
+        assert np.array_equal(last[j], lasts[n - size + j]), (batch, j)
+    targets.destroy()
+    pixel_colors.destroy()
+
+
+@pytest.mark.parametrize("batch,graph", [(0, True), (0, False), (4, True), (1, True)])
+def test_views_match_single_view_renders(device, scene, batch, graph):
+    r, cams, colors, lasts, images = scene
+    r.setViewBatching(batch, 0, graph)
+    _check(device, r, cams, colors, lasts, images, batch)
+    _check(device, r, cams, colors, lasts, images, batch)  # replays the captured batch
+    assert device.check() == 0
+
+
+def test_autotuned_views_match(device, scene):
+    r, cams, colors, lasts, images = scene
+    tuned = r.tuneViews(cams, BG)
+    assert tuned["batch"] in {1, 4, len(cams)} and tuned["coopMin"] in {256, 512, 1024, 2048}
+    assert len(tuned["seconds"]) >= 4 and min(tuned["seconds"]) > 0
+    assert r.viewBatching == {"batch": tuned["batch"], "coopMin": tuned["coopMin"]}
+    _check(device, r, cams, colors, lasts, images, tuned["batch"])
