@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--views", type=int, default=263, help="training views (photos) to render and cycle through")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
+    ap.add_argument("--workload", default="train", choices=["train", "sort"],
+                    help="train: the headline training step; sort: config 2's sort/scan/ranges stress "
+                         "(1.1M Gaussians at 1960x1090, ~12M 64-bit keys, the reference's 6-pass sort)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     return args
@@ -253,8 +257,27 @@ def run_ours(args, rank, world, local, group):
     e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * H * 4 + camera_bytes + adam_bytes
            + 8 + 16, "d2h_bytes_per_step": 8 + 4}
 
-    # Per-kernel times: the same steps launched directly, each kernel bracketed by events.
+    # The same steps without graph replay (config 3 reports the captured step
+    # against the uncaptured one).
     trainer.setGraph(False)
+    trainer.step()
+    device.synchronize()
+    start.record()
+    for _ in range(args.steps):
+        trainer.step()
+    end.record()
+    uncaptured = {"value": round(args.steps / (start.elapsed_ms(end) / 1000.0), 2), "unit": UNIT}
+
+    # Held-out views: all 37 rendered together (batched stages, graph replay,
+    # batch size and cooperative threshold from the autotuner) against the
+    # per-view encode loop, in frames/s.
+    held = None if args.no_held_out else held_out_views(args)
+    if rank == 0 and held is not None:
+        held_out = measure_held_out(device, trainer.renderer, held, args.steps)
+    else:
+        held_out = None
+
+    # Per-kernel times: the same steps launched directly, each kernel bracketed by events.
     device.synchronize()
     device.setKernelTiming(True)
     device.kernelTimingReport()
@@ -298,6 +321,7 @@ def run_ours(args, rank, world, local, group):
         "kernels": {k: {"avg_us": round(v["avg_us"], 2), "share": round(v["share"], 4), "launches": v["launches"]}
                     for k, v in sorted(kernels.items(), key=lambda kv: -kv[1]["share"])},
         "dominant_kernel": dominant, "blend": blend, "pairs": pairs, "gaussians": n,
+        "uncaptured_step": uncaptured, "held_out": held_out,
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, raw, sh, views_host(views), cams, samples=1)
@@ -308,6 +332,52 @@ def run_ours(args, rank, world, local, group):
         p.free()
     device.destroy()
     return result
+
+
+def held_out_views(args):
+    from diorama_gb300 import scenes
+
+    _train, held = scenes.ring_cameras()
+    return held
+
+
+def measure_held_out(device, renderer, held, repeats: int) -> dict:
+    """Frames/s of the 37 held-out views: batched (autotuned, graph replay) and
+    one encode() per view, with the batched images checked against the per-view
+    ones."""
+    W, H = held[0].viewport
+    n = len(held)
+    bg = (0.0, 0.0, 0.0)
+    targets = device.createBuffer(n * W * H * 4)
+    tuned = renderer.tuneViews(held, bg, targets)
+    renderer.renderViews(held, bg, targets)
+    device.synchronize()
+    start, end = device.event(), device.event()
+    reps = max(1, repeats // 4)
+    start.record()
+    for _ in range(reps):
+        renderer.renderViews(held, bg, targets)
+    end.record()
+    batched = n * reps / (start.elapsed_ms(end) / 1000.0)
+    tex = device.createTexture(W, H)
+    for cam in held[:2]:
+        renderer.encode(None, tex, cam, bg)
+        renderer.afterSubmit()
+    start.record()
+    for _ in range(reps):
+        for cam in held:
+            renderer.encode(None, tex, cam, bg)
+    end.record()
+    per_view = n * reps / (start.elapsed_ms(end) / 1000.0)
+    # The last view's image both ways.
+    renderer.encode(None, tex, held[-1], bg)
+    renderer.afterSubmit()
+    same = bool(np.array_equal(tex.buffer.read(np.uint8), targets.read(np.uint8, offset=(n - 1) * W * H * 4)))
+    tex.destroy()
+    targets.destroy()
+    return {"views": n, "frames_per_s": round(batched, 1), "per_view_frames_per_s": round(per_view, 1),
+            "batch": tuned["batch"], "coop_min": tuned["coopMin"], "tuner_candidates": len(tuned["seconds"]),
+            "last_view_identical": same}
 
 
 def views_host(views):
@@ -378,10 +448,76 @@ def run_reference(args, rank, world, group):
     }
 
 
+def run_sort_stress(args, rank, local):
+    """Config 2 through the reference-structured TileRasterizer: tile counts, the
+    exclusive scan, 64-bit (tile, depth) keys, the 6-pass radix sort and the
+    ranges, each kernel timed with CUDA events; GB/s of the algorithmic bytes
+    against the measured HBM peak. (The keys, permutation and ranges are checked
+    bit for bit against the oracle by tests/test_gpu_configs.py.)"""
+    if rank != 0:
+        return None
+    from diorama_gb300 import Device, GaussianRenderer, TileRasterizer, scenes
+    import oracle
+
+    raw, sh, camera = scenes.config2(0)
+    act = scenes.activate64(raw).astype(np.float32)
+    device = Device(local)
+    r = GaussianRenderer(device)
+    r.setGaussians(act.reshape(-1), {"rest": sh.reshape(-1), "degree": 3})
+    r.encode(None, None, camera, (0, 0, 0))
+    r.afterSubmit()
+    cam = oracle.camera_array(camera.view, camera.proj, camera.viewport)
+    camera_buf = device.upload(cam)
+    n = act.shape[0]
+    tr = TileRasterizer(device, camera_buf, r.splatBuffer, n, r.tiles.pairCapacity)
+    for _ in range(max(args.warmup, 3)):
+        tr.encode(None, None, camera.viewport, (0, 0, 0))
+        tr.afterSubmit()
+    device.synchronize()
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    for _ in range(args.steps):
+        tr.encode(None, None, camera.viewport, (0, 0, 0))
+    device.synchronize()
+    report = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    keys = tr.lastPairCount
+    tiles = math.ceil(camera.viewport[0] / 16) * math.ceil(camera.viewport[1] / 16)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    per = {name: 1000 * t / c for name, (c, t) in report.items()}  # us per launch
+    launches = {name: c // args.steps for name, (c, _t) in report.items()}
+    sort_us = per.get("sort_histogram", 0) * launches.get("sort_histogram", 0) + \
+        per.get("sort_pass", 0) * launches.get("sort_pass", 0)
+    sort_bytes = 152.0 * keys  # 6 passes x (read + write 8 B key + 4 B value) + 8 B of histogram reads
+    scan_bytes = 8.0 * n
+    ranges_bytes = 8.0 * keys + 8.0 * tiles
+
+    def frac(b, us):
+        return {"gb_s": round(b / (us * 1e-6) / 1e9, 1), "frac_of_measured": round(b / (us * 1e-6) / 1e9 / hbm, 3),
+                "us": round(us, 2)}
+
+    result = {
+        "metric": "config 2 sort/scan/ranges", "workload": "config 2: 1.1M Gaussians in [-3,3]^3 at 1960x1090, "
+        "16x16 tiles, reference-structured tile stage", "keys": keys, "gaussians": n, "tiles": tiles,
+        "steps": args.steps, "peak_hbm_gbs": hbm,
+        "sort": frac(sort_bytes, sort_us), "scan": frac(scan_bytes, per.get("scan", 0.0)),
+        "find_ranges": frac(ranges_bytes, per.get("find_ranges", 0.0)),
+        "kernels": {k: {"avg_us": round(v, 2), "launches_per_frame": launches[k]} for k, v in per.items()},
+    }
+    tr.destroy()
+    camera_buf.destroy()
+    r.destroy()
+    device.destroy()
+    return result
+
+
 def main():
     args = parse()
     rank, world, local, group = dist_setup(args)
-    if args.impl == "reference":
+    if args.workload == "sort":
+        result = run_sort_stress(args, rank, local) if args.impl == "ours" else None
+    elif args.impl == "reference":
         result = run_reference(args, rank, world, group)
     else:
         result = run_ours(args, rank, world, local, group)
