@@ -13,13 +13,13 @@ from .gaussians import (FLOATS_PER_GAUSSIAN, FLOATS_PER_SPLAT, SH_REST_FLOATS, G
 from .gpu import Buffer, Device, Texture, initGpu, readBuffer
 from .primitives import PrefixSum, RadixSort
 from .renderer import CameraData, GaussianRenderer, SphericalHarmonics, TileRasterizer
-from .training import (DEFAULT_SETTINGS, MOMENT_SLOTS, Densification, RawGaussians, Trainer, TrainingLoss,
-                       TrainingSettings, TrainingView, activate)
+from .training import (DEFAULT_SETTINGS, MOMENT_SLOTS, Densification, DensifyMLP, RawGaussians, Trainer,
+                       TrainingLoss, TrainingSettings, TrainingView, activate)
 
 __all__ = [
     "DioramaError", "FLOATS_PER_GAUSSIAN", "FLOATS_PER_SPLAT", "SH_REST_FLOATS", "MOMENT_SLOTS", "Gaussian",
     "Splat2D", "packGaussians", "packSplats", "unpackSplats", "Buffer", "Device", "Texture", "initGpu", "readBuffer",
     "PrefixSum", "RadixSort", "CameraData", "GaussianRenderer", "SphericalHarmonics", "TileRasterizer",
-    "DEFAULT_SETTINGS", "Densification", "RawGaussians", "Trainer", "TrainingLoss", "TrainingSettings",
+    "DEFAULT_SETTINGS", "Densification", "DensifyMLP", "RawGaussians", "Trainer", "TrainingLoss", "TrainingSettings",
     "TrainingView", "activate",
 ]

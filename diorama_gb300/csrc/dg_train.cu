@@ -4,11 +4,14 @@
 // CUDA graph.
 #include "dg_common.cuh"
 #include "dg_loss.cuh"
+#include "dg_mlp.cuh"
 #include "dg_render.cuh"
 #include "dg_scan.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <unordered_map>
 
 namespace dg {
 namespace {
@@ -135,8 +138,12 @@ __global__ void reset_opacity_kernel(float* __restrict__ params, float2* __restr
 }
 
 // src/shaders/adam.wgsl:126-134
+// src/shaders/adam.wgsl:126-134. aux (the learned densification's extra
+// statistics) gets the sum of squared norms since the last densification and the
+// count of steps seen over the Gaussian's life.
 __global__ void stats_kernel(const AdamParams* __restrict__ ap, const float* __restrict__ splats,
-                             const float* __restrict__ splat_grads, float4* __restrict__ stats, uint32_t count) {
+                             const float* __restrict__ splat_grads, float4* __restrict__ stats,
+                             float2* __restrict__ aux, uint32_t count) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const float radius = splats[(size_t)i * FLOATS_PER_SPLAT + 3];
@@ -146,18 +153,23 @@ __global__ void stats_kernel(const AdamParams* __restrict__ ap, const float* __r
   const float len = sqrtf(gx * gx + gy * gy);
   const float4 s = stats[i];
   stats[i] = make_float4(s.x + len, s.y + 1.0f, fmaxf(s.z, radius), 0.0f);
+  const float2 a = aux[i];
+  aux[i] = make_float2(a.x + len * len, a.y + 1.0f);
 }
 
 // What happens to Gaussian i (src/shaders/densify.wgsl:72-85): 0 drop, 1 keep, 2 clone, 3 split.
+// With a veto (the learned proposal's), a candidate the model declined is kept
+// as it is, subject to the same pruning.
 __device__ __forceinline__ uint32_t densify_action(const DensifyParams& dp, const float* __restrict__ params,
-                                                   const float4* __restrict__ stats, uint32_t i) {
+                                                   const float4* __restrict__ stats, uint32_t i,
+                                                   const uint8_t* __restrict__ veto = nullptr) {
   const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
   const float4 s = stats[i];
   const float grad = s.y > 0.0f ? s.x / s.y : 0.0f;
   const float size = expf(fmaxf(p[4], fmaxf(p[5], p[6])));
   const float opacity = sigmoidf_(p[3]);
   auto removed = [&](float o, float sz) { return o < dp.min_opacity || (dp.max_size > 0.0f && sz > dp.max_size); };
-  if (grad >= dp.grad_threshold) {
+  if (grad >= dp.grad_threshold && !(veto && veto[i])) {
     if (size <= dp.clone_max_size) return removed(opacity, size) ? 0u : 2u;
     return removed(opacity, size / SPLIT_SHRINK) ? 0u : 3u;
   }
@@ -166,7 +178,8 @@ __device__ __forceinline__ uint32_t densify_action(const DensifyParams& dp, cons
 
 // src/shaders/densify.wgsl:96-107
 __global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, const float* __restrict__ params,
-                                                            const float4* __restrict__ stats, uint32_t count,
+                                                            const float4* __restrict__ stats,
+                                                            const uint8_t* __restrict__ veto, uint32_t count,
                                                             uint32_t* __restrict__ outputs,
                                                             uint32_t* __restrict__ counters) {
   __shared__ uint32_t local[4];
@@ -174,7 +187,7 @@ __global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, co
   __syncthreads();
   const uint32_t i = blockIdx.x * 256 + threadIdx.x;
   if (i < count) {
-    const uint32_t a = densify_action(dp, params, stats, i);
+    const uint32_t a = densify_action(dp, params, stats, i, veto);
     outputs[i] = a == 0 ? 0u : (a >= 2 ? 2u : 1u);
     atomicAdd(&local[a], 1u);
   }
@@ -194,20 +207,36 @@ __device__ __forceinline__ float unit_of(uint32_t h) { return ((float)(h >> 8u) 
 // one thread per (Gaussian, moment slot) and copies the Adam moments (kept for a
 // kept Gaussian and a clone's original, zero for new ones), the raw parameters
 // and the SH coefficients; densify_place_kernel then places split children.
+// The identity of each output Gaussian and its learned-densification statistics
+// travel along (slot 0's thread): a kept Gaussian and a clone's original keep
+// theirs, a new Gaussian gets identity first_id + its output index and zeros.
 __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
                                                            const float4* __restrict__ stats,
+                                                           const uint8_t* __restrict__ veto,
                                                            const float* __restrict__ sh,
                                                            const float2* __restrict__ moments,
+                                                           const uint32_t* __restrict__ ids,
+                                                           const float2* __restrict__ aux,
                                                            const uint32_t* __restrict__ outputs, uint32_t count,
-                                                           float* __restrict__ new_params, float* __restrict__ new_sh,
-                                                           float2* __restrict__ new_moments) {
+                                                           uint32_t first_id, float* __restrict__ new_params,
+                                                           float* __restrict__ new_sh,
+                                                           float2* __restrict__ new_moments,
+                                                           uint32_t* __restrict__ new_ids,
+                                                           float2* __restrict__ new_aux) {
   const uint32_t e = blockIdx.x * 256 + threadIdx.x;
   if (e >= count * MOMENT_SLOTS) return;
   const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
-  const uint32_t a = densify_action(dp, params, stats, i);
+  const uint32_t a = densify_action(dp, params, stats, i, veto);
   if (a == 0) return;
   const uint32_t o = outputs[i];
   const uint32_t copies = a == 1 ? 1u : 2u;
+  if (k == 0) {
+    for (uint32_t c = 0; c < copies; c++) {
+      const bool keep = (a == 1 || a == 2) && c == 0;
+      new_ids[o + c] = keep ? ids[i] : first_id + o + c;
+      new_aux[o + c] = make_float2(0.0f, keep ? aux[i].y : 0.0f);
+    }
+  }
   const float2 m = moments[e];
   const float2 zero = make_float2(0.f, 0.f);
   float value = 0.0f;
@@ -239,11 +268,12 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
 
 // Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and Box-Muller.
 __global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__ params,
-                                     const float4* __restrict__ stats, const uint32_t* __restrict__ outputs,
-                                     uint32_t count, float* __restrict__ new_params) {
+                                     const float4* __restrict__ stats, const uint8_t* __restrict__ veto,
+                                     const uint32_t* __restrict__ outputs, uint32_t count,
+                                     float* __restrict__ new_params) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  if (densify_action(dp, params, stats, i) != 3) return;
+  if (densify_action(dp, params, stats, i, veto) != 3) return;
   const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
   // rotation_matrix (src/shaders/gaussianMath.wgsl:13-25)
   float dot = p[8] * p[8];
@@ -280,6 +310,97 @@ __global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__
       out[row] = p[row] + v;
     }
   }
+}
+
+// The learned densification's inputs (see DG_MLP_FEATURES in the header),
+// for every Gaussian.
+struct FeatureParams {
+  float centroid[3];
+  float inv_extent, inv_threshold, inv_interval;
+  float iteration;
+};
+
+__global__ void densify_features_kernel(FeatureParams fp, const float* __restrict__ params,
+                                        const float4* __restrict__ stats, const float2* __restrict__ aux,
+                                        uint32_t count, float* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
+  const float4 s = stats[i];
+  const float2 a = aux[i];
+  const float n = fmaxf(s.y, 1.0f);
+  const float mean = s.y > 0.0f ? s.x / s.y : 0.0f;
+  const float var = s.y > 0.0f ? fmaxf(a.x / n - mean * mean, 0.0f) : 0.0f;
+  const float dx = p[0] - fp.centroid[0], dy = p[1] - fp.centroid[1], dz = p[2] - fp.centroid[2];
+  const float r = 0.5f + SH_C0 * p[12], g = 0.5f + SH_C0 * p[13], b = 0.5f + SH_C0 * p[14];
+  float* f = out + (size_t)i * 12;
+  f[0] = mean * fp.inv_threshold;
+  f[1] = s.y * fp.inv_interval;
+  f[2] = log1pf(s.z);
+  f[3] = p[4];
+  f[4] = p[5];
+  f[5] = p[6];
+  f[6] = sigmoidf_(p[3]);
+  f[7] = sqrtf(dx * dx + dy * dy + dz * dz) * fp.inv_extent;
+  f[8] = 0.299f * r + 0.587f * g + 0.114f * b;
+  f[9] = (fp.iteration - p[15]) * 1e-3f;
+  f[10] = a.y * 1e-3f;
+  f[11] = sqrtf(var) * fp.inv_threshold;
+}
+
+// The learned decision: a plain-rule candidate the model is confident about
+// (max(p, 1 - p) >= min_confidence) is vetoed when p < 0.5. tallies: scored,
+// confident, vetoed.
+__global__ void densify_veto_kernel(DensifyParams dp, const float* __restrict__ params,
+                                    const float4* __restrict__ stats, const float* __restrict__ survive,
+                                    float min_confidence, uint32_t count, uint8_t* __restrict__ veto,
+                                    unsigned long long* __restrict__ tallies) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  uint8_t v = 0;
+  if (densify_action(dp, params, stats, i) >= 2) {
+    const float p = survive[i];
+    atomicAdd(&tallies[0], 1ull);
+    if (fmaxf(p, 1.0f - p) >= min_confidence) {
+      atomicAdd(&tallies[1], 1ull);
+      if (p < 0.5f) {
+        v = 1;
+        atomicAdd(&tallies[2], 1ull);
+      }
+    }
+  }
+  veto[i] = v;
+}
+
+// The densify log: each clone/split candidate's features and the identities of
+// its new children (a clone's copy; both halves of a split), and the identities
+// of the Gaussians dropped. Slots come from atomics; order does not matter.
+__global__ void densify_log_kernel(DensifyParams dp, const float* __restrict__ params,
+                                   const float4* __restrict__ stats, const uint8_t* __restrict__ veto,
+                                   const float* __restrict__ features, const uint32_t* __restrict__ ids,
+                                   const uint32_t* __restrict__ outputs, uint32_t count, uint32_t first_id,
+                                   float* __restrict__ log, uint32_t* __restrict__ dropped,
+                                   uint32_t* __restrict__ cursors) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const uint32_t a = densify_action(dp, params, stats, i, veto);
+  if (a == 0) {
+    dropped[atomicAdd(&cursors[1], 1u)] = ids[i];
+    return;
+  }
+  if (a < 2) return;
+  const uint32_t slot = atomicAdd(&cursors[0], 1u);
+  float* row = log + (size_t)slot * 14;
+  for (int k = 0; k < 12; k++) row[k] = features[(size_t)i * 12 + k];
+  const uint32_t o = outputs[i];
+  const uint32_t c0 = a == 2 ? first_id + o + 1 : first_id + o, c1 = a == 2 ? 0xffffffffu : first_id + o + 1;
+  row[12] = __uint_as_float(c0);
+  row[13] = __uint_as_float(c1);
+}
+
+__global__ void iota_kernel(uint32_t* __restrict__ out, uint32_t count) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) out[i] = i;
 }
 
 }  // namespace
@@ -320,6 +441,30 @@ struct dg_trainer {
              pixel_grads == o.pixel_grads;
     }
   } graph_key{};
+  // Learned densification. Every Gaussian has an identity (children get fresh
+  // ones) and aux statistics (float2: squared gradient norms since the last
+  // densification, steps seen over its life).
+  dg_buffer* ids = nullptr;
+  dg_buffer* aux = nullptr;
+  uint32_t next_id = 0;
+  float centroid[3] = {0.0f, 0.0f, 0.0f};  // of the training cameras
+  dg_densify_mlp* mlp = nullptr;
+  float mlp_confidence = 0.6f;
+  uint64_t mlp_tallies[3] = {0, 0, 0};  // scored, confident, vetoed
+  // The densify log: samples wait until their horizon; a child dropped before it
+  // counts against its sample.
+  bool log_enabled = false;
+  uint32_t log_horizon = 1000;
+  struct Pending {
+    float features[12];
+    uint32_t children[2];
+    uint32_t due, alive;
+    bool resolved;
+  };
+  std::vector<Pending> pending;
+  std::unordered_map<uint32_t, uint32_t> tracked;  // child identity -> pending index
+  std::vector<float> done_features;
+  std::vector<uint8_t> done_labels;
 };
 
 namespace dg {
@@ -352,7 +497,7 @@ static dg_status launch_stats(dg_trainer* t) {
   DG_LAUNCH(t->ctx, "stats",
             stats_kernel<<<ceil_div(t->count, 256), 256, 0, t->ctx->stream>>>(
                 typed<AdamParams>(t->adam_params), typed<float>(r->splats), typed<float>(r->grad_splats),
-                typed<float4>(t->stats), t->count));
+                typed<float4>(t->stats), typed<float2>(t->aux), t->count));
   return DG_OK;
 }
 
@@ -422,6 +567,37 @@ static dg_status run_graph_step(dg_trainer* t) {
 
 static dg_status storage(dg_trainer* t, size_t bytes, dg_buffer** out) { return alloc_buffer(t->ctx, bytes, out); }
 
+// Labels the pending samples whose horizon has come (1: a child is still alive)
+// and drops resolved entries once they are most of the list.
+static void resolve_samples(dg_trainer* t) {
+  uint32_t resolved = 0;
+  for (auto& p : t->pending) {
+    if (!p.resolved && p.due <= t->iteration) {
+      p.resolved = true;
+      t->done_features.insert(t->done_features.end(), p.features, p.features + 12);
+      t->done_labels.push_back(p.alive > 0 ? 1 : 0);
+      for (uint32_t c : p.children)
+        if (c != 0xffffffffu) t->tracked.erase(c);
+    }
+    resolved += p.resolved;
+  }
+  if (resolved > 1024 && 2 * resolved > t->pending.size()) {
+    std::vector<dg_trainer::Pending> keep;
+    for (auto& p : t->pending)
+      if (!p.resolved) keep.push_back(p);
+    t->pending.swap(keep);
+    t->tracked.clear();
+    for (uint32_t k = 0; k < t->pending.size(); k++)
+      for (uint32_t c : t->pending[k].children)
+        if (c != 0xffffffffu) t->tracked[c] = k;
+  }
+}
+
+// The camera center of a column-major world-to-camera matrix: -R^T t.
+static void camera_center(const float* view, float* out) {
+  for (int j = 0; j < 3; j++) out[j] = -(view[j * 4 + 0] * view[12] + view[j * 4 + 1] * view[13] + view[j * 4 + 2] * view[14]);
+}
+
 }  // namespace dg
 
 extern "C" {
@@ -486,6 +662,18 @@ dg_status dg_trainer_create(dg_context* ctx, const float* params, const float* s
   if (st == DG_OK) st = storage(t, (size_t)count * MOMENT_SLOTS * 8, &t->moments);
   if (st == DG_OK) st = storage(t, (size_t)count * 16, &t->stats);
   if (st == DG_OK) st = storage(t, sizeof(AdamParams), &t->adam_params);
+  if (st == DG_OK) st = storage(t, (size_t)count * 4, &t->ids);
+  if (st == DG_OK) st = storage(t, (size_t)count * 8, &t->aux);
+  if (st == DG_OK) {
+    iota_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(typed<uint32_t>(t->ids), count);
+    ctx->launches++;
+    t->next_id = count;
+    for (uint32_t k = 0; k < view_count; k++) {
+      float c[3];
+      camera_center(views[k].camera.view, c);
+      for (int j = 0; j < 3; j++) t->centroid[j] += c[j] / view_count;
+    }
+  }
   if (st == DG_OK) st = renderer_ensure_gradients(t->renderer);
   if (st != DG_OK) {
     dg_trainer_destroy(t);
@@ -565,50 +753,135 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   dp.min_opacity = (float)s.min_opacity;
   dp.max_size = prune_large ? (float)(0.1 * s.extent) : 0.0f;
   dp.seed = t->iteration;
+  std::vector<dg_buffer*> temps;
+  auto temp = [&](size_t bytes, dg_buffer** out) {
+    const dg_status st = alloc_buffer(ctx, std::max<size_t>(bytes, 16), out);
+    if (st == DG_OK) temps.push_back(*out);
+    return st;
+  };
+  auto release = [&]() {
+    for (dg_buffer* b : temps) free_buffer(b);
+    temps.clear();
+  };
+  dg_status st = DG_OK;
   dg_buffer *outputs = nullptr, *counters = nullptr, *scratch = nullptr;
-  DG_TRY(alloc_buffer(ctx, (size_t)count * 4 + 4, &outputs));  // + the scan total
-  DG_TRY(alloc_buffer(ctx, 16, &counters));
-  DG_TRY(alloc_buffer(ctx, scan_scratch_bytes(count), &scratch));
+  dg_buffer *features = nullptr, *survive = nullptr, *veto = nullptr, *tallies = nullptr;
+  if (st == DG_OK) st = temp((size_t)count * 4 + 4, &outputs);  // + the scan total
+  if (st == DG_OK) st = temp(16, &counters);
+  if (st == DG_OK) st = temp(scan_scratch_bytes(count), &scratch);
+  // The learned proposal's inputs, and its decision on the plain rule's candidates.
+  if (st == DG_OK && (t->log_enabled || t->mlp)) {
+    st = temp((size_t)count * 12 * 4, &features);
+    if (st == DG_OK) {
+      FeatureParams fp;
+      for (int j = 0; j < 3; j++) fp.centroid[j] = t->centroid[j];
+      fp.inv_extent = (float)(1.0 / s.extent);
+      fp.inv_threshold = (float)(1.0 / s.densify_grad_threshold);
+      fp.inv_interval = 1.0f / (float)std::max(1u, s.densify_interval);
+      fp.iteration = (float)t->iteration;
+      DG_LAUNCH(ctx, "densify_features",
+                densify_features_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+                    fp, typed<float>(t->params), typed<float4>(t->stats), typed<float2>(t->aux), count,
+                    typed<float>(features)));
+    }
+  }
+  if (st == DG_OK && t->mlp) {
+    st = temp((size_t)count * 4, &survive);
+    if (st == DG_OK) st = temp(count, &veto);
+    if (st == DG_OK) st = temp(24, &tallies);
+    if (st == DG_OK) st = mlp_predict_launch(t->mlp, typed<float>(features), count, typed<float>(survive));
+    if (st == DG_OK) {
+      DG_LAUNCH(ctx, "densify_veto",
+                densify_veto_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+                    dp, typed<float>(t->params), typed<float4>(t->stats), typed<float>(survive), t->mlp_confidence,
+                    count, typed<uint8_t>(veto), typed<unsigned long long>(tallies)));
+    }
+  }
+  if (st != DG_OK) {
+    release();
+    return st;
+  }
+  const uint8_t* veto_ptr = veto ? typed<uint8_t>(veto) : nullptr;
   DG_LAUNCH(ctx, "densify_count",
             densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<float4>(t->stats), count, typed<uint32_t>(outputs),
+                dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, count, typed<uint32_t>(outputs),
                 typed<uint32_t>(counters)));
   uint32_t* total_ptr = typed<uint32_t>(outputs) + count;
-  DG_TRY(scan_launch(ctx, typed<uint32_t>(outputs), count, nullptr, total_ptr, scratch->ptr));
+  st = scan_launch(ctx, typed<uint32_t>(outputs), count, nullptr, total_ptr, scratch->ptr);
   uint32_t readback[5];
-  DG_CUDA(cudaMemcpyAsync(readback, total_ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
-  DG_CUDA(cudaMemcpyAsync(readback + 1, counters->ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
-  DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  unsigned long long tally[3] = {0, 0, 0};
+  if (st == DG_OK) {
+    DG_CUDA(cudaMemcpyAsync(readback, total_ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    DG_CUDA(cudaMemcpyAsync(readback + 1, counters->ptr, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    if (tallies) DG_CUDA(cudaMemcpyAsync(tally, tallies->ptr, 24, cudaMemcpyDeviceToHost, ctx->stream));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  if (st != DG_OK) {
+    release();
+    return st;
+  }
   const uint32_t new_count = readback[0];
   if (new_count == 0) {
-    free_buffer(outputs);
-    free_buffer(counters);
-    free_buffer(scratch);
+    release();
     return fail(DG_ERROR_STATE, "Densification removed every Gaussian.");
   }
   if (new_count >= (1u << 26)) {
-    free_buffer(outputs);
-    free_buffer(counters);
-    free_buffer(scratch);
+    release();
     return fail(DG_ERROR_STATE, "Densification would exceed 2^26 Gaussians (Adam indexes slots with 32 bits).");
   }
+  for (int k = 0; k < 3; k++) t->mlp_tallies[k] += tally[k];
   t->densifications.push_back(
       {t->iteration, count, new_count, readback[2], readback[3], readback[4], readback[1]});
+  const uint32_t first_id = t->next_id;
+  // The log: candidates' features and new children, and the identities dropped.
+  const uint32_t candidates = readback[3] + readback[4], dropped_count = readback[1];
+  std::vector<float> log_rows;
+  std::vector<uint32_t> dropped_ids;
+  if (t->log_enabled) {
+    dg_buffer *log = nullptr, *dropped = nullptr, *cursors = nullptr;
+    st = temp((size_t)candidates * 14 * 4, &log);
+    if (st == DG_OK) st = temp((size_t)dropped_count * 4, &dropped);
+    if (st == DG_OK) st = temp(8, &cursors);
+    if (st == DG_OK) {
+      DG_LAUNCH(ctx, "densify_log",
+                densify_log_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+                    dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, typed<float>(features),
+                    typed<uint32_t>(t->ids), typed<uint32_t>(outputs), count, first_id, typed<float>(log),
+                    typed<uint32_t>(dropped), typed<uint32_t>(cursors)));
+      log_rows.resize((size_t)candidates * 14);
+      dropped_ids.resize(dropped_count);
+      if (candidates)
+        DG_CUDA(cudaMemcpyAsync(log_rows.data(), log->ptr, log_rows.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      if (dropped_count)
+        DG_CUDA(cudaMemcpyAsync(dropped_ids.data(), dropped->ptr, dropped_count * 4, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+    }
+  }
   dg_buffer *params = nullptr, *sh = nullptr, *moments = nullptr, *stats = nullptr, *gaussians = nullptr;
-  DG_TRY(storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &params));
-  DG_TRY(storage(t, (size_t)new_count * SH_REST_FLOATS * 4, &sh));
-  DG_TRY(storage(t, (size_t)new_count * MOMENT_SLOTS * 8, &moments));
-  DG_TRY(storage(t, (size_t)new_count * 16, &stats));
-  DG_TRY(storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &gaussians));
+  dg_buffer *ids = nullptr, *aux = nullptr;
+  if (st == DG_OK) st = storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &params);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * SH_REST_FLOATS * 4, &sh);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * MOMENT_SLOTS * 8, &moments);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * 16, &stats);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * FLOATS_PER_GAUSSIAN * 4, &gaussians);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * 4, &ids);
+  if (st == DG_OK) st = storage(t, (size_t)new_count * 8, &aux);
+  if (st != DG_OK) {
+    for (dg_buffer* b : {params, sh, moments, stats, gaussians, ids, aux}) free_buffer(b);
+    release();
+    return st;
+  }
   dg_renderer* r = t->renderer;
   const uint64_t elements = (uint64_t)count * MOMENT_SLOTS;
   DG_LAUNCH(ctx, "densify_copy",
             densify_copy_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<float4>(t->stats), typed<float>(r->sh), typed<float2>(t->moments),
-                typed<uint32_t>(outputs), count, typed<float>(params), typed<float>(sh), typed<float2>(moments)));
+                dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, typed<float>(r->sh),
+                typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),
+                count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
+                typed<uint32_t>(ids), typed<float2>(aux)));
   DG_LAUNCH(ctx, "densify_place",
             densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<float4>(t->stats), typed<uint32_t>(outputs), count,
+                dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, typed<uint32_t>(outputs), count,
                 typed<float>(params)));
   const uint64_t floats = (uint64_t)new_count * FLOATS_PER_GAUSSIAN;
   DG_LAUNCH(ctx, "activate",
@@ -616,13 +889,86 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
                 typed<float>(params), typed<float>(gaussians), new_count));
   // Hand the new set to the renderer; the old buffers go once the work above is done.
   drop_graph(t);
-  DG_TRY(dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree));
-  DG_TRY(renderer_ensure_gradients(r));
-  for (dg_buffer* b : {t->params, t->moments, t->stats, outputs, counters, scratch}) free_buffer(b);
+  st = dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree);
+  if (st == DG_OK) st = renderer_ensure_gradients(r);
+  if (t->log_enabled && st == DG_OK) {
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+    // Drops first (they happened before the new children existed), then the new samples.
+    for (uint32_t id : dropped_ids) {
+      auto it = t->tracked.find(id);
+      if (it == t->tracked.end()) continue;
+      dg_trainer::Pending& p = t->pending[it->second];
+      if (p.alive > 0) p.alive--;
+      t->tracked.erase(it);
+    }
+    for (uint32_t k = 0; k < candidates; k++) {
+      const float* row = log_rows.data() + (size_t)k * 14;
+      dg_trainer::Pending p{};
+      std::memcpy(p.features, row, 12 * 4);
+      std::memcpy(p.children, row + 12, 8);
+      p.due = t->iteration + t->log_horizon;
+      p.alive = p.children[1] == 0xffffffffu ? 1u : 2u;
+      p.resolved = false;
+      for (uint32_t c : p.children)
+        if (c != 0xffffffffu) t->tracked[c] = (uint32_t)t->pending.size();
+      t->pending.push_back(p);
+    }
+  }
+  resolve_samples(t);
+  for (dg_buffer* b : {t->params, t->moments, t->stats, t->ids, t->aux}) free_buffer(b);
+  release();
   t->params = params;
   t->moments = moments;
   t->stats = stats;
+  t->ids = ids;
+  t->aux = aux;
   t->count = new_count;
+  t->next_id = first_id + new_count;
+  return st;
+}
+
+dg_status dg_trainer_set_densify_log(dg_trainer* t, int32_t enabled, uint32_t horizon) {
+  DG_REQUIRE(t, "NULL argument");
+  t->log_enabled = enabled != 0;
+  t->log_horizon = horizon ? horizon : 1000;
+  return DG_OK;
+}
+
+dg_status dg_trainer_take_densify_samples(dg_trainer* t, float* features, uint8_t* labels, uint32_t capacity,
+                                          uint32_t* count, uint32_t* pending) {
+  DG_REQUIRE(t && count, "NULL argument");
+  resolve_samples(t);
+  const uint32_t have = (uint32_t)t->done_labels.size();
+  uint32_t waiting = 0;
+  for (const auto& p : t->pending) waiting += !p.resolved;
+  if (pending) *pending = waiting;
+  if (!features) {
+    *count = have;
+    return DG_OK;
+  }
+  DG_REQUIRE(labels, "NULL argument");
+  const uint32_t n = std::min(capacity, have);
+  std::memcpy(features, t->done_features.data(), (size_t)n * 12 * 4);
+  std::memcpy(labels, t->done_labels.data(), n);
+  t->done_features.erase(t->done_features.begin(), t->done_features.begin() + (size_t)n * 12);
+  t->done_labels.erase(t->done_labels.begin(), t->done_labels.begin() + n);
+  *count = n;
+  return DG_OK;
+}
+
+dg_status dg_trainer_set_densify_mlp(dg_trainer* t, dg_densify_mlp* mlp, float min_confidence) {
+  DG_REQUIRE(t, "NULL argument");
+  DG_REQUIRE(min_confidence >= 0.5f && min_confidence <= 1.0f, "min_confidence must be in [0.5, 1]");
+  t->mlp = mlp;
+  t->mlp_confidence = min_confidence;
+  return DG_OK;
+}
+
+dg_status dg_trainer_densify_mlp_stats(const dg_trainer* t, uint64_t* scored, uint64_t* confident, uint64_t* vetoed) {
+  DG_REQUIRE(t && scored && confident && vetoed, "NULL argument");
+  *scored = t->mlp_tallies[0];
+  *confident = t->mlp_tallies[1];
+  *vetoed = t->mlp_tallies[2];
   return DG_OK;
 }
 
@@ -753,7 +1099,7 @@ dg_status dg_trainer_destroy(dg_trainer* t) {
   drop_graph(t);
   dg_renderer_destroy(t->renderer);
   dg_training_loss_destroy(t->loss);
-  for (dg_buffer* b : {t->target, t->params, t->moments, t->stats, t->adam_params}) free_buffer(b);
+  for (dg_buffer* b : {t->target, t->params, t->moments, t->stats, t->adam_params, t->ids, t->aux}) free_buffer(b);
   delete t;
   return DG_OK;
 }

@@ -138,6 +138,64 @@ def _views_c(views) -> ctypes.Array:
     return arr
 
 
+MLP_FEATURES = 12
+MLP_PARAMS = 5122
+
+
+class DensifyMLP:
+    """The learned densification proposal's model: MLP 12 -> 64 -> 64 -> 2, GELU,
+    BF16 weights, FP32 accumulation, trained and run by hand-written tensor-core
+    kernels. No reference counterpart."""
+
+    def __init__(self, device: Device, seed: int = 0):
+        self.device = device
+        handle = c_void_p()
+        _lib.call("dg_densify_mlp_create", device.handle, seed, ctypes.byref(handle))
+        self.handle = handle
+
+    def train(self, features: np.ndarray, labels: np.ndarray, epochs: int = 5, batch: int = 1024,
+              lr: float = 1e-3, weightDecay: float = 0.01, seed: int = 0) -> list[float]:
+        """AdamW over shuffled minibatches; returns each epoch's mean cross-entropy."""
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, MLP_FEATURES)
+        y = np.ascontiguousarray(labels, np.uint8).reshape(-1)
+        assert f.shape[0] == y.size
+        losses = (c_double * epochs)()
+        _lib.call("dg_densify_mlp_train", self.handle, f.ctypes.data, y.ctypes.data, y.size, epochs, batch, lr,
+                  weightDecay, seed, losses)
+        return list(losses)
+
+    def predict(self, features: Buffer, count: int, survive: Buffer) -> None:
+        """survive[i] = P(candidate i's children survive), both device buffers."""
+        _lib.call("dg_densify_mlp_predict", self.handle, features.handle, count, survive.handle)
+
+    def predictHost(self, features: np.ndarray) -> np.ndarray:
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, MLP_FEATURES)
+        fb = self.device.upload(f)
+        out = self.device.createBuffer(max(4, f.shape[0] * 4))
+        self.predict(fb, f.shape[0], out)
+        p = out.read(np.float32)[: f.shape[0]].copy()
+        fb.destroy()
+        out.destroy()
+        return p
+
+    def weights(self) -> np.ndarray:
+        """MLP_PARAMS FP32 weights (W1 [12,64], b1, W2 [64,64], b2, W3 [64,2], b3)
+        followed by the 24 normalization values (mean, 1/deviation)."""
+        out = np.zeros(MLP_PARAMS + 2 * MLP_FEATURES, np.float32)
+        _lib.call("dg_densify_mlp_get_weights", self.handle, out.ctypes.data)
+        return out
+
+    def setWeights(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, np.float32).reshape(-1)
+        assert w.size == MLP_PARAMS + 2 * MLP_FEATURES
+        _lib.call("dg_densify_mlp_set_weights", self.handle, w.ctypes.data)
+
+    def destroy(self) -> None:
+        if self.handle:
+            _lib.call("dg_densify_mlp_destroy", self.handle)
+            self.handle = None
+
+
 class Trainer:
     """Trains Gaussians to match a set of photos, following the reference's loop."""
 
@@ -237,6 +295,39 @@ class Trainer:
     def setGraph(self, enabled: bool) -> None:
         """Replay each optimize() step as one captured CUDA graph."""
         _lib.call("dg_trainer_set_graph", self.handle, int(enabled))
+
+    # Learned densification (no reference counterpart; the reference densifies by
+    # its gradient threshold alone, which stays the fallback).
+    def setDensifyLog(self, enabled: bool, horizon: int = 1000) -> None:
+        """Log every clone/split candidate's features; each is labelled `horizon`
+        steps later by whether any of its new children is still alive."""
+        _lib.call("dg_trainer_set_densify_log", self.handle, int(enabled), horizon)
+
+    def takeDensifySamples(self) -> tuple[np.ndarray, np.ndarray, int]:
+        """The labelled samples so far (moved out of the log): features [n, 12],
+        labels [n] (0/1), and how many still wait for their horizon."""
+        n, pending = ctypes.c_uint32(), ctypes.c_uint32()
+        _lib.call("dg_trainer_take_densify_samples", self.handle, None, None, 0, ctypes.byref(n),
+                  ctypes.byref(pending))
+        features = np.zeros((n.value, MLP_FEATURES), np.float32)
+        labels = np.zeros(n.value, np.uint8)
+        if n.value:
+            _lib.call("dg_trainer_take_densify_samples", self.handle, features.ctypes.data, labels.ctypes.data,
+                      n.value, ctypes.byref(n), ctypes.byref(pending))
+        return features[: n.value], labels[: n.value], pending.value
+
+    def setDensifyMLP(self, mlp: "DensifyMLP | None", minConfidence: float = 0.6) -> None:
+        """Let the model decide the plain rule's clone/split candidates where it is
+        confident (max(p, 1 - p) >= minConfidence); None restores the plain rule."""
+        _lib.call("dg_trainer_set_densify_mlp", self.handle, mlp.handle if mlp is not None else None, minConfidence)
+        self._mlp = mlp
+
+    @property
+    def densifyMLPStats(self) -> dict:
+        scored, confident, vetoed = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        _lib.call("dg_trainer_densify_mlp_stats", self.handle, ctypes.byref(scored), ctypes.byref(confident),
+                  ctypes.byref(vetoed))
+        return {"scored": scored.value, "confident": confident.value, "vetoed": vetoed.value}
 
     def destroy(self) -> None:
         if self.handle:

@@ -43,6 +43,7 @@ typedef struct dg_tile_rasterizer dg_tile_rasterizer;
 typedef struct dg_renderer dg_renderer;
 typedef struct dg_training_loss dg_training_loss;
 typedef struct dg_trainer dg_trainer;
+typedef struct dg_densify_mlp dg_densify_mlp;
 
 /* CameraData (src/gaussianRenderer.ts:11-15): column-major view and proj, viewport in pixels. */
 typedef struct dg_camera {
@@ -295,6 +296,53 @@ dg_status dg_trainer_densification(const dg_trainer* t, uint32_t index, dg_densi
  * kernel directly. Results are identical either way. */
 dg_status dg_trainer_set_graph(dg_trainer* t, int32_t enabled);
 dg_status dg_trainer_destroy(dg_trainer* t);
+
+/* ---- Learned densification proposal. No reference counterpart: the reference
+ * densifies by its gradient threshold alone (src/shaders/densify.wgsl:72-85),
+ * which stays the fallback. A candidate's 12 features (DG_MLP_FEATURES):
+ *   0 mean view-space gradient norm / threshold   1 gradient samples / interval
+ *   2 log(1 + max screen radius)                  3-5 log-scales (raw)
+ *   6 opacity                                     7 distance to the training cameras' centroid / extent
+ *   8 luminance of the DC colour                  9 age in steps / 1000
+ *  10 steps seen over its life / 1000            11 std of the gradient norm samples / threshold */
+#define DG_MLP_FEATURES 12
+#define DG_MLP_PARAMS 5122
+/* The model: MLP 12 -> 64 -> 64 -> 2, GELU, BF16 weights, FP32 accumulation,
+ * He-initialized from seed. */
+dg_status dg_densify_mlp_create(dg_context* ctx, uint32_t seed, dg_densify_mlp** out);
+/* Trains on count labelled samples (host arrays: features [count][12], labels
+ * 0/1): sets the input normalization from their mean and deviation, then runs
+ * `epochs` shuffled passes of minibatches of `batch` with AdamW (lr,
+ * weight_decay). mean_loss (NULL or room for `epochs`) receives each epoch's mean
+ * cross-entropy. */
+dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
+                               uint32_t epochs, uint32_t batch, float lr, float weight_decay, uint32_t seed,
+                               double* mean_loss);
+/* survive[i] = P(the children of candidate i survive); device buffers holding
+ * features [count][12] and survive [count]. */
+dg_status dg_densify_mlp_predict(dg_densify_mlp* m, dg_buffer* features, uint32_t count, dg_buffer* survive);
+/* The model as DG_MLP_PARAMS FP32 weights (W1 [12][64], b1, W2 [64][64], b2,
+ * W3 [64][2], b3) followed by 24 normalization values (mean, 1/deviation). */
+dg_status dg_densify_mlp_get_weights(dg_densify_mlp* m, float* out);
+dg_status dg_densify_mlp_set_weights(dg_densify_mlp* m, const float* in);
+dg_status dg_densify_mlp_destroy(dg_densify_mlp* m);
+/* Logs, at each densification, every clone/split candidate's features with the
+ * identities of its children; a sample is labelled once `horizon` steps have
+ * passed: 1 if any of its children is still alive then. */
+dg_status dg_trainer_set_densify_log(dg_trainer* t, int32_t enabled, uint32_t horizon);
+/* Moves up to `capacity` labelled samples out of the log (features [n][12],
+ * labels [n]; features may be NULL to only count) and sets *count = n and
+ * *pending = the samples still waiting for their horizon. */
+dg_status dg_trainer_take_densify_samples(dg_trainer* t, float* features, uint8_t* labels, uint32_t capacity,
+                                          uint32_t* count, uint32_t* pending);
+/* Learned densification: the model scores the plain rule's clone/split
+ * candidates; one it is confident about (max(p, 1 - p) >= min_confidence) is
+ * densified if p >= 0.5 and kept as it is otherwise; the rest follow the plain
+ * rule. NULL restores the plain rule. The trainer does not own the model. */
+dg_status dg_trainer_set_densify_mlp(dg_trainer* t, dg_densify_mlp* mlp, float min_confidence);
+/* Totals over the learned densifications: candidates scored, confident ones,
+ * and of those the ones not densified. */
+dg_status dg_trainer_densify_mlp_stats(const dg_trainer* t, uint64_t* scored, uint64_t* confident, uint64_t* vetoed);
 
 #ifdef __cplusplus
 }
