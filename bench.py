@@ -57,9 +57,15 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
-    ap.add_argument("--workload", default="train", choices=["train", "sort"],
+    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify"],
                     help="train: the headline training step; sort: config 2's sort/scan/ranges stress "
-                         "(1.1M Gaussians at 1960x1090, ~12M 64-bit keys, the reference's 6-pass sort)")
+                         "(1.1M Gaussians at 1960x1090, the reference's 6-pass sort); densify: config 1/4, "
+                         "plain vs learned densification on the planes-and-boxes scene (minutes)")
+    ap.add_argument("--train-steps", type=int, default=30_000, help="densify workload: steps per training run")
+    ap.add_argument("--plain-runs", type=int, default=3, help="densify workload: seeded plain runs that log labels")
+    ap.add_argument("--unbalanced", action="store_true",
+                    help="densify workload: plain cross-entropy (by default both labels weigh the same: ~98%% of "
+                         "children survive, and unweighted the model only learns that)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     return args
@@ -512,11 +518,142 @@ def run_sort_stress(args, rank, local):
     return result
 
 
+def run_densify_experiment(args, rank, local):
+    """Configs 1 and 4: the planes-and-boxes scene (500k ground-truth Gaussians,
+    263 training and 37 held-out 980x545 views), trained from 100k noisy surface
+    samples. Seeded plain runs log each clone/split candidate's features and
+    whether its children survive pruning 1,000 steps later; the model (MLP 12 ->
+    64 -> 64 -> 2, BF16, AdamW lr 1e-3, 5 epochs) learns from those labels; then a
+    plain and a learned run from the same start are compared on held-out PSNR and
+    SSIM, Gaussian count, training wall time and time to reach the plain run's
+    final held-out PSNR minus 0.1 dB (first reached, and for good: the opacity
+    resets every 3,000 steps pull the PSNR down until densification ends)."""
+    if rank != 0:
+        return None
+    from diorama_gb300 import (DEFAULT_SETTINGS, DensifyMLP, Device, GaussianRenderer, RawGaussians, Trainer,
+                               TrainingView, activate, scenes)
+
+    device = Device(local)
+    truth_raw, truth_sh = scenes.surface_scene(GROUND_TRUTH, TRUTH_SEED)
+    train_cams, held_cams = scenes.ring_cameras()
+    W, H = train_cams[0].viewport
+    photographer = GaussianRenderer(device)
+    photographer.setGaussians(activate(truth_raw), {"rest": truth_sh.reshape(-1), "degree": 3})
+
+    def photos(cams, prefix):
+        out = []
+        for k, cam in enumerate(cams):
+            tex = device.createTexture(W, H)
+            photographer.encode(None, tex, cam, (0, 0, 0))
+            out.append(TrainingView(f"{prefix} {k}", cam, tex))
+        return out
+
+    train_views, held_views = photos(train_cams, "train"), photos(held_cams, "held-out")
+    device.synchronize()
+    photographer.destroy()
+    settings = replace(DEFAULT_SETTINGS, extent=4.0, opacityLr=0.05)
+    steps = args.train_steps
+    every = max(100, steps // 30)
+
+    def run(seed, mlp=None, log=False):
+        raw, sh = scenes.surface_scene(100_000, seed, noise=0.01)
+        t = Trainer(device, RawGaussians(raw.reshape(-1), sh.reshape(-1)), train_views, settings)
+        t.setGraph(True)
+        if log:
+            t.setDensifyLog(True, 1000)
+        if mlp is not None:
+            t.setDensifyMLP(mlp, 0.6)
+        curve, train_s = [], 0.0
+        done = 0
+        while done < steps:
+            n = min(every, steps - done)
+            device.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(n):
+                t.step()
+            device.synchronize()
+            train_s += time.perf_counter() - t0
+            done += n
+            curve.append({"step": done, "train_s": round(train_s, 3), "psnr": round(t.evaluate(held_views, False)["psnr"], 3),
+                          "gaussians": t.count})
+        final = t.evaluate(held_views, True)
+        start = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            t.evaluate(held_views, False)
+        eval_fps = len(held_views) * reps / (time.perf_counter() - start)
+        result = {"seed": seed, "steps": steps, "train_s": round(train_s, 2), "steps_per_s": round(steps / train_s, 1),
+                  "psnr": round(final["psnr"], 3), "ssim": round(final["ssim"], 4), "gaussians": t.count,
+                  "densifications": len(t.densifications), "held_out_eval_frames_per_s": round(eval_fps, 1),
+                  "curve": curve}
+        samples = t.takeDensifySamples() if log else None
+        if mlp is not None:
+            result["mlp"] = t.densifyMLPStats
+        t.destroy()
+        return result, samples
+
+    logged, features, labels = [], [], []
+    for seed in range(1, args.plain_runs + 1):
+        result, (f, y, pending) = run(seed, log=True)
+        logged.append({k: result[k] for k in ("seed", "psnr", "ssim", "gaussians", "train_s")} |
+                      {"samples": int(y.size), "survived": float(y.mean()) if y.size else None, "unlabelled": pending})
+        features.append(f)
+        labels.append(y)
+    features, labels = np.concatenate(features), np.concatenate(labels)
+    mlp = DensifyMLP(device, seed=7)
+    t0 = time.perf_counter()
+    losses = mlp.train(features, labels, epochs=5, batch=1024, lr=1e-3, weightDecay=0.01, seed=7,
+                       balanceClasses=not args.unbalanced)
+    device.synchronize()
+    train_mlp_s = time.perf_counter() - t0
+    accuracy = float(np.mean((mlp.predictHost(features) >= 0.5) == (labels == 1)))
+    eval_seed = args.plain_runs + 1
+    plain, _ = run(eval_seed)
+    learned, _ = run(eval_seed, mlp=mlp)
+    target = plain["psnr"] - 0.1
+
+    def time_to(curve):
+        for c in curve:
+            if c["psnr"] >= target:
+                return c["train_s"]
+        return None
+
+    def time_to_sustained(curve):
+        # From the first evaluation after which the PSNR never drops below the target.
+        at = None
+        for c in curve:
+            if c["psnr"] < target:
+                at = None
+            elif at is None:
+                at = c["train_s"]
+        return at
+
+    for r in (plain, learned):
+        r["time_to_target_s"] = time_to(r["curve"])
+        r["time_to_sustained_target_s"] = time_to_sustained(r["curve"])
+    mlp.destroy()
+    for v in train_views + held_views:
+        v.image.destroy()
+    device.destroy()
+    return {
+        "metric": "time to held-out PSNR, learned vs plain densify", "unit": "s",
+        "workload": "configs 1/4: planes-and-boxes scene (500k ground truth), 263 + 37 views at 980x545, "
+                    f"{steps} steps from 100k noisy surface samples", "target_psnr": round(target, 3),
+        "plain_runs_logged": logged, "samples": int(labels.size), "survived_rate": float(labels.mean()),
+        "mlp": {"epochs": 5, "batch": 1024, "lr": 1e-3, "weight_decay": 0.01, "balanced_classes": not args.unbalanced,
+                "losses": [round(x, 5) for x in losses],
+                "train_accuracy": round(accuracy, 4), "train_s": round(train_mlp_s, 3)},
+        "plain": plain, "learned": learned,
+    }
+
+
 def main():
     args = parse()
     rank, world, local, group = dist_setup(args)
     if args.workload == "sort":
         result = run_sort_stress(args, rank, local) if args.impl == "ours" else None
+    elif args.workload == "densify":
+        result = run_densify_experiment(args, rank, local) if args.impl == "ours" else None
     elif args.impl == "reference":
         result = run_reference(args, rank, world, group)
     else:

@@ -197,11 +197,14 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_predict_kernel(const float* _
 }
 
 // Forward and backward over `batch` samples order[first..first+batch): adds the
-// mean cross-entropy's gradients to grads (master layout) and its sum to loss.
+// gradients of the mean cross-entropy, each sample weighted by its class's
+// weight (class_weight.x for label 0, .y for 1), to grads (master layout) and
+// the unweighted cross-entropy's sum to loss.
 __global__ void __launch_bounds__(MLP_THREADS) mlp_train_kernel(
     const float* __restrict__ features, const uint8_t* __restrict__ labels, const uint32_t* __restrict__ order,
-    uint32_t first, uint32_t batch, const float* __restrict__ norm, const __nv_bfloat16* __restrict__ packed,
-    const float* __restrict__ master, float* __restrict__ grads, float* __restrict__ loss) {
+    uint32_t first, uint32_t batch, float2 class_weight, const float* __restrict__ norm,
+    const __nv_bfloat16* __restrict__ packed, const float* __restrict__ master, float* __restrict__ grads,
+    float* __restrict__ loss) {
   // Transposed copies for the weight gradients: [feature][sample of the CTA].
   __shared__ __align__(16) __nv_bfloat16 s_xt[IN_PAD][ROWS];
   __shared__ __align__(16) __nv_bfloat16 s_a1t[HID][ROWS];
@@ -230,12 +233,13 @@ __global__ void __launch_bounds__(MLP_THREADS) mlp_train_kernel(
       const uint32_t r = w_first + g + 8 * h;
       if (r < end) {
         const float y = labels[order[r]] ? 1.0f : 0.0f;
+        const float wy = (y > 0.5f ? class_weight.y : class_weight.x) * inv_batch;
         const float m = fmaxf(z3[2 * h], z3[2 * h + 1]);
         const float e0 = expf(z3[2 * h] - m), e1 = expf(z3[2 * h + 1] - m);
         const float p1 = e1 / (e0 + e1);
         atomicAdd(loss, -logf(fmaxf(y > 0.5f ? p1 : 1.0f - p1, 1e-30f)));
-        d3[2 * h] = ((1.0f - p1) - (1.0f - y)) * inv_batch;
-        d3[2 * h + 1] = (p1 - y) * inv_batch;
+        d3[2 * h] = ((1.0f - p1) - (1.0f - y)) * wy;
+        d3[2 * h + 1] = (p1 - y) * wy;
       }
     }
   }
@@ -534,11 +538,13 @@ dg_status dg_densify_mlp_create(dg_context* ctx, uint32_t seed, dg_densify_mlp**
 
 // Trains on count labelled samples (features[count][12], labels 0/1, host arrays):
 // the input normalization is set from the samples' mean and standard deviation,
-// then `epochs` shuffled passes of minibatches of `batch` with AdamW. mean_loss
-// receives each epoch's mean cross-entropy (room for `epochs` values; may be NULL).
+// then `epochs` shuffled passes of minibatches of `batch` with AdamW. With
+// balance_classes, each class's samples weigh count / (2 * its size), so both
+// classes count equally. mean_loss receives each epoch's mean cross-entropy
+// (room for `epochs` values; may be NULL).
 dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
-                               uint32_t epochs, uint32_t batch, float lr, float weight_decay, uint32_t seed,
-                               double* mean_loss) {
+                               uint32_t epochs, uint32_t batch, float lr, float weight_decay, int32_t balance_classes,
+                               uint32_t seed, double* mean_loss) {
   DG_REQUIRE(m && features && labels, "NULL argument");
   DG_REQUIRE(count > 0 && epochs > 0 && batch > 0, "nothing to train on");
   dg_context* ctx = m->ctx;
@@ -557,6 +563,13 @@ dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const u
     m->norm_host[IN + k] = (float)(1.0 / std::sqrt(var[k] / count + 1e-12));
   }
   DG_TRY(write_async(ctx, m->norm->ptr, m->norm_host.data(), 2 * IN * 4));
+  uint64_t positives = 0;
+  for (uint32_t i = 0; i < count; i++) positives += labels[i] != 0;
+  float2 class_weight = make_float2(1.0f, 1.0f);
+  if (balance_classes && positives > 0 && positives < count) {
+    class_weight.x = (float)((double)count / (2.0 * (double)(count - positives)));
+    class_weight.y = (float)((double)count / (2.0 * (double)positives));
+  }
   dg_buffer *f = nullptr, *l = nullptr, *order = nullptr;
   DG_TRY(alloc_buffer(ctx, (size_t)count * IN * 4, &f));
   DG_TRY(alloc_buffer(ctx, count, &l));
@@ -577,7 +590,8 @@ dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const u
       const float bc1 = 1.0f - std::pow(0.9f, (float)m->steps), bc2 = 1.0f - std::pow(0.999f, (float)m->steps);
       DG_LAUNCH(ctx, "mlp_train",
                 mlp_train_kernel<<<ceil_div(n, ROWS), MLP_THREADS, 0, ctx->stream>>>(
-                    typed<float>(f), typed<uint8_t>(l), typed<uint32_t>(order), first, n, typed<float>(m->norm),
+                    typed<float>(f), typed<uint8_t>(l), typed<uint32_t>(order), first, n, class_weight,
+                    typed<float>(m->norm),
                     typed<__nv_bfloat16>(m->packed), typed<float>(m->master), typed<float>(m->grads),
                     typed<float>(m->loss)));
       DG_LAUNCH(ctx, "mlp_adamw",

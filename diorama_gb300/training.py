@@ -154,14 +154,15 @@ class DensifyMLP:
         self.handle = handle
 
     def train(self, features: np.ndarray, labels: np.ndarray, epochs: int = 5, batch: int = 1024,
-              lr: float = 1e-3, weightDecay: float = 0.01, seed: int = 0) -> list[float]:
-        """AdamW over shuffled minibatches; returns each epoch's mean cross-entropy."""
+              lr: float = 1e-3, weightDecay: float = 0.01, seed: int = 0, balanceClasses: bool = False) -> list[float]:
+        """AdamW over shuffled minibatches (balanceClasses: both labels weigh the
+        same in the loss); returns each epoch's mean cross-entropy."""
         f = np.ascontiguousarray(features, np.float32).reshape(-1, MLP_FEATURES)
         y = np.ascontiguousarray(labels, np.uint8).reshape(-1)
         assert f.shape[0] == y.size
         losses = (c_double * epochs)()
         _lib.call("dg_densify_mlp_train", self.handle, f.ctypes.data, y.ctypes.data, y.size, epochs, batch, lr,
-                  weightDecay, seed, losses)
+                  weightDecay, int(balanceClasses), seed, losses)
         return list(losses)
 
     def predict(self, features: Buffer, count: int, survive: Buffer) -> None:

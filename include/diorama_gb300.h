@@ -313,11 +313,11 @@ dg_status dg_densify_mlp_create(dg_context* ctx, uint32_t seed, dg_densify_mlp**
 /* Trains on count labelled samples (host arrays: features [count][12], labels
  * 0/1): sets the input normalization from their mean and deviation, then runs
  * `epochs` shuffled passes of minibatches of `batch` with AdamW (lr,
- * weight_decay). mean_loss (NULL or room for `epochs`) receives each epoch's mean
- * cross-entropy. */
+ * weight_decay). balance_classes weighs each class by count / (2 * its size).
+ * mean_loss (NULL or room for `epochs`) receives each epoch's mean cross-entropy. */
 dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
-                               uint32_t epochs, uint32_t batch, float lr, float weight_decay, uint32_t seed,
-                               double* mean_loss);
+                               uint32_t epochs, uint32_t batch, float lr, float weight_decay, int32_t balance_classes,
+                               uint32_t seed, double* mean_loss);
 /* survive[i] = P(the children of candidate i survive); device buffers holding
  * features [count][12] and survive [count]. */
 dg_status dg_densify_mlp_predict(dg_densify_mlp* m, dg_buffer* features, uint32_t count, dg_buffer* survive);
