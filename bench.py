@@ -176,7 +176,15 @@ def build_scene(args):
     return raw, sh, truth_raw, truth_sh, train_cams[: args.views]
 
 
-# Algorithmic bytes per unit (DESIGN.md): what each kernel must move at minimum.
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one
+# `ncu --set full --clock-control none` capture of each kernel at 1.1M Gaussians
+# (`python bench.py --steps 2 --warmup 3 --views 8 --no-cpu-baseline --no-graph
+# --no-held-out`, one launch, `-k regex:<kernel> -s 3 -c 1`).
+NCU_TRAFFIC = {"adam_sh": 1_493_375_488, "adam_param": 722_076_416, "preprocess_backward": 590_148_608,
+               "preprocess": 134_020_864}
+
+
+# Algorithmic bytes per unit: what each kernel must move at minimum.
 def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6) -> float | None:
     return {
         # Trainable slots x (read p, g, m, v: 16 B; write p, m, v: 12 B): 45 SH slots, then
@@ -311,7 +319,7 @@ def run_ours(args, rank, world, local, group):
         roofline = {"kernel": dom_mem, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 3), "peak_source": peak_source,
                     "algorithmic_bytes_per_launch": by, "launches_per_step": launches_per_step,
-                    "traffic": None}
+                    "traffic": NCU_TRAFFIC.get(dom_mem) if n == 1_100_000 else None}
     blend = {}
     for k in ("rasterize", "rasterize_backward"):
         if k in kernels:
