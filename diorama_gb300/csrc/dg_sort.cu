@@ -36,6 +36,7 @@ constexpr uint32_t FLAG_MASK = 3u << 30;
 constexpr uint32_t VALUE_MASK = (1u << 30) - 1;
 constexpr int HIST_THREADS = 256;
 constexpr int MAX_PASSES = 8;
+constexpr int LOOK_WIDTH = 4;  // predecessors read per look-back step
 
 template <int KW>
 struct KeyOf;
@@ -179,24 +180,35 @@ __global__ void __launch_bounds__(SORT_THREADS, 3)
   const uint32_t global_start = block_exclusive_256(pass_hist[d], s_tmp);
   s_block_start[d] = block_start;
 
-  // Decoupled look-back over earlier tiles, for this thread's digit.
+  // Decoupled look-back over earlier tiles, for this thread's digit: the states
+  // of LOOK_WIDTH predecessors are read together (one round trip instead of
+  // LOOK_WIDTH), then taken in order back to the first inclusive prefix.
   uint32_t prefix = 0;
   if (tile > 0) {
     int32_t look = (int32_t)tile - 1;
     uint32_t spins = 0;
-    while (look >= 0) {
-      uint32_t s = load_status(&status[look * RADIX + d]);
-      while ((s & FLAG_MASK) == 0) {
-        if (++spins > SPIN_LIMIT) {
-          atomicOr(error, DEVICE_ERROR_SORT_WAIT);
-          s = FLAG_PREFIX;  // give up: the order is wrong, but nothing hangs
-          break;
+    bool found = false;
+    while (look >= 0 && !found) {
+      uint32_t st[LOOK_WIDTH];
+#pragma unroll
+      for (int k = 0; k < LOOK_WIDTH; k++)
+        st[k] = look - k >= 0 ? load_status(&status[(look - k) * RADIX + d]) : FLAG_PREFIX;
+#pragma unroll
+      for (int k = 0; k < LOOK_WIDTH; k++) {
+        if (found || look - k < 0) break;
+        uint32_t s = st[k];
+        while ((s & FLAG_MASK) == 0) {
+          if (++spins > SPIN_LIMIT) {
+            atomicOr(error, DEVICE_ERROR_SORT_WAIT);
+            s = FLAG_PREFIX;  // give up: the order is wrong, but nothing hangs
+            break;
+          }
+          s = load_status(&status[(look - k) * RADIX + d]);
         }
-        s = load_status(&status[look * RADIX + d]);
+        prefix += s & VALUE_MASK;
+        found = (s & FLAG_MASK) == FLAG_PREFIX;
       }
-      prefix += s & VALUE_MASK;
-      if ((s & FLAG_MASK) == FLAG_PREFIX) break;
-      look--;
+      look -= LOOK_WIDTH;
     }
     store_status(&status[tile * RADIX + d], FLAG_PREFIX | ((prefix + tile_count) & VALUE_MASK));
   }
