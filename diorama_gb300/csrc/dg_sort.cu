@@ -62,19 +62,54 @@ struct PassShifts {
   uint32_t shift[MAX_PASSES];
 };
 
-// Digit histograms of every pass from one read of the keys.
+// Digit histograms of every pass from one read of the keys. Each thread takes
+// HIST_ITEMS consecutive keys and counts runs of equal digits in a register,
+// adding a run to the CTA's shared histogram when the digit changes: a splat's
+// pairs sit next to each other with the same depth and nearby tiles, so runs are
+// common, and the lanes of a warp rarely land on one bin in the same instant.
+constexpr uint32_t HIST_ITEMS = 8;
+
 template <int KW>
 __global__ void __launch_bounds__(HIST_THREADS) sort_histogram_kernel(const typename KeyOf<KW>::type* __restrict__ keys,
                                                                       uint32_t capacity, const uint32_t* __restrict__ count,
                                                                       uint32_t passes, PassShifts shifts,
                                                                       uint32_t* __restrict__ hist) {
+  using K = typename KeyOf<KW>::type;
   __shared__ uint32_t s_hist[MAX_PASSES][RADIX];
   for (uint32_t i = threadIdx.x; i < passes * RADIX; i += HIST_THREADS) s_hist[i / RADIX][i % RADIX] = 0;
   __syncthreads();
   const uint32_t n = count ? min(*count, capacity) : capacity;
-  for (uint32_t i = blockIdx.x * HIST_THREADS + threadIdx.x; i < n; i += gridDim.x * HIST_THREADS) {
-    uint64_t key = keys[i];
-    for (uint32_t p = 0; p < passes; p++) atomicAdd(&s_hist[p][(key >> shifts.shift[p]) & 0xff], 1u);
+  const uint64_t stride = (uint64_t)gridDim.x * HIST_THREADS * HIST_ITEMS;
+  for (uint64_t base = ((uint64_t)blockIdx.x * HIST_THREADS + threadIdx.x) * HIST_ITEMS; base < n; base += stride) {
+    K k[HIST_ITEMS];
+    const uint64_t left = (uint64_t)n - base;
+    const uint32_t m = left < HIST_ITEMS ? (uint32_t)left : HIST_ITEMS;
+    if (m == HIST_ITEMS && (reinterpret_cast<uintptr_t>(keys + base) & 15) == 0) {
+      // 16-byte loads (base is a multiple of 8 keys: 32 or 64 bytes in).
+      const uint4* src = reinterpret_cast<const uint4*>(keys + base);
+#pragma unroll
+      for (uint32_t q = 0; q < HIST_ITEMS * sizeof(K) / 16; q++)
+        reinterpret_cast<uint4*>(k)[q] = src[q];
+    } else {
+#pragma unroll
+      for (uint32_t j = 0; j < HIST_ITEMS; j++) k[j] = j < m ? keys[base + j] : K(0);
+    }
+    for (uint32_t p = 0; p < passes; p++) {
+      uint32_t run_digit = (uint32_t)((uint64_t)k[0] >> shifts.shift[p]) & 0xffu, run = 1;
+#pragma unroll
+      for (uint32_t j = 1; j < HIST_ITEMS; j++) {
+        if (j >= m) break;
+        const uint32_t d = (uint32_t)((uint64_t)k[j] >> shifts.shift[p]) & 0xffu;
+        if (d == run_digit) {
+          run++;
+        } else {
+          atomicAdd(&s_hist[p][run_digit], run);
+          run_digit = d;
+          run = 1;
+        }
+      }
+      atomicAdd(&s_hist[p][run_digit], run);
+    }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < passes * RADIX; i += HIST_THREADS) {
@@ -271,7 +306,7 @@ dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32
   DG_CUDA(cudaMemsetAsync(scratch, 0, l.total, ctx->stream));
   PassShifts shifts{};
   for (uint32_t p = 0; p < plan.passes; p++) shifts.shift[p] = plan.shift[p];
-  uint32_t hist_blocks = std::min<uint32_t>(ceil_div(plan.capacity, HIST_THREADS * 16), (uint32_t)ctx->sm_count * 4);
+  uint32_t hist_blocks = std::min<uint32_t>(ceil_div(plan.capacity, HIST_THREADS * HIST_ITEMS * 4), (uint32_t)ctx->sm_count * 8);
   hist_blocks = std::max(1u, hist_blocks);
   DG_LAUNCH(ctx, "sort_histogram",
             sort_histogram_kernel<KW><<<hist_blocks, HIST_THREADS, 0, ctx->stream>>>(
