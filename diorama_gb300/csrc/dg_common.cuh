@@ -152,12 +152,10 @@ namespace dg {
 
 // e^x by Cody-Waite reduction x = n ln2 + r (|r| <= ln2/2), e^r from its Taylor
 // series to degree 7 by Horner's rule, and scaling by 2^n through the exponent
-// bits; results below the smallest normal float are 0. The blend's forward and
-// backward both use it, so their alpha tests agree exactly; its error is about
-// one ulp.
-__host__ __device__ __forceinline__ float exp_blend(float x) {
-  if (x < -87.0f) return 0.0f;
-  if (x > 88.0f) return INFINITY;
+// bits, for -87 <= x <= 88 (the blend calls it only on powers between a splat's
+// cutoff, above ln(1/255) - 1e-3, and 0). The blend's forward and backward both
+// use it, so their alpha tests agree exactly; its error is about one ulp.
+__host__ __device__ __forceinline__ float exp_blend_core(float x) {
   float n = rintf(x * 1.44269504088896341f);
   float r = fmaf(n, -0.693145751953125f, x);
   r = fmaf(n, -1.428606820309417232e-6f, r);
@@ -178,6 +176,13 @@ __host__ __device__ __forceinline__ float exp_blend(float x) {
   std::memcpy(&scale, &bits, 4);
 #endif
   return p * scale;
+}
+
+// exp_blend_core over the whole float range: 0 below -87, infinity above 88.
+__host__ __device__ __forceinline__ float exp_blend(float x) {
+  if (x < -87.0f) return 0.0f;
+  if (x > 88.0f) return INFINITY;
+  return exp_blend_core(x);
 }
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }

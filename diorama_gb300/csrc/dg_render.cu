@@ -476,7 +476,7 @@ struct PixelBlend {
     }
 #pragma unroll
     for (uint32_t u = 0; u < 4; u++) {
-      const float a = fminf(0.99f, st.color[e[u]].w * exp_blend(need[u] ? power[u] : 0.0f));
+      const float a = fminf(0.99f, st.color[e[u]].w * exp_blend_core(need[u] ? power[u] : 0.0f));
       alpha[u] = need[u] && a >= 1.0f / 255.0f ? a : 0.0f;
     }
     return true;

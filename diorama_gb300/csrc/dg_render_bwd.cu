@@ -3,7 +3,7 @@
 //
 // Compiled with the default --fmad=true: gradients only need to agree to rounding
 // (their tile sums meet through float atomics anyway). The arithmetic that decides
-// which splats a pixel blended (blend_power, exp_blend, the alpha product and its
+// which splats a pixel blended (blend_power, exp_blend_core, the alpha product and its
 // thresholds) is written with non-fusing intrinsics or explicit fmaf, so it makes
 // exactly the forward pass's decisions.
 #include "dg_render.cuh"
@@ -94,7 +94,7 @@ __device__ __forceinline__ BlendTerm blend_term(const WarpStage& st, uint32_t e,
   t.dy = cy - m.y;
   const float power = blend_power(q.x, q.y, q.z, t.dx, t.dy);
   const bool need = eligible && power >= q.w && power <= 0.0f;
-  t.G = exp_blend(need ? power : 0.0f);
+  t.G = exp_blend_core(need ? power : 0.0f);
   t.alpha = fminf(0.99f, __fmul_rn(st.color[e].w, t.G));
   t.blended = need && t.alpha >= 1.0f / 255.0f;
   return t;
@@ -126,7 +126,10 @@ struct PixelBackward {
   // Steps in front of a splat this pixel blended and writes its 9 gradient shares.
   __device__ __forceinline__ void shares(const BlendTerm& t, float4 q, float4 c, float* w) {
     const float alpha = t.alpha, G = t.G, dx = t.dx, dy = t.dy;
-    const float inv = __frcp_rn(1.0f - alpha);  // 1 / (1 - alpha), used twice
+    // 1 / (1 - alpha), used twice; the approximate reciprocal (~1 ulp) is plenty:
+    // a chunk's chain of divisions is at most CHUNK entries long.
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(1.0f - alpha));
     T = T * inv;
     bhx = na * ncx + (1.0f - na) * bhx;
     bhy = na * ncy + (1.0f - na) * bhy;
