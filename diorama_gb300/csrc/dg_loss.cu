@@ -9,8 +9,9 @@
 // once, and does the separable blurs in shared memory:
 //   ssim_kernel:     moments -> blur h -> blur v -> SSIM and its three partials
 //   gradient_kernel: partials -> blur h -> blur v -> dL/dpixel and the pixel loss
-// Sums run over the taps -5..5 in order and skip taps past the image, as the
-// WGSL does, so the values are the reference's float32 values.
+// Sums run over the taps -5..5 in order; taps past the image add exactly 0 (the
+// halo holds zeros there), the same as the WGSL's skipping them, so the values
+// are the reference's float32 values.
 //
 // The same ssim_kernel also measures held-out renders (PSNR and SSIM of the
 // 8-bit-quantized image, src/trainer.ts:371-386 and src/metrics.ts) on the GPU.
@@ -80,20 +81,18 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
   // Horizontal pass over every halo row, for the 16 output columns.
   for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
     const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    const int gy = y0 + row;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f;
-    if (gy >= 0 && gy < h) {
-      for (int t = -HALO; t <= HALO; t++) {
-        const int gx = blockIdx.x * LT + col + t;
-        if (gx < 0 || gx >= w) continue;
-        const float wt = win.w[t < 0 ? -t : t];
-        const float xv = s_x[row][col + HALO + t][ch], yv = s_y[row][col + HALO + t][ch];
-        a0 = a0 + wt * xv;
-        a1 = a1 + wt * yv;
-        a2 = a2 + wt * (xv * xv);
-        a3 = a3 + wt * (yv * yv);
-        a4 = a4 + wt * (xv * yv);
-      }
+    // Taps past the image read the halo's zeros and add exactly 0: the same sums
+    // as skipping them, without a branch per tap.
+#pragma unroll
+    for (int t = -HALO; t <= HALO; t++) {
+      const float wt = win.w[t < 0 ? -t : t];
+      const float xv = s_x[row][col + HALO + t][ch], yv = s_y[row][col + HALO + t][ch];
+      a0 = a0 + wt * xv;
+      a1 = a1 + wt * yv;
+      a2 = a2 + wt * (xv * xv);
+      a3 = a3 + wt * (yv * yv);
+      a4 = a4 + wt * (xv * yv);
     }
     s_h[0][row][col][ch] = a0;
     s_h[1][row][col][ch] = a1;
@@ -111,9 +110,8 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
       float m[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      for (int t = -HALO; t <= HALO; t++) {
-        const int yy = gy + t;
-        if (yy < 0 || yy >= h) continue;
+#pragma unroll
+      for (int t = -HALO; t <= HALO; t++) {  // rows past the image were blurred to 0
         const float wt = win.w[t < 0 ? -t : t];
 #pragma unroll
         for (int q = 0; q < 5; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
@@ -187,16 +185,12 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
   __syncthreads();
   for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
     const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    const int gy = y0 + row;
     float a[3] = {0.f, 0.f, 0.f};
-    if (gy >= 0 && gy < h) {
-      for (int t = -HALO; t <= HALO; t++) {
-        const int gx = blockIdx.x * LT + col + t;
-        if (gx < 0 || gx >= w) continue;
-        const float wt = win.w[t < 0 ? -t : t];
 #pragma unroll
-        for (int q = 0; q < 3; q++) a[q] = a[q] + wt * s_p[q][row][col + HALO + t][ch];
-      }
+    for (int t = -HALO; t <= HALO; t++) {  // the halo holds zeros past the image
+      const float wt = win.w[t < 0 ? -t : t];
+#pragma unroll
+      for (int q = 0; q < 3; q++) a[q] = a[q] + wt * s_p[q][row][col + HALO + t][ch];
     }
 #pragma unroll
     for (int q = 0; q < 3; q++) s_h[q][row][col][ch] = a[q];
@@ -217,9 +211,8 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
 #pragma unroll
   for (int ch = 0; ch < 3; ch++) {
     float m[3] = {0.f, 0.f, 0.f};
-    for (int t = -HALO; t <= HALO; t++) {
-      const int yy = gy + t;
-      if (yy < 0 || yy >= h) continue;
+#pragma unroll
+    for (int t = -HALO; t <= HALO; t++) {  // rows past the image were blurred to 0
       const float wt = win.w[t < 0 ? -t : t];
 #pragma unroll
       for (int q = 0; q < 3; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
