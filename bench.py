@@ -180,17 +180,16 @@ def build_scene(args):
 # `ncu --set full --clock-control none` capture of each kernel at 1.1M Gaussians
 # (`python bench.py --steps 2 --warmup 3 --views 8 --no-cpu-baseline --no-graph
 # --no-held-out`, one launch, `-k regex:<kernel> -s 3 -c 1`).
-NCU_TRAFFIC = {"adam_sh": 1_493_375_488, "adam_param": 722_076_416, "preprocess_backward": 590_148_608,
-               "preprocess": 134_020_864}
+NCU_TRAFFIC = {"preprocess": 134_020_864}
 
 
 # Algorithmic bytes per unit: what each kernel must move at minimum.
 def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6) -> float | None:
     return {
-        # Trainable slots x (read p, g, m, v: 16 B; write p, m, v: 12 B): 45 SH slots, then
-        # 14 Gaussian slots plus the 56 B of activated parameters.
-        "adam_sh": 1260.0 * n,
-        "adam_param": 448.0 * n,
+        # The preprocess backward fused with Adam: read the activated Gaussian 64, SH 180,
+        # splat gradients 36 and visibility 4, raw parameters 56 and moments 472 (59 used
+        # slots); write SH 180, parameters 56, moments 472 and activated values 56.
+        "preprocess_backward_adam": 1576.0 * n,
         "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
         "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
         "sort_pass": 24.0 * pairs,  # per pass: read and write 8 B key + 4 B value

@@ -143,6 +143,12 @@ const Camera* renderer_camera(dg_renderer* r);
 // The backward kernels (dg_render_bwd.cu).
 dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status launch_preprocess_backward(dg_renderer* r);
+struct AdamParams;
+// The training step's preprocess backward with Adam applied at once (the same
+// values as launch_preprocess_backward followed by the Adam kernels); with
+// keep_gradients the gradients are stored as well.
+dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam, float* params, float2* moments,
+                                         bool keep_gradients);
 // Batched views (dg_views.cu): renders count views in batches of `batch` into
 // targets (count rgba8 images, may be NULL) and pixel_colors (count vec4 images,
 // may be NULL).

@@ -6,6 +6,7 @@
 // which splats a pixel blended (blend_power, exp_blend_core, the alpha product and its
 // thresholds) is written with non-fusing intrinsics or explicit fmaf, so it makes
 // exactly the forward pass's decisions.
+#include "dg_adam.cuh"
 #include "dg_render.cuh"
 #include "dg_render_kernels.cuh"
 
@@ -302,19 +303,16 @@ __device__ __forceinline__ void copy_floats(float* __restrict__ dst, const float
 }
 
 // src/shaders/preprocessBackward.wgsl:28-181 for one Gaussian: the 16-float
-// Gaussian gradient (slots 7 and 15 zero) to gg, and the 45 SH gradients over
+// Gaussian gradient (slots 7 and 15 zero) to out, and the 45 SH gradients over
 // its 45 SH coefficients in shv (shared memory).
 __device__ __forceinline__ void preprocess_backward_one(const Camera& cam, uint32_t i, const float* __restrict__ gaussians,
                                                         float* shv, uint32_t basis_count,
                                                         const float* __restrict__ splats,
-                                                        const float* __restrict__ splat_grads, float* __restrict__ gg) {
-  float out[16];
+                                                        const float* __restrict__ splat_grads, float (&out)[16]) {
 #pragma unroll
   for (int k = 0; k < 16; k++) out[k] = 0.0f;
   const bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
   if (!visible) {
-#pragma unroll
-    for (int k = 0; k < 4; k++) reinterpret_cast<float4*>(gg)[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint32_t k = 0; k < SH_REST_FLOATS; k++) shv[k] = 0.0f;
     return;
   }
@@ -503,9 +501,12 @@ __device__ __forceinline__ void preprocess_backward_one(const Camera& cam, uint3
   out[12] = raw_grad[0];
   out[13] = raw_grad[1];
   out[14] = raw_grad[2];
+}
+
+__device__ __forceinline__ void store16(float* __restrict__ dst, const float (&v)[16]) {
 #pragma unroll
   for (int k = 0; k < 4; k++)
-    reinterpret_cast<float4*>(gg)[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+    reinterpret_cast<float4*>(dst)[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
 }
 
 // One thread per Gaussian. The CTA's SH coefficients are staged in shared memory
@@ -525,11 +526,116 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
   const uint32_t i = block_start + threadIdx.x;
-  if (i < count)
+  if (i < count) {
+    float out[16];
     preprocess_backward_one(s_cam, i, gaussians, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count, splats, splat_grads,
-                            gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN);
+                            out);
+    store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);
+  }
   __syncthreads();
   copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
+}
+
+// The training step's preprocess backward with Adam applied at once
+// (src/shaders/preprocessBackward.wgsl:28-181, then src/shaders/adam.wgsl:80-107):
+// the CTA computes its 128 Gaussians' gradients into shared memory (the SH
+// coefficients staged there turn into their gradients), then steps Adam over the
+// CTA's slots, one thread per slot, reading and writing the Gaussians' raw
+// parameters, SH coefficients, moment records and activated values as contiguous
+// runs: the 180 + 64 bytes of gradients per Gaussian never go to memory and back.
+// The same values as preprocess_backward_kernel followed by the Adam kernels.
+// gaussian_grads and sh_grads (may be NULL) also receive the gradients.
+__global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
+    const Camera* __restrict__ camera, float* __restrict__ gaussians, float* __restrict__ sh, uint32_t count,
+    const uint32_t* __restrict__ scene_params, const float* __restrict__ splats, const float* __restrict__ splat_grads,
+    const AdamParams* __restrict__ adam, float* __restrict__ params, float2* __restrict__ moments,
+    float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
+  constexpr uint32_t GP = FLOATS_PER_GAUSSIAN + 1;  // a row pitch prime to 32
+  __shared__ Camera s_cam;
+  __shared__ __align__(16) float s_sh[PBWD_THREADS * SH_REST_FLOATS];  // coefficients, then their gradients
+  __shared__ float s_pg[PBWD_THREADS * GP];                            // parameter gradients
+  __shared__ AdamParams s_ap;
+  load_camera(s_cam, camera);
+  if (threadIdx.x == 0) s_ap = *adam;
+  const uint32_t block_start = blockIdx.x * PBWD_THREADS;
+  const uint32_t here = min(PBWD_THREADS, count - block_start);
+  copy_floats(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  __syncthreads();
+  const uint32_t degree = scene_params[0];
+  const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
+  const uint32_t i = block_start + threadIdx.x;
+  if (i < count) {
+    float out[16];
+    preprocess_backward_one(s_cam, i, gaussians, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count, splats, splat_grads,
+                            out);
+#pragma unroll
+    for (int k = 0; k < 16; k++) s_pg[threadIdx.x * GP + k] = out[k];
+    if (gaussian_grads) store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);
+  }
+  __syncthreads();
+  if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
+  const AdamParams& ap = s_ap;
+  // The SH slots (moment slots 16-60 of each record): each thread loads a batch of
+  // slots before stepping them, so that enough reads are in flight to cover DRAM
+  // latency at this kernel's occupancy.
+  constexpr uint32_t SH_BATCH = 9;  // 45 slots per thread in a full CTA = 5 batches
+  float* sh_block = sh + (size_t)block_start * SH_REST_FLOATS;
+  float2* sh_moments = moments + (size_t)block_start * MOMENT_SLOTS + FLOATS_PER_GAUSSIAN;
+  const uint32_t sh_total = here * SH_REST_FLOATS;
+  for (uint32_t base = threadIdx.x; base < sh_total; base += PBWD_THREADS * SH_BATCH) {
+    float2 m[SH_BATCH];
+    float v[SH_BATCH];
+#pragma unroll
+    for (uint32_t u = 0; u < SH_BATCH; u++) {
+      const uint32_t e = base + u * PBWD_THREADS;
+      if (e < sh_total) {
+        const uint32_t g = e / SH_REST_FLOATS;
+        m[u] = sh_moments[(size_t)g * MOMENT_SLOTS + (e - g * SH_REST_FLOATS)];
+        v[u] = sh_block[e];
+      }
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < SH_BATCH; u++) {
+      const uint32_t e = base + u * PBWD_THREADS;
+      if (e < sh_total) {
+        const uint32_t g = e / SH_REST_FLOATS;
+        sh_block[e] = adam_step_fast(v[u], s_sh[e], m[u], ap.sh_lr, ap.inv_bias_correction1,
+                                     ap.inv_sqrt_bias_correction2);
+        sh_moments[(size_t)g * MOMENT_SLOTS + (e - g * SH_REST_FLOATS)] = m[u];
+      }
+    }
+  }
+  // The raw parameter slots (0-15 but 7 and 15) and their activated values, all
+  // of a thread's slots loaded at once (16 per thread in a full CTA).
+  constexpr uint32_t P_BATCH = 8;
+  float* p_block = params + (size_t)block_start * FLOATS_PER_GAUSSIAN;
+  float* a_block = gaussians + (size_t)block_start * FLOATS_PER_GAUSSIAN;
+  float2* p_moments = moments + (size_t)block_start * MOMENT_SLOTS;
+  const uint32_t p_total = here * FLOATS_PER_GAUSSIAN;
+  for (uint32_t base = threadIdx.x; base < p_total; base += PBWD_THREADS * P_BATCH) {
+    float2 m[P_BATCH];
+    float v[P_BATCH];
+#pragma unroll
+    for (uint32_t u = 0; u < P_BATCH; u++) {
+      const uint32_t e = base + u * PBWD_THREADS;
+      const uint32_t k = e & 15u;  // the same for every u: PBWD_THREADS is a multiple of 16
+      if (e < p_total && k != 7 && k != 15) {
+        m[u] = p_moments[(size_t)(e >> 4) * MOMENT_SLOTS + k];
+        v[u] = p_block[e];
+      }
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < P_BATCH; u++) {
+      const uint32_t e = base + u * PBWD_THREADS;
+      const uint32_t g = e >> 4, k = e & 15u;
+      if (e < p_total && k != 7 && k != 15) {
+        float act;
+        p_block[e] = adam_param_slot(ap, k, v[u], s_pg[g * GP + k], m[u], act);
+        p_moments[(size_t)g * MOMENT_SLOTS + k] = m[u];
+        a_block[e] = act;
+      }
+    }
+  }
 }
 
 
@@ -548,6 +654,17 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
                 typed<uint2>(tr->chunks), typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last),
                 typed<float4>(tr->checkpoints), typed<uint32_t>(tr->blend_mask), typed<float4>(pixel_grads),
                 typed<float>(splat_grads), counter));
+  return DG_OK;
+}
+
+dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam, float* params, float2* moments,
+                                         bool keep_gradients) {
+  DG_LAUNCH(r->ctx, "preprocess_backward_adam",
+            preprocess_backward_adam_kernel<<<ceil_div(r->count, PBWD_THREADS), PBWD_THREADS, 0, r->ctx->stream>>>(
+                typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
+                typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats), adam, params,
+                moments, keep_gradients ? typed<float>(r->grad_gaussians) : nullptr,
+                keep_gradients ? typed<float>(r->grad_sh) : nullptr));
   return DG_OK;
 }
 

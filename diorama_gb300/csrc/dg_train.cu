@@ -2,6 +2,7 @@
 // stream compaction (src/shaders/densify.wgsl), and the Trainer loop of
 // src/trainer.ts, with each optimize() step optionally replayed as one captured
 // CUDA graph.
+#include "dg_adam.cuh"
 #include "dg_common.cuh"
 #include "dg_loss.cuh"
 #include "dg_mlp.cuh"
@@ -21,15 +22,6 @@ constexpr float RESET_LOGIT = -4.59511985013459f;  // logit(0.01), src/shaders/a
 constexpr float SPLIT_SHRINK = 1.6f;
 constexpr float LOG_SPLIT_SHRINK = 0.470003629245735553f;  // ln 1.6
 
-// AdamParams (src/shaders/adam.wgsl:9-22)
-struct AdamParams {
-  float bias_correction1, bias_correction2;
-  float position_lr, opacity_lr, scale_lr, rotation_lr, color_lr, sh_lr;
-  float viewport[2];
-  // Reciprocals of the bias corrections (and of the second's square root), from the host.
-  float inv_bias_correction1, inv_sqrt_bias_correction2;
-};
-
 // DensifyParams (src/shaders/densify.wgsl:149-161)
 struct DensifyParams {
   float grad_threshold, clone_max_size, min_opacity, max_size;
@@ -44,76 +36,6 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
   if (k == 3) return sigmoidf_(raw);
   if (k >= 12 && k <= 14) return 0.5f + SH_C0 * raw;
   return raw;
-}
-
-// src/shaders/adam.wgsl:80-107 as two flat elementwise kernels over Adam's slots:
-// adam_sh_kernel over the 45 SH coefficients of every Gaussian (moment slots
-// 16-60) and adam_param_kernel over the 16 raw parameters (slots 0-15). Each
-// thread takes one slot, so parameters, gradients and moments are read in
-// consecutive runs and no thread waits on another. (One kernel over all 61 slots
-// of each moment record measured slower: its warps mix the two paths and seven
-// streams.) Slots 7 and 15 (padding, which holds densification stamps) are left
-// alone.
-//
-// The step uses the host's reciprocals of the bias corrections and approximate
-// square root and division: within a few ulps of
-// value - lr (m / bc1) / (sqrt(v / bc2) + eps).
-__device__ __forceinline__ float sqrt_approx(float x) {
-  float r;
-  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-
-__device__ __forceinline__ float adam_step_fast(float value, float grad, float2& m, float lr, float inv_bc1,
-                                                float inv_sqrt_bc2) {
-  m.x = 0.9f * m.x + 0.1f * grad;
-  m.y = 0.999f * m.y + 0.001f * grad * grad;
-  return value - __fdividef(lr * (m.x * inv_bc1), sqrt_approx(m.y) * inv_sqrt_bc2 + 1e-15f);
-}
-
-__global__ void __launch_bounds__(256) adam_sh_kernel(const AdamParams* __restrict__ ap, float* __restrict__ sh,
-                                                      float2* __restrict__ moments, const float* __restrict__ sgrad,
-                                                      uint32_t count) {
-  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
-  if (e >= count * SH_REST_FLOATS) return;
-  const uint32_t i = e / SH_REST_FLOATS, j = e - i * SH_REST_FLOATS;
-  const size_t slot = (size_t)i * MOMENT_SLOTS + FLOATS_PER_GAUSSIAN + j;
-  float2 m = moments[slot];
-  const float x = sh[e], g = sgrad[e];
-  sh[e] = adam_step_fast(x, g, m, ap->sh_lr, ap->inv_bias_correction1, ap->inv_sqrt_bias_correction2);
-  moments[slot] = m;
-}
-
-__global__ void __launch_bounds__(256) adam_param_kernel(const AdamParams* __restrict__ ap,
-                                                         float* __restrict__ params, float2* __restrict__ moments,
-                                                         const float* __restrict__ ggrad,
-                                                         float* __restrict__ gaussians, uint32_t count) {
-  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
-  if (e >= count * FLOATS_PER_GAUSSIAN) return;
-  const uint32_t i = e >> 4, k = e & 15u;
-  if (k == 7 || k == 15) return;
-  const size_t slot = (size_t)i * MOMENT_SLOTS + k;
-  float2 m = moments[slot];
-  const float x = params[e];
-  // The chain rule through the activation and the learning rate of slot k,
-  // without branches: the 16 slots of a Gaussian share a warp, and each would
-  // otherwise take its own path. One expf serves the sigmoid (k = 3) and the
-  // exponential (k = 4-6); the values equal the per-slot formulas bit for bit.
-  const bool opacity = k == 3, scale = k >= 4 && k <= 6, color = k >= 12;
-  const float ex = expf(opacity ? -x : x);
-  const float sig = 1.0f / (1.0f + ex);
-  const float g0 = ggrad[e];
-  const float grad = opacity ? g0 * sig * (1.0f - sig) : scale ? g0 * ex : color ? g0 * SH_C0 : g0;
-  const float lr = k < 3 ? ap->position_lr
-                 : opacity ? ap->opacity_lr
-                 : scale ? ap->scale_lr
-                 : color ? ap->color_lr
-                         : ap->rotation_lr;
-  const float next = adam_step_fast(x, grad, m, lr, ap->inv_bias_correction1, ap->inv_sqrt_bias_correction2);
-  params[e] = next;
-  moments[slot] = m;
-  const float ey = expf(opacity ? -next : next);
-  gaussians[e] = opacity ? 1.0f / (1.0f + ey) : scale ? ey : color ? 0.5f + SH_C0 * next : next;
 }
 
 // src/shaders/adam.wgsl:74-77, one thread per raw float.
@@ -431,6 +353,7 @@ struct dg_trainer {
   std::vector<dg_densification> densifications;
   // The captured optimize() step.
   bool graph_enabled = false;
+  bool keep_gradients = false;  // store the Gaussian gradients Adam consumes in registers
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_launches = 0;
   struct Key {
@@ -501,19 +424,6 @@ static dg_status launch_stats(dg_trainer* t) {
   return DG_OK;
 }
 
-static dg_status launch_adam(dg_trainer* t) {
-  dg_renderer* r = t->renderer;
-  DG_LAUNCH(t->ctx, "adam_sh",
-            adam_sh_kernel<<<ceil_div((uint64_t)t->count * SH_REST_FLOATS, 256), 256, 0, t->ctx->stream>>>(
-                typed<AdamParams>(t->adam_params), typed<float>(r->sh), typed<float2>(t->moments),
-                typed<float>(r->grad_sh), t->count));
-  DG_LAUNCH(t->ctx, "adam_param",
-            adam_param_kernel<<<ceil_div((uint64_t)t->count * FLOATS_PER_GAUSSIAN, 256), 256, 0, t->ctx->stream>>>(
-                typed<AdamParams>(t->adam_params), typed<float>(t->params), typed<float2>(t->moments),
-                typed<float>(r->grad_gaussians), typed<float>(r->gaussians), t->count));
-  return DG_OK;
-}
-
 // The kernels of one optimize() step, in order. Everything the host decides per
 // step (camera, photo, SH degree, learning rates) is in device uniforms written
 // before this runs, so the same launches can be captured once and replayed.
@@ -521,9 +431,14 @@ static dg_status launch_step(dg_trainer* t, bool with_adam) {
   dg_renderer* r = t->renderer;
   DG_TRY(renderer_launch_forward(r, t->target));
   DG_TRY(loss_launch(t->loss, r->rasterizer->pixel_color));
-  DG_TRY(renderer_launch_backward(r, t->loss->pixel_grads, true));
+  // The splat gradients; each Gaussian's own gradients come from the preprocess
+  // backward pass, which on an Adam step applies Adam to them at once (on a
+  // densification step nothing uses them unless they are kept).
+  DG_TRY(renderer_launch_backward(r, t->loss->pixel_grads, !with_adam && t->keep_gradients));
   DG_TRY(launch_stats(t));
-  if (with_adam) DG_TRY(launch_adam(t));
+  if (with_adam)
+    DG_TRY(launch_preprocess_backward_adam(r, typed<AdamParams>(t->adam_params), typed<float>(t->params),
+                                           typed<float2>(t->moments), t->keep_gradients));
   // The frame's pair count, for afterSubmit (src/tileRasterizer.ts:187-191).
   dg_tile_rasterizer* tr = r->rasterizer;
   DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, t->ctx->stream));
@@ -925,6 +840,13 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   t->count = new_count;
   t->next_id = first_id + new_count;
   return st;
+}
+
+dg_status dg_trainer_set_keep_gradients(dg_trainer* t, int32_t enabled) {
+  DG_REQUIRE(t, "NULL argument");
+  t->keep_gradients = enabled != 0;
+  drop_graph(t);
+  return DG_OK;
 }
 
 dg_status dg_trainer_set_densify_log(dg_trainer* t, int32_t enabled, uint32_t horizon) {

@@ -297,6 +297,11 @@ class Trainer:
         """Replay each optimize() step as one captured CUDA graph."""
         _lib.call("dg_trainer_set_graph", self.handle, int(enabled))
 
+    def setKeepGradients(self, enabled: bool) -> None:
+        """Also store each step's Gaussian gradients in renderer.gradients (Adam
+        consumes them in registers otherwise); the parameters are the same."""
+        _lib.call("dg_trainer_set_keep_gradients", self.handle, int(enabled))
+
     # Learned densification (no reference counterpart; the reference densifies by
     # its gradient threshold alone, which stays the fallback).
     def setDensifyLog(self, enabled: bool, horizon: int = 1000) -> None:

@@ -295,6 +295,11 @@ dg_status dg_trainer_densification(const dg_trainer* t, uint32_t index, dg_densi
  * when the Gaussian count or the pair capacity changes). enabled = 0 launches each
  * kernel directly. Results are identical either way. */
 dg_status dg_trainer_set_graph(dg_trainer* t, int32_t enabled);
+/* An optimize() step applies Adam to each Gaussian's gradients as the backward
+ * pass produces them, without storing them; enabled = 1 stores them too, in the
+ * renderer's gradient buffers (gradients{gaussians, sh}), as the reference's
+ * separate passes leave them. The parameters are the same either way. */
+dg_status dg_trainer_set_keep_gradients(dg_trainer* t, int32_t enabled);
 dg_status dg_trainer_destroy(dg_trainer* t);
 
 /* ---- Learned densification proposal. No reference counterpart: the reference

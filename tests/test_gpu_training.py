@@ -69,6 +69,7 @@ def test_adam_step_matches_oracle(device):
     moments = rng.uniform(-1, 1, n * 61 * 2).astype(np.float32)
     moments[1::2] = np.abs(moments[1::2])
     t.buffers["moments"].write(moments)
+    t.setKeepGradients(True)
     t.optimize()
     grads = t.renderer.gradients
     gg, sg = grads["gaussians"].read(np.float32), grads["sh"].read(np.float32)
