@@ -57,10 +57,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
-    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify"],
+    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn"],
                     help="train: the headline training step; sort: config 2's sort/scan/ranges stress "
                          "(1.1M Gaussians at 1960x1090, the reference's 6-pass sort); densify: config 1/4, "
-                         "plain vs learned densification on the planes-and-boxes scene (minutes)")
+                         "plain vs learned densification on the planes-and-boxes scene (minutes); knn: the "
+                         "starting Gaussians' nearest-neighbour distances of a point cloud")
+    ap.add_argument("--knn-points", type=int, default=1_100_000, help="knn workload: points in the cloud")
     ap.add_argument("--train-steps", type=int, default=30_000, help="densify workload: steps per training run")
     ap.add_argument("--plain-runs", type=int, default=3, help="densify workload: seeded plain runs that log labels")
     ap.add_argument("--unbalanced", action="store_true",
@@ -525,6 +527,71 @@ def run_sort_stress(args, rank, local):
     return result
 
 
+def run_knn(args, rank, local):
+    """The starting Gaussians' neighbour distances (src/loadDataset.ts:124-149) of
+    a structure-from-motion-like cloud (clusters, a plane, 1% far outliers,
+    duplicates): the grid search on the GPU with the points resident (value) and
+    through the host API with its copies (e2e); the oracle's brute force, the
+    reference's algorithm, timed on a sample of query points on the host cores.
+    (The results are checked bit for bit against the brute force by
+    tests/test_gpu_init.py.)"""
+    if rank != 0:
+        return None
+    from diorama_gb300 import Device, scenes
+    from diorama_gb300.dataset import meanNeighborDistance2, meanNeighborDistance2Buffers
+    import oracle
+
+    n = args.knn_points
+    positions = scenes.clustered_cloud(n, 3)
+    device = Device(local)
+    points = np.zeros((n, 4), np.float32)
+    points[:, :3] = positions.reshape(-1, 3)
+    pbuf = device.upload(points)
+    out = device.createBuffer(n * 4)
+    for _ in range(args.warmup):
+        meanNeighborDistance2Buffers(device, pbuf, n, out)
+    device.synchronize()
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    walls = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        meanNeighborDistance2Buffers(device, pbuf, n, out)
+        device.synchronize()
+        walls.append(time.perf_counter() - t0)
+    report = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    e2e = []
+    for _ in range(max(2, args.steps // 2)):
+        t0 = time.perf_counter()
+        meanNeighborDistance2(device, positions)
+        e2e.append(time.perf_counter() - t0)
+    sample = 2000
+    which = np.random.default_rng(7).choice(n, sample, replace=False).astype(np.uint32)
+    t0 = time.perf_counter()
+    oracle.mean_neighbor_distance2_of(positions, which)
+    cpu_s = time.perf_counter() - t0
+    wall = statistics.median(walls)
+    result = {
+        "metric": "nearest-neighbour distances", "value": round(n / wall, 1), "unit": "points/s",
+        "ms_per_call": round(wall * 1e3, 3), "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n:,} points: 80% in clusters (sigma 0.01-0.5), 15% on a plane, 5% outliers "
+                               "(sigma 60), 0.5% duplicates; 3 nearest neighbours each"},
+        "steps": args.steps, "warmup": args.warmup,
+        "kernels": {k: {"avg_us": round(1000 * t / c, 2), "launches_per_call": c // args.steps}
+                    for k, (c, t) in report.items()},
+        "e2e": {"value": round(n / statistics.median(e2e), 1), "unit": "points/s",
+                "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 4},
+        "cpu_baseline": {"value": round(sample / cpu_s, 1), "unit": "points/s", "cores": oracle.num_threads(),
+                         "kind": "port", "sample": f"brute force (the reference's algorithm) for {sample} query "
+                                                   f"points over all {n:,}"},
+    }
+    pbuf.destroy()
+    out.destroy()
+    device.destroy()
+    return result
+
+
 def run_densify_experiment(args, rank, local):
     """Configs 1 and 4: the planes-and-boxes scene (500k ground-truth Gaussians,
     263 training and 37 held-out 980x545 views), trained from 100k noisy surface
@@ -661,6 +728,8 @@ def main():
         result = run_sort_stress(args, rank, local) if args.impl == "ours" else None
     elif args.workload == "densify":
         result = run_densify_experiment(args, rank, local) if args.impl == "ours" else None
+    elif args.workload == "knn":
+        result = run_knn(args, rank, local) if args.impl == "ours" else None
     elif args.impl == "reference":
         result = run_reference(args, rank, world, group)
     else:

@@ -175,6 +175,9 @@ SIGNATURES = {
     "dg_trainer_densification": (None, [_P, c_uint32, POINTER(DensificationC)]),
     "dg_trainer_set_graph": (None, [_P, c_int32]),
     "dg_trainer_set_keep_gradients": (None, [_P, c_int32]),
+    "dg_mean_neighbor_distance2": (None, [_P, c_void_p, c_uint32, c_void_p]),
+    "dg_mean_neighbor_distance2_buffers": (None, [_P, _P, c_uint32, _P]),
+    "dg_initial_gaussians": (None, [_P, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]),
     "dg_trainer_destroy": (None, [_P]),
     "dg_densify_mlp_create": (None, [_P, c_uint32, POINTER(c_void_p)]),
     "dg_densify_mlp_train": (None, [_P, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_float, c_float, c_int32,

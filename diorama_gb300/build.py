@@ -28,7 +28,7 @@ HEADER = PACKAGE.parent / "include" / "diorama_gb300.h"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-DNDEBUG", "--expt-relaxed-constexpr"]
 # Files whose float expressions must round exactly as written.
-EXACT = {"dg_render.cu", "dg_loss.cu"}
+EXACT = {"dg_render.cu", "dg_loss.cu", "dg_init.cu"}
 
 
 def nvcc() -> str:

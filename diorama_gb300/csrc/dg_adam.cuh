@@ -1,6 +1,7 @@
-// Adam's per-slot arithmetic (src/shaders/adam.wgsl:52-106), shared by the
-// elementwise Adam kernels (dg_train.cu) and the backward pass that applies
-// Adam as soon as it has a Gaussian's gradients (dg_render_bwd.cu).
+// Adam's per-slot arithmetic (src/shaders/adam.wgsl:52-106) and the
+// densification statistics (src/shaders/adam.wgsl:126-134), used by the backward
+// pass that applies Adam as soon as it has a Gaussian's gradients
+// (dg_render_bwd.cu) and by the trainer's own kernels (dg_train.cu).
 #pragma once
 #include "dg_common.cuh"
 
@@ -53,6 +54,25 @@ __device__ __forceinline__ float adam_param_slot(const AdamParams& ap, uint32_t 
   const float ey = expf(opacity ? -next : next);
   activated = opacity ? 1.0f / (1.0f + ey) : scale ? ey : color ? 0.5f + SH_C0 * next : next;
   return next;
+}
+
+// src/shaders/adam.wgsl:126-134 for Gaussian i: if it was drawn (radius > 0), the
+// length of its screen-space mean gradient in pixels, a count and the largest
+// radius go into stats; aux (the learned densification's extra statistics) gets
+// the squared length and the count of steps seen over the Gaussian's life.
+__device__ __forceinline__ void accumulate_stats_one(const float* __restrict__ viewport,
+                                                     const float* __restrict__ splats,
+                                                     const float* __restrict__ splat_grads, float4* __restrict__ stats,
+                                                     float2* __restrict__ aux, uint32_t i) {
+  const float radius = splats[(size_t)i * FLOATS_PER_SPLAT + 3];
+  if (radius == 0.0f) return;
+  const float gx = splat_grads[(size_t)i * SPLAT_GRADS] * viewport[0] * 0.5f;
+  const float gy = splat_grads[(size_t)i * SPLAT_GRADS + 1] * viewport[1] * 0.5f;
+  const float len = sqrtf(gx * gx + gy * gy);
+  const float4 s = stats[i];
+  stats[i] = make_float4(s.x + len, s.y + 1.0f, fmaxf(s.z, radius), 0.0f);
+  const float2 a = aux[i];
+  aux[i] = make_float2(a.x + len * len, a.y + 1.0f);
 }
 
 }  // namespace dg

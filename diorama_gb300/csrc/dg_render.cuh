@@ -144,11 +144,12 @@ const Camera* renderer_camera(dg_renderer* r);
 dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status launch_preprocess_backward(dg_renderer* r);
 struct AdamParams;
-// The training step's preprocess backward with Adam applied at once (the same
-// values as launch_preprocess_backward followed by the Adam kernels); with
+// The training step's preprocess backward with Adam applied at once to each
+// Gaussian's raw parameters and SH (src/shaders/adam.wgsl:52-106) and the
+// densification statistics added up (src/shaders/adam.wgsl:126-134); with
 // keep_gradients the gradients are stored as well.
 dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam, float* params, float2* moments,
-                                         bool keep_gradients);
+                                         float4* stats, float2* aux, bool keep_gradients);
 // Batched views (dg_views.cu): renders count views in batches of `batch` into
 // targets (count rgba8 images, may be NULL) and pixel_colors (count vec4 images,
 // may be NULL).

@@ -543,13 +543,15 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
 // CTA's slots, one thread per slot, reading and writing the Gaussians' raw
 // parameters, SH coefficients, moment records and activated values as contiguous
 // runs: the 180 + 64 bytes of gradients per Gaussian never go to memory and back.
-// The same values as preprocess_backward_kernel followed by the Adam kernels.
+// Each thread also adds its Gaussian's densification statistics
+// (src/shaders/adam.wgsl:126-134).
 // gaussian_grads and sh_grads (may be NULL) also receive the gradients.
 __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
     const Camera* __restrict__ camera, float* __restrict__ gaussians, float* __restrict__ sh, uint32_t count,
     const uint32_t* __restrict__ scene_params, const float* __restrict__ splats, const float* __restrict__ splat_grads,
     const AdamParams* __restrict__ adam, float* __restrict__ params, float2* __restrict__ moments,
-    float* __restrict__ gaussian_grads, float* __restrict__ sh_grads) {
+    float4* __restrict__ stats, float2* __restrict__ aux, float* __restrict__ gaussian_grads,
+    float* __restrict__ sh_grads) {
   constexpr uint32_t GP = FLOATS_PER_GAUSSIAN + 1;  // a row pitch prime to 32
   __shared__ Camera s_cam;
   __shared__ __align__(16) float s_sh[PBWD_THREADS * SH_REST_FLOATS];  // coefficients, then their gradients
@@ -571,6 +573,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
 #pragma unroll
     for (int k = 0; k < 16; k++) s_pg[threadIdx.x * GP + k] = out[k];
     if (gaussian_grads) store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);
+    accumulate_stats_one(s_ap.viewport, splats, splat_grads, stats, aux, i);
   }
   __syncthreads();
   if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
@@ -658,12 +661,12 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
 }
 
 dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam, float* params, float2* moments,
-                                         bool keep_gradients) {
+                                         float4* stats, float2* aux, bool keep_gradients) {
   DG_LAUNCH(r->ctx, "preprocess_backward_adam",
             preprocess_backward_adam_kernel<<<ceil_div(r->count, PBWD_THREADS), PBWD_THREADS, 0, r->ctx->stream>>>(
                 typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                 typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats), adam, params,
-                moments, keep_gradients ? typed<float>(r->grad_gaussians) : nullptr,
+                moments, stats, aux, keep_gradients ? typed<float>(r->grad_gaussians) : nullptr,
                 keep_gradients ? typed<float>(r->grad_sh) : nullptr));
   return DG_OK;
 }

@@ -59,24 +59,14 @@ __global__ void reset_opacity_kernel(float* __restrict__ params, float2* __restr
   gaussians[at] = sigmoidf_(v);
 }
 
-// src/shaders/adam.wgsl:126-134
-// src/shaders/adam.wgsl:126-134. aux (the learned densification's extra
-// statistics) gets the sum of squared norms since the last densification and the
-// count of steps seen over the Gaussian's life.
+// src/shaders/adam.wgsl:126-134 on a step without Adam (a densification step);
+// on the others the backward pass with Adam accumulates them.
 __global__ void stats_kernel(const AdamParams* __restrict__ ap, const float* __restrict__ splats,
                              const float* __restrict__ splat_grads, float4* __restrict__ stats,
                              float2* __restrict__ aux, uint32_t count) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  const float radius = splats[(size_t)i * FLOATS_PER_SPLAT + 3];
-  if (radius == 0.0f) return;
-  const float gx = splat_grads[(size_t)i * SPLAT_GRADS] * ap->viewport[0] * 0.5f;
-  const float gy = splat_grads[(size_t)i * SPLAT_GRADS + 1] * ap->viewport[1] * 0.5f;
-  const float len = sqrtf(gx * gx + gy * gy);
-  const float4 s = stats[i];
-  stats[i] = make_float4(s.x + len, s.y + 1.0f, fmaxf(s.z, radius), 0.0f);
-  const float2 a = aux[i];
-  aux[i] = make_float2(a.x + len * len, a.y + 1.0f);
+  accumulate_stats_one(ap->viewport, splats, splat_grads, stats, aux, i);
 }
 
 // What happens to Gaussian i (src/shaders/densify.wgsl:72-85): 0 drop, 1 keep, 2 clone, 3 split.
@@ -432,13 +422,16 @@ static dg_status launch_step(dg_trainer* t, bool with_adam) {
   DG_TRY(renderer_launch_forward(r, t->target));
   DG_TRY(loss_launch(t->loss, r->rasterizer->pixel_color));
   // The splat gradients; each Gaussian's own gradients come from the preprocess
-  // backward pass, which on an Adam step applies Adam to them at once (on a
-  // densification step nothing uses them unless they are kept).
+  // backward pass, which on an Adam step applies Adam to them at once and adds up
+  // the densification statistics (on a densification step nothing uses them
+  // unless they are kept).
   DG_TRY(renderer_launch_backward(r, t->loss->pixel_grads, !with_adam && t->keep_gradients));
-  DG_TRY(launch_stats(t));
   if (with_adam)
     DG_TRY(launch_preprocess_backward_adam(r, typed<AdamParams>(t->adam_params), typed<float>(t->params),
-                                           typed<float2>(t->moments), t->keep_gradients));
+                                           typed<float2>(t->moments), typed<float4>(t->stats),
+                                           typed<float2>(t->aux), t->keep_gradients));
+  else
+    DG_TRY(launch_stats(t));
   // The frame's pair count, for afterSubmit (src/tileRasterizer.ts:187-191).
   dg_tile_rasterizer* tr = r->rasterizer;
   DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, t->ctx->stream));

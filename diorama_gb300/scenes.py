@@ -138,3 +138,26 @@ def ring_cameras(count: int = 300, seed: int = 3, width: int = 980, height: int 
     train = [c for i, c in enumerate(cams) if i % 8 != 7]
     held = [c for i, c in enumerate(cams) if i % 8 == 7]
     return train, held
+
+
+def clustered_cloud(count: int, seed: int) -> np.ndarray:
+    """A structure-from-motion-like point cloud (count × 3 floats, flat): dense
+    clusters of varied size (80%), a thin plane (15%), far outliers (the rest)
+    and some exact duplicates."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    clusters = max(1, count // 2000)
+    centres = rng.uniform(-5, 5, (clusters, 3))
+    sizes = rng.uniform(0.01, 0.5, clusters)
+    n_cluster = int(count * 0.8)
+    which = rng.integers(0, clusters, n_cluster)
+    parts.append(centres[which] + rng.normal(0, 1, (n_cluster, 3)) * sizes[which, None])
+    n_plane = int(count * 0.15)
+    plane = rng.uniform(-4, 4, (n_plane, 3))
+    plane[:, 1] = -1.5
+    parts.append(plane)
+    parts.append(rng.normal(0, 60, (count - n_cluster - n_plane, 3)))
+    points = np.concatenate(parts).astype(np.float32)
+    dup = rng.integers(0, count, count // 200)
+    points[rng.integers(0, count, dup.size)] = points[dup]
+    return points.reshape(-1)

@@ -349,6 +349,26 @@ dg_status dg_trainer_set_densify_mlp(dg_trainer* t, dg_densify_mlp* mlp, float m
  * and of those the ones not densified. */
 dg_status dg_trainer_densify_mlp_stats(const dg_trainer* t, uint64_t* scored, uint64_t* confident, uint64_t* vetoed);
 
+/* ---- Starting Gaussians from a point cloud (src/loadDataset.ts:93-149). */
+/* meanNeighborDistance2 (src/loadDataset.ts:124-149, src/shaders/nearestNeighbors.wgsl:13-44):
+ * distance2[i] = the mean of the squared distances from point i to its 3 nearest
+ * other points (duplicates count; with fewer than 4 points each missing neighbour
+ * counts as 3.4e38, so 1 or 2 points give infinity). The same values as the
+ * reference's brute force, found through a grid. positions: count × 3 f32 (host);
+ * distance2: count f32 (host). Blocks until done. */
+dg_status dg_mean_neighbor_distance2(dg_context* ctx, const float* positions, uint32_t count, float* distance2);
+/* The same on device buffers: points holds count × 4 f32 (xyz and padding, the
+ * reference's points buffer), distance2 count f32. Blocks on one 64-byte readback
+ * of the points' bounds; the rest is enqueued on the context's stream. */
+dg_status dg_mean_neighbor_distance2_buffers(dg_context* ctx, dg_buffer* points, uint32_t count,
+                                             dg_buffer* distance2);
+/* initialGaussians (src/loadDataset.ts:99-121): one raw Gaussian per point (params
+ * count × 16 f32, host) with the point's position, colour (colors count × 3 u8,
+ * host), opacity 0.1, rotation (1, 0, 0, 0) and log-scale 0.5 ln max(distance2,
+ * 1e-7) on all three axes; sh (count × 45 f32, host) is zeroed. Blocks. */
+dg_status dg_initial_gaussians(dg_context* ctx, const float* positions, const uint8_t* colors, uint32_t count,
+                               float* params, float* sh);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,6 +63,9 @@ def lib():
             "or_densify_count": (None, [_f32p, _f32p, _u32, _f32p, _u32p, _u32p]),
             "or_densify_scatter": (None, [_f32p, _f32p, _f32p, _f32p, _u32p, _u32, _f32p, _u32, _f32p, _f32p, _f32p]),
             "or_pcg": (_u32, [_u32]),
+            "or_mean_neighbor_distance2": (None, [_f32p, _u32, _f32p]),
+            "or_mean_neighbor_distance2_of": (None, [_f32p, _u32, _u32p, _u32, _f32p]),
+            "or_initial_gaussians": (None, [_f32p, _u8p, _f32p, _u32, _f32p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -214,6 +217,39 @@ def densify(params, stats, sh, moments, dp, seed):
     new_moments = np.zeros(total * MOMENT_SLOTS * 2, np.float32)
     lib().or_densify_scatter(params, stats, sh, moments, outputs, n, dpa, seed, new_params, new_sh, new_moments)
     return new_params, new_sh, new_moments, tally
+
+
+def mean_neighbor_distance2(positions) -> np.ndarray:
+    """Brute-force mean squared distance to the 3 nearest other points
+    (positions: n × 3 floats)."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    points = np.zeros((pos.shape[0], 4), np.float32)
+    points[:, :3] = pos
+    out = np.zeros(pos.shape[0], np.float32)
+    lib().or_mean_neighbor_distance2(points.reshape(-1), pos.shape[0], out)
+    return out
+
+
+def mean_neighbor_distance2_of(positions, which) -> np.ndarray:
+    """mean_neighbor_distance2 for the listed points only, over all points."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    points = np.zeros((pos.shape[0], 4), np.float32)
+    points[:, :3] = pos
+    which = np.ascontiguousarray(which, np.uint32)
+    out = np.zeros(which.size, np.float32)
+    lib().or_mean_neighbor_distance2_of(points.reshape(-1), pos.shape[0], which, which.size, out)
+    return out
+
+
+def initial_gaussians(positions, colors, distance2) -> np.ndarray:
+    """The starting raw Gaussians (n × 16 floats) from points, colours and
+    neighbour distances."""
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+    n = pos.size // 3
+    params = np.zeros(n * FLOATS_PER_GAUSSIAN, np.float32)
+    lib().or_initial_gaussians(pos, np.ascontiguousarray(colors, np.uint8).reshape(-1),
+                               np.ascontiguousarray(distance2, np.float32), n, params)
+    return params
 
 
 def exp_ref(x: float) -> float:

@@ -1155,3 +1155,65 @@ uint32_t or_render_frame(const float* cam, const float* bg, const float* gaussia
   or_rasterize(cam, bg, splats, values, ranges, pixel_color, pixel_last, rgba8);
   return total;
 }
+
+/* src/shaders/nearestNeighbors.wgsl:13-44, by brute force as the reference does:
+ * for each point (points: n × 4 floats, xyz + padding) the mean of the squared
+ * distances to its 3 nearest other points. d = q - p per component, then
+ * d.x² + d.y² + d.z² summed from x; the three smallest kept with the WGSL's strict
+ * comparisons, starting from 3.4e38. */
+static float neighbor_distance2_of(const float* points, uint32_t n, uint32_t i) {
+  const float* me = points + (size_t)i * 4;
+  float b0 = 3.4e38f, b1 = 3.4e38f, b2 = 3.4e38f;
+  for (uint32_t j = 0; j < n; j++) {
+    if (j == i) continue;
+    const float* q = points + (size_t)j * 4;
+    const float dx = q[0] - me[0], dy = q[1] - me[1], dz = q[2] - me[2];
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < b2) {
+      if (d2 < b1) {
+        b2 = b1;
+        if (d2 < b0) {
+          b1 = b0;
+          b0 = d2;
+        } else {
+          b1 = d2;
+        }
+      } else {
+        b2 = d2;
+      }
+    }
+  }
+  return (b0 + b1 + b2) / 3.0f;
+}
+
+void or_mean_neighbor_distance2(const float* points, uint32_t n, float* out) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < (int64_t)n; i++) out[i] = neighbor_distance2_of(points, n, (uint32_t)i);
+}
+
+/* The same for the m points listed in `which` only (out[k] for point which[k]). */
+void or_mean_neighbor_distance2_of(const float* points, uint32_t n, const uint32_t* which, uint32_t m, float* out) {
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int64_t k = 0; k < (int64_t)m; k++) out[k] = neighbor_distance2_of(points, n, which[k]);
+}
+
+/* src/loadDataset.ts:99-121: the starting raw Gaussians. The arithmetic there is
+ * JavaScript's float64, rounded to float32 by the Float32Array stores. */
+void or_initial_gaussians(const float* positions, const uint8_t* colors, const float* distance2, uint32_t n,
+                          float* params) {
+  const double sh_c0 = 0.28209479177387814;
+  const float opacity_logit = (float)log(0.1 / 0.9);
+  for (uint32_t i = 0; i < n; i++) {
+    float* g = params + (size_t)i * FPG;
+    memset(g, 0, FPG * sizeof(float));
+    const double d2 = (double)distance2[i];
+    const double log_scale = 0.5 * log(d2 > 1e-7 ? d2 : 1e-7);
+    for (int k = 0; k < 3; k++) {
+      g[k] = positions[(size_t)i * 3 + k];
+      g[4 + k] = (float)log_scale;
+      g[12 + k] = (float)(((double)colors[(size_t)i * 3 + k] / 255.0 - 0.5) / sh_c0);
+    }
+    g[3] = opacity_logit;
+    g[8] = 1.0f;
+  }
+}

@@ -13,6 +13,7 @@ import oracle
 from diorama_gb300 import CameraData, Gaussian, packGaussians
 from diorama_gb300.mat4 import IDENTITY, perspective
 from diorama_gb300.random import mulberry32
+from diorama_gb300.scenes import clustered_cloud  # noqa: F401
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 
@@ -119,3 +120,29 @@ def sort_keys(size: int) -> np.ndarray:
 
 def pack(gaussians) -> np.ndarray:
     return packGaussians(gaussians)
+
+
+def neighbor_check_points():
+    """src/checks/dataset.ts:28-41: 3,001 points in [-2, 2)³ from mulberry32(31),
+    point 1000 an exact copy of point 7, then one colour per point from the same
+    generator."""
+    random = mulberry32(31)
+    count = 3001
+    positions = np.array([random() * 4 - 2 for _ in range(count * 3)], np.float64).astype(np.float32)
+    positions[3 * 1000:3 * 1001] = positions[3 * 7:3 * 8]
+    colors = np.array([math.floor(random() * 256) for _ in range(count * 3)], np.uint8)
+    return positions, colors
+
+
+def neighbor_distance2_f64(positions: np.ndarray) -> np.ndarray:
+    """src/checks/dataset.ts:60-80: the CPU brute force in float64."""
+    p = positions.reshape(-1, 3).astype(np.float64)
+    out = np.zeros(p.shape[0])
+    for start in range(0, p.shape[0], 512):
+        d = p[start:start + 512, None, :] - p[None, :, :]
+        d2 = (d * d).sum(-1)
+        rows = np.arange(d2.shape[0])
+        d2[rows, start + rows] = np.inf
+        out[start:start + 512] = np.sort(np.partition(d2, 2, axis=1)[:, :3], axis=1).sum(1) / 3
+    return out
+
