@@ -10,7 +10,9 @@ loaded or no CUDA device is present, creating a Device raises.
 from ._lib import DioramaError
 from .gaussians import (FLOATS_PER_GAUSSIAN, FLOATS_PER_SPLAT, SH_REST_FLOATS, Gaussian, Splat2D, packGaussians,
                         packSplats, unpackSplats)
+from .dataset import initialGaussians, meanNeighborDistance2, meanNeighborDistance2Buffers
 from .gpu import Buffer, Device, Texture, initGpu, readBuffer
+from .ply import GaussianScene, parseGaussianPly, writeGaussianPly
 from .primitives import PrefixSum, RadixSort
 from .renderer import CameraData, GaussianRenderer, SphericalHarmonics, TileRasterizer
 from .training import (DEFAULT_SETTINGS, MOMENT_SLOTS, Densification, DensifyMLP, RawGaussians, Trainer,
@@ -21,5 +23,6 @@ __all__ = [
     "Splat2D", "packGaussians", "packSplats", "unpackSplats", "Buffer", "Device", "Texture", "initGpu", "readBuffer",
     "PrefixSum", "RadixSort", "CameraData", "GaussianRenderer", "SphericalHarmonics", "TileRasterizer",
     "DEFAULT_SETTINGS", "Densification", "DensifyMLP", "RawGaussians", "Trainer", "TrainingLoss", "TrainingSettings",
-    "TrainingView", "activate",
+    "TrainingView", "activate", "GaussianScene", "parseGaussianPly", "writeGaussianPly", "initialGaussians",
+    "meanNeighborDistance2", "meanNeighborDistance2Buffers",
 ]

@@ -175,6 +175,10 @@ SIGNATURES = {
     "dg_trainer_densification": (None, [_P, c_uint32, POINTER(DensificationC)]),
     "dg_trainer_set_graph": (None, [_P, c_int32]),
     "dg_trainer_set_keep_gradients": (None, [_P, c_int32]),
+    "dg_trainer_save_checkpoint": (None, [_P, c_char_p]),
+    "dg_trainer_resume": (None, [_P, c_char_p, c_void_p, c_uint32, c_void_p, POINTER(_P)]),
+    "dg_parse_gaussian_ply": (None, [c_void_p, c_uint64, POINTER(c_uint32), POINTER(c_uint32), c_void_p, c_void_p]),
+    "dg_write_gaussian_ply": (None, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint64, POINTER(c_uint64)]),
     "dg_mean_neighbor_distance2": (None, [_P, c_void_p, c_uint32, c_void_p]),
     "dg_mean_neighbor_distance2_buffers": (None, [_P, _P, c_uint32, _P]),
     "dg_initial_gaussians": (None, [_P, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]),

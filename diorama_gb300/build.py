@@ -1,7 +1,7 @@
 """Builds libdiorama_gb300.so for sm_103a with nvcc, in-tree, into diorama_gb300/_build/.
 
-Each .cu file compiles to an object in parallel, then nvcc links the shared
-library. The renderer and the loss are compiled with --fmad=false: their float
+Each .cu file (and each host-only .cpp file) compiles to an object in parallel,
+then nvcc links the shared library. The renderer and the loss are compiled with --fmad=false: their float
 expressions are evaluated exactly as written (fused multiply-adds only where the
 source spells out fmaf), which is what makes the forward pass bit-identical to
 the CPU oracle's restatement of the reference.
@@ -60,8 +60,8 @@ def _stale(target: Path, inputs: list[Path]) -> bool:
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> Path:
     """Compiles the library if needed and returns its path."""
     extra = list(extra or [])
-    sources = sorted(SOURCES.glob("*.cu"))
-    headers = sorted(SOURCES.glob("*.cuh")) + [HEADER]
+    sources = sorted(SOURCES.glob("*.cu")) + sorted(SOURCES.glob("*.cpp"))
+    headers = sorted(SOURCES.glob("*.cuh")) + sorted(SOURCES.glob("*.h")) + [HEADER]
     if not force and not _stale(LIBRARY, sources + headers + [Path(__file__)]):
         return LIBRARY
     BUILD.mkdir(parents=True, exist_ok=True)

@@ -6,6 +6,7 @@
 #include "dg_common.cuh"
 #include "dg_loss.cuh"
 #include "dg_mlp.cuh"
+#include "dg_ply.h"
 #include "dg_render.cuh"
 #include "dg_scan.cuh"
 
@@ -1020,3 +1021,227 @@ dg_status dg_trainer_destroy(dg_trainer* t) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- checkpoints
+// No reference counterpart: the reference saves trained Gaussians
+// (src/plyWriter.ts) but cannot resume training. A checkpoint is a .ply whose
+// vertex element holds writeGaussianPly's 62 properties first, so that the
+// reference's reader (src/plyLoader.ts) and other 3DGS viewers open it as a
+// scene, followed by the rest of each Gaussian's training state as further float
+// properties: the raw parameters' pad floats 7 and 15 (densification stamps),
+// Adam's 61 moment pairs, the densification statistics and the learned
+// densification's statistics. Further elements hold the identities, the
+// trainer's counters, the rest of the current round of views and the
+// densification history. Resuming from it continues the run exactly where it
+// stopped (up to the float-atomic order of the backward pass).
+
+namespace dg {
+namespace {
+
+constexpr const char* CHECKPOINT_COMMENT = "diorama_gb300 training checkpoint 1";
+const char* const TRAINER_FIELDS[] = {"iteration", "sh_degree",   "adam_steps", "random_state",
+                                      "next_id",   "view_count", "due_densify", "due_reset"};
+const char* const DENSIFICATION_FIELDS[] = {"step", "before", "after", "kept", "cloned", "split", "removed"};
+const char* const STAT_NAMES[] = {"densify_grad_sum", "densify_grad_count", "densify_max_radius", "densify_stat_3",
+                                  "densify_grad_sq_sum", "densify_steps_seen"};
+
+std::vector<PlyElement> checkpoint_elements(uint32_t count, uint32_t queue, uint32_t history) {
+  PlyElement vertex{"vertex", count, gaussian_vertex_properties()};
+  vertex.properties.push_back(PlyProperty{"pad_7", PlyType::Float});
+  vertex.properties.push_back(PlyProperty{"pad_15", PlyType::Float});
+  for (uint32_t k = 0; k < MOMENT_SLOTS; k++) {
+    vertex.properties.push_back(PlyProperty{"adam_m_" + std::to_string(k), PlyType::Float});
+    vertex.properties.push_back(PlyProperty{"adam_v_" + std::to_string(k), PlyType::Float});
+  }
+  for (const char* n : STAT_NAMES) vertex.properties.push_back(PlyProperty{n, PlyType::Float});
+  PlyElement ids{"gaussian_id", count, {PlyProperty{"id", PlyType::Uint}}};
+  PlyElement trainer{"trainer", 1, {}};
+  for (const char* n : TRAINER_FIELDS) trainer.properties.push_back(PlyProperty{n, PlyType::Uint});
+  PlyElement order{"view_queue", queue, {PlyProperty{"view", PlyType::Uint}}};
+  PlyElement history_e{"densification", history, {}};
+  for (const char* n : DENSIFICATION_FIELDS) history_e.properties.push_back(PlyProperty{n, PlyType::Uint});
+  return {vertex, ids, trainer, order, history_e};
+}
+
+struct File {
+  FILE* f = nullptr;
+  ~File() {
+    if (f) fclose(f);
+  }
+};
+
+}  // namespace
+}  // namespace dg
+
+dg_status dg_trainer_save_checkpoint(dg_trainer* t, const char* path) {
+  DG_REQUIRE(t && path, "NULL argument");
+  const uint32_t n = t->count;
+  std::vector<float> params((size_t)n * FLOATS_PER_GAUSSIAN), sh((size_t)n * SH_REST_FLOATS),
+      moments((size_t)n * MOMENT_SLOTS * 2), stats((size_t)n * 4), aux((size_t)n * 2);
+  std::vector<uint32_t> ids(n);
+  cudaStream_t st = t->ctx->stream;
+  DG_CUDA(cudaMemcpyAsync(params.data(), t->params->ptr, params.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(sh.data(), t->renderer->sh->ptr, sh.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(moments.data(), t->moments->ptr, moments.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(stats.data(), t->stats->ptr, stats.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(aux.data(), t->aux->ptr, aux.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaMemcpyAsync(ids.data(), t->ids->ptr, ids.size() * 4, cudaMemcpyDeviceToHost, st));
+  DG_CUDA(cudaStreamSynchronize(st));
+  const auto elements = checkpoint_elements(n, (uint32_t)t->queue.size(), (uint32_t)t->densifications.size());
+  const std::string header = ply_header_text(elements, {CHECKPOINT_COMMENT});
+  File file;
+  file.f = fopen(path, "wb");
+  if (!file.f) return fail(DG_ERROR_INVALID_ARGUMENT, std::string("cannot open ") + path + " for writing");
+  bool ok = fwrite(header.data(), 1, header.size(), file.f) == header.size();
+  const size_t stride = elements[0].properties.size();
+  std::vector<float> rows;
+  const size_t batch = 4096;
+  for (size_t first = 0; ok && first < n; first += batch) {
+    const size_t here = std::min(batch, (size_t)n - first);
+    rows.assign(here * stride, 0.0f);
+    for (size_t r = 0; r < here; r++) {
+      const size_t i = first + r;
+      float* row = rows.data() + r * stride;
+      gaussian_row(params.data() + i * FLOATS_PER_GAUSSIAN, sh.data() + i * SH_REST_FLOATS, row);
+      size_t at = 62;
+      row[at++] = params[i * FLOATS_PER_GAUSSIAN + 7];
+      row[at++] = params[i * FLOATS_PER_GAUSSIAN + 15];
+      std::memcpy(row + at, moments.data() + i * MOMENT_SLOTS * 2, MOMENT_SLOTS * 8);
+      at += MOMENT_SLOTS * 2;
+      std::memcpy(row + at, stats.data() + i * 4, 16);
+      std::memcpy(row + at + 4, aux.data() + i * 2, 8);
+    }
+    ok = fwrite(rows.data(), 4, rows.size(), file.f) == rows.size();
+  }
+  const uint32_t counters[] = {t->iteration, t->sh_degree, t->adam_steps, t->random_state, t->next_id,
+                               (uint32_t)t->views.size(), t->due_densify ? 1u : 0u, t->due_reset ? 1u : 0u};
+  ok = ok && fwrite(ids.data(), 4, n, file.f) == n;
+  ok = ok && fwrite(counters, 4, 8, file.f) == 8;
+  ok = ok && fwrite(t->queue.data(), 4, t->queue.size(), file.f) == t->queue.size();
+  for (const auto& d : t->densifications) {
+    const uint32_t row[] = {d.step, d.before, d.after, d.kept, d.cloned, d.split, d.removed};
+    ok = ok && fwrite(row, 4, 7, file.f) == 7;
+  }
+  if (!ok) return fail(DG_ERROR_INVALID_ARGUMENT, std::string("writing ") + path + " failed");
+  return DG_OK;
+}
+
+dg_status dg_trainer_resume(dg_context* ctx, const char* path, const dg_training_view* views, uint32_t view_count,
+                            const dg_training_settings* settings, dg_trainer** out) {
+  DG_REQUIRE(ctx && path && out, "NULL argument");
+  std::vector<uint8_t> bytes;
+  {
+    File file;
+    file.f = fopen(path, "rb");
+    if (!file.f) return fail(DG_ERROR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+    fseek(file.f, 0, SEEK_END);
+    const long size = ftell(file.f);
+    fseek(file.f, 0, SEEK_SET);
+    if (size < 0) return fail(DG_ERROR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+    bytes.resize((size_t)size);
+    if (fread(bytes.data(), 1, bytes.size(), file.f) != bytes.size())
+      return fail(DG_ERROR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+  }
+  PlyHeader h;
+  DG_TRY(ply_parse_header(bytes.data(), bytes.size(), &h));
+  bool tagged = false;
+  for (const auto& c : h.comments) tagged = tagged || c == CHECKPOINT_COMMENT;
+  DG_REQUIRE(tagged, "not a training checkpoint (a plain .ply has no training state to resume)");
+  const char* names[] = {"vertex", "gaussian_id", "trainer", "view_queue", "densification"};
+  DG_REQUIRE(h.elements.size() >= 5, "a training checkpoint has 5 elements");
+  std::vector<uint64_t> offset(5);
+  uint64_t at = h.body;
+  for (int e = 0; e < 5; e++) {
+    DG_REQUIRE(h.elements[e].name == names[e] && !h.elements[e].opaque, "unexpected element in the checkpoint");
+    offset[e] = at;
+    at += h.elements[e].count * h.elements[e].row_bytes();
+  }
+  DG_REQUIRE(at <= bytes.size(), "The .ply file is shorter than its header says.");
+  const PlyElement& v = h.elements[0];
+  const uint32_t n = (uint32_t)v.count;
+  DG_REQUIRE(h.elements[1].count == n && h.elements[2].count == 1, "inconsistent checkpoint element counts");
+  // Each element's properties are located by name (all 4-byte floats or uints).
+  auto column = [&](const PlyElement& e, const std::string& name, int* out_col) -> dg_status {
+    const int k = e.find(name);
+    if (k < 0 || e.properties[k].type == PlyType::Uchar)
+      return fail(DG_ERROR_INVALID_ARGUMENT, "the checkpoint has no \"" + name + "\" property");
+    *out_col = k;
+    return DG_OK;
+  };
+  auto word = [&](int e, uint64_t row, int col) {
+    uint32_t w;
+    std::memcpy(&w, bytes.data() + offset[e] + row * h.elements[e].row_bytes() + (uint64_t)col * 4, 4);
+    return w;
+  };
+  auto real = [&](int e, uint64_t row, int col) {
+    const uint32_t w = word(e, row, col);
+    float f;
+    std::memcpy(&f, &w, 4);
+    return f;
+  };
+  // Raw parameter k from its vertex property (src/plyWriter.ts:8-12 names them).
+  const char* param_names[FLOATS_PER_GAUSSIAN] = {"x",     "y",     "z",     "opacity", "scale_0", "scale_1",
+                                                  "scale_2", "pad_7", "rot_0", "rot_1",   "rot_2",   "rot_3",
+                                                  "f_dc_0", "f_dc_1", "f_dc_2", "pad_15"};
+  int pc[FLOATS_PER_GAUSSIAN], rc[SH_REST_FLOATS], mc[MOMENT_SLOTS * 2], sc[6], idc, uc[8], qc, dc[7];
+  for (uint32_t k = 0; k < FLOATS_PER_GAUSSIAN; k++) DG_TRY(column(v, param_names[k], &pc[k]));
+  for (uint32_t k = 0; k < SH_REST_FLOATS; k++) DG_TRY(column(v, "f_rest_" + std::to_string(k), &rc[k]));
+  for (uint32_t k = 0; k < MOMENT_SLOTS; k++) {
+    DG_TRY(column(v, "adam_m_" + std::to_string(k), &mc[2 * k]));
+    DG_TRY(column(v, "adam_v_" + std::to_string(k), &mc[2 * k + 1]));
+  }
+  for (int k = 0; k < 6; k++) DG_TRY(column(v, STAT_NAMES[k], &sc[k]));
+  DG_TRY(column(h.elements[1], "id", &idc));
+  for (int k = 0; k < 8; k++) DG_TRY(column(h.elements[2], TRAINER_FIELDS[k], &uc[k]));
+  DG_TRY(column(h.elements[3], "view", &qc));
+  for (int k = 0; k < 7; k++) DG_TRY(column(h.elements[4], DENSIFICATION_FIELDS[k], &dc[k]));
+  DG_REQUIRE(word(2, 0, uc[5]) == view_count, "the checkpoint was trained on a different number of views");
+
+  constexpr uint32_t per_channel = SH_REST_FLOATS / 3;
+  std::vector<float> params((size_t)n * FLOATS_PER_GAUSSIAN), sh((size_t)n * SH_REST_FLOATS),
+      moments((size_t)n * MOMENT_SLOTS * 2), stats((size_t)n * 4), aux((size_t)n * 2);
+  std::vector<uint32_t> ids(n);
+  for (uint64_t i = 0; i < n; i++) {
+    for (uint32_t k = 0; k < FLOATS_PER_GAUSSIAN; k++) params[i * FLOATS_PER_GAUSSIAN + k] = real(0, i, pc[k]);
+    for (uint32_t c = 0; c < per_channel; c++)
+      for (uint32_t channel = 0; channel < 3; channel++)
+        sh[i * SH_REST_FLOATS + c * 3 + channel] = real(0, i, rc[channel * per_channel + c]);
+    for (uint32_t k = 0; k < MOMENT_SLOTS * 2; k++) moments[i * MOMENT_SLOTS * 2 + k] = real(0, i, mc[k]);
+    for (int k = 0; k < 4; k++) stats[i * 4 + k] = real(0, i, sc[k]);
+    for (int k = 0; k < 2; k++) aux[i * 2 + k] = real(0, i, sc[4 + k]);
+    ids[i] = word(1, i, idc);
+  }
+  dg_trainer* t = nullptr;
+  DG_TRY(dg_trainer_create(ctx, params.data(), sh.data(), n, views, view_count, settings, &t));
+  dg_status st = write_async(ctx, t->moments->ptr, moments.data(), moments.size() * 4);
+  if (st == DG_OK) st = write_async(ctx, t->stats->ptr, stats.data(), stats.size() * 4);
+  if (st == DG_OK) st = write_async(ctx, t->aux->ptr, aux.data(), aux.size() * 4);
+  if (st == DG_OK) st = write_async(ctx, t->ids->ptr, ids.data(), ids.size() * 4);
+  t->iteration = word(2, 0, uc[0]);
+  const uint32_t degree = word(2, 0, uc[1]);
+  t->adam_steps = word(2, 0, uc[2]);
+  t->random_state = word(2, 0, uc[3]);
+  t->next_id = word(2, 0, uc[4]);
+  t->due_densify = word(2, 0, uc[6]) != 0;
+  t->due_reset = word(2, 0, uc[7]) != 0;
+  for (uint64_t k = 0; k < h.elements[3].count; k++) {
+    const uint32_t view = word(3, k, qc);
+    if (view >= view_count && st == DG_OK) st = fail(DG_ERROR_INVALID_ARGUMENT, "a queued view is out of range");
+    t->queue.push_back(view);
+  }
+  for (uint64_t k = 0; k < h.elements[4].count; k++) {
+    uint32_t f[7];
+    for (int j = 0; j < 7; j++) f[j] = word(4, k, dc[j]);
+    t->densifications.push_back(dg_densification{f[0], f[1], f[2], f[3], f[4], f[5], f[6]});
+  }
+  if (st == DG_OK && degree > 3) st = fail(DG_ERROR_INVALID_ARGUMENT, "SH degree above 3 in the checkpoint");
+  if (st == DG_OK && degree > 0) st = dg_renderer_set_sh_degree(t->renderer, degree);
+  if (st == DG_OK) t->sh_degree = degree;
+  if (st == DG_OK) st = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? DG_OK : fail(DG_ERROR_CUDA, "resume upload");
+  if (st != DG_OK) {
+    dg_trainer_destroy(t);
+    return st;
+  }
+  *out = t;
+  return DG_OK;
+}

@@ -200,20 +200,25 @@ class DensifyMLP:
 class Trainer:
     """Trains Gaussians to match a set of photos, following the reference's loop."""
 
-    def __init__(self, device: Device, raw: RawGaussians, views, settings: TrainingSettings):
+    def __init__(self, device: Device, raw: RawGaussians | None, views, settings: TrainingSettings,
+                 _resume_from: str | None = None):
         self.device = device
         self.views = list(views)
         self.settings = settings
-        params = np.ascontiguousarray(raw.params, np.float32).reshape(-1)
-        sh = np.ascontiguousarray(raw.sh, np.float32).reshape(-1)
-        count = params.size // FLOATS_PER_GAUSSIAN
-        if sh.size != count * SH_REST_FLOATS:
-            raise ValueError(f"Expected {count * SH_REST_FLOATS} spherical-harmonic floats, got {sh.size}.")
         self._views_c = _views_c(self.views)
         cs = settings.to_c()
         handle = c_void_p()
-        _lib.call("dg_trainer_create", device.handle, params.ctypes.data, sh.ctypes.data, count, self._views_c,
-                  len(self.views), ctypes.byref(cs), ctypes.byref(handle))
+        if _resume_from is not None:
+            _lib.call("dg_trainer_resume", device.handle, str(_resume_from).encode(), self._views_c, len(self.views),
+                      ctypes.byref(cs), ctypes.byref(handle))
+        else:
+            params = np.ascontiguousarray(raw.params, np.float32).reshape(-1)
+            sh = np.ascontiguousarray(raw.sh, np.float32).reshape(-1)
+            count = params.size // FLOATS_PER_GAUSSIAN
+            if sh.size != count * SH_REST_FLOATS:
+                raise ValueError(f"Expected {count * SH_REST_FLOATS} spherical-harmonic floats, got {sh.size}.")
+            _lib.call("dg_trainer_create", device.handle, params.ctypes.data, sh.ctypes.data, count, self._views_c,
+                      len(self.views), ctypes.byref(cs), ctypes.byref(handle))
         self.handle = handle
         self.renderer = GaussianRenderer(device, _handle=_lib.fn("dg_trainer_renderer")(handle))
 
@@ -261,6 +266,17 @@ class Trainer:
 
     def resetOpacity(self) -> None:
         _lib.call("dg_trainer_reset_opacity", self.handle)
+
+    @classmethod
+    def resume(cls, device: Device, path, views, settings: TrainingSettings) -> "Trainer":
+        """A trainer in the state saveCheckpoint recorded (no reference counterpart),
+        over the same views in the same order."""
+        return cls(device, None, views, settings, _resume_from=str(path))
+
+    def saveCheckpoint(self, path) -> None:
+        """Writes a .ply that 3DGS viewers open as the current scene and that
+        Trainer.resume continues training from (no reference counterpart)."""
+        _lib.call("dg_trainer_save_checkpoint", self.handle, str(path).encode())
 
     def exportRaw(self) -> RawGaussians:
         n = self.count

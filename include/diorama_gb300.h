@@ -300,6 +300,19 @@ dg_status dg_trainer_set_graph(dg_trainer* t, int32_t enabled);
  * renderer's gradient buffers (gradients{gaussians, sh}), as the reference's
  * separate passes leave them. The parameters are the same either way. */
 dg_status dg_trainer_set_keep_gradients(dg_trainer* t, int32_t enabled);
+/* Checkpoints. No reference counterpart: the reference writes trained Gaussians
+ * (src/plyWriter.ts) but cannot resume. The file is a .ply whose vertex element
+ * starts with writeGaussianPly's 62 properties (so the reference's reader and 3DGS
+ * viewers open it as a scene) and goes on with each Gaussian's training state
+ * (pad floats, Adam moments, densification statistics); further elements hold the
+ * identities, the trainer's counters, the rest of the current round of views and
+ * the densification history. A learned densification model and its sample log
+ * are not part of it. */
+dg_status dg_trainer_save_checkpoint(dg_trainer* t, const char* path);
+/* A trainer in the state a checkpoint recorded, over the same views (the same
+ * number, in the same order) and settings. */
+dg_status dg_trainer_resume(dg_context* ctx, const char* path, const dg_training_view* views, uint32_t view_count,
+                            const dg_training_settings* settings, dg_trainer** out);
 dg_status dg_trainer_destroy(dg_trainer* t);
 
 /* ---- Learned densification proposal. No reference counterpart: the reference
@@ -348,6 +361,20 @@ dg_status dg_trainer_set_densify_mlp(dg_trainer* t, dg_densify_mlp* mlp, float m
 /* Totals over the learned densifications: candidates scored, confident ones,
  * and of those the ones not densified. */
 dg_status dg_trainer_densify_mlp_stats(const dg_trainer* t, uint64_t* scored, uint64_t* confident, uint64_t* vetoed);
+
+/* ---- .ply files (host only; no GPU needed) */
+/* parseGaussianPly (src/plyLoader.ts:21-104): the activated Gaussians of a binary
+ * little-endian 3DGS .ply (gaussians count × 16 f32, packed like packGaussians;
+ * sh_rest count × 45 f32, zero past the file's degree) and its SH degree. With
+ * gaussians = sh_rest = NULL only *count and *sh_degree are set. Fails
+ * (DG_ERROR_INVALID_ARGUMENT, with the reference's message) where it throws. */
+dg_status dg_parse_gaussian_ply(const void* bytes, uint64_t size, uint32_t* count, uint32_t* sh_degree,
+                                float* gaussians, float* sh_rest);
+/* writeGaussianPly (src/plyWriter.ts:14-43): raw params (count × 16) and sh
+ * (count × 45) as .ply bytes. *size gets the file's length; out (capacity bytes)
+ * may be NULL to ask for it. */
+dg_status dg_write_gaussian_ply(const float* params, const float* sh, uint32_t count, void* out, uint64_t capacity,
+                                uint64_t* size);
 
 /* ---- Starting Gaussians from a point cloud (src/loadDataset.ts:93-149). */
 /* meanNeighborDistance2 (src/loadDataset.ts:124-149, src/shaders/nearestNeighbors.wgsl:13-44):
