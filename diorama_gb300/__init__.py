@@ -10,7 +10,9 @@ loaded or no CUDA device is present, creating a Device raises.
 from ._lib import DioramaError
 from .gaussians import (FLOATS_PER_GAUSSIAN, FLOATS_PER_SPLAT, SH_REST_FLOATS, Gaussian, Splat2D, packGaussians,
                         packSplats, unpackSplats)
-from .dataset import initialGaussians, meanNeighborDistance2, meanNeighborDistance2Buffers
+from .dataset import (Dataset, Reconstruction, TrainingCamera, cameraView, initialGaussians, loadDataset, loadViews,
+                      meanNeighborDistance2, meanNeighborDistance2Buffers, parseColmap, splitDataset,
+                      trainingCameraData, verticalFov)
 from .gpu import Buffer, Device, Texture, initGpu, readBuffer
 from .ply import GaussianScene, parseGaussianPly, writeGaussianPly
 from .primitives import PrefixSum, RadixSort
@@ -24,5 +26,6 @@ __all__ = [
     "PrefixSum", "RadixSort", "CameraData", "GaussianRenderer", "SphericalHarmonics", "TileRasterizer",
     "DEFAULT_SETTINGS", "Densification", "DensifyMLP", "RawGaussians", "Trainer", "TrainingLoss", "TrainingSettings",
     "TrainingView", "activate", "GaussianScene", "parseGaussianPly", "writeGaussianPly", "initialGaussians",
-    "meanNeighborDistance2", "meanNeighborDistance2Buffers",
+    "meanNeighborDistance2", "meanNeighborDistance2Buffers", "Dataset", "Reconstruction", "TrainingCamera",
+    "cameraView", "loadDataset", "loadViews", "parseColmap", "splitDataset", "trainingCameraData", "verticalFov",
 ]

@@ -55,6 +55,12 @@ class TrainingSettingsC(ctypes.Structure):
     ]
 
 
+class TrainingCameraC(ctypes.Structure):
+    _fields_ = [("name", c_char_p), ("width", c_double), ("height", c_double), ("position", c_double * 3),
+                ("right", c_double * 3), ("down", c_double * 3), ("forward", c_double * 3), ("fx", c_double),
+                ("fy", c_double)]
+
+
 class TrainingViewC(ctypes.Structure):
     _fields_ = [("camera", Camera), ("image", c_void_p)]
 
@@ -179,6 +185,12 @@ SIGNATURES = {
     "dg_trainer_resume": (None, [_P, c_char_p, c_void_p, c_uint32, c_void_p, POINTER(_P)]),
     "dg_parse_gaussian_ply": (None, [c_void_p, c_uint64, POINTER(c_uint32), POINTER(c_uint32), c_void_p, c_void_p]),
     "dg_write_gaussian_ply": (None, [c_void_p, c_void_p, c_uint32, c_void_p, c_uint64, POINTER(c_uint64)]),
+    "dg_parse_colmap": (None, [c_void_p, c_uint64, c_void_p, c_uint64, c_void_p, c_uint64, POINTER(_P)]),
+    "dg_colmap_camera_count": (c_uint32, [_P]),
+    "dg_colmap_camera": (None, [_P, c_uint32, POINTER(TrainingCameraC)]),
+    "dg_colmap_point_count": (c_uint64, [_P]),
+    "dg_colmap_points": (None, [_P, c_void_p, c_void_p]),
+    "dg_colmap_destroy": (None, [_P]),
     "dg_mean_neighbor_distance2": (None, [_P, c_void_p, c_uint32, c_void_p]),
     "dg_mean_neighbor_distance2_buffers": (None, [_P, _P, c_uint32, _P]),
     "dg_initial_gaussians": (None, [_P, c_void_p, c_void_p, c_uint32, c_void_p, c_void_p]),

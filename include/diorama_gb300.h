@@ -376,6 +376,28 @@ dg_status dg_parse_gaussian_ply(const void* bytes, uint64_t size, uint32_t* coun
 dg_status dg_write_gaussian_ply(const float* params, const float* sh, uint32_t count, void* out, uint64_t capacity,
                                 uint64_t* size);
 
+/* ---- COLMAP sparse reconstructions (host only; no GPU needed) */
+typedef struct dg_colmap dg_colmap;
+/* TrainingCamera (src/sceneCameras.ts:6-19): a photo's name, size, centre, axes in
+ * world space (x right, y down, z forward) and focal lengths in pixels. */
+typedef struct dg_training_camera {
+  const char* name; /* owned by the reconstruction it came from */
+  double width, height;
+  double position[3], right[3], down[3], forward[3];
+  double fx, fy;
+} dg_training_camera;
+/* parseColmap (src/colmap.ts:18-31): the contents of cameras.bin, images.bin and
+ * points3D.bin. Cameras come sorted by photo name; only SIMPLE_PINHOLE and
+ * PINHOLE camera models are accepted, as in the reference. */
+dg_status dg_parse_colmap(const void* cameras_bin, uint64_t cameras_size, const void* images_bin,
+                          uint64_t images_size, const void* points_bin, uint64_t points_size, dg_colmap** out);
+uint32_t dg_colmap_camera_count(const dg_colmap* r);
+dg_status dg_colmap_camera(const dg_colmap* r, uint32_t index, dg_training_camera* out);
+uint64_t dg_colmap_point_count(const dg_colmap* r);
+/* positions: count × 3 f32; colors: count × 3 u8. */
+dg_status dg_colmap_points(const dg_colmap* r, float* positions, uint8_t* colors);
+dg_status dg_colmap_destroy(dg_colmap* r);
+
 /* ---- Starting Gaussians from a point cloud (src/loadDataset.ts:93-149). */
 /* meanNeighborDistance2 (src/loadDataset.ts:124-149, src/shaders/nearestNeighbors.wgsl:13-44):
  * distance2[i] = the mean of the squared distances from point i to its 3 nearest
