@@ -182,7 +182,7 @@ def build_scene(args):
 # `ncu --set full --clock-control none` capture of each kernel at 1.1M Gaussians
 # (`python bench.py --steps 2 --warmup 3 --views 8 --no-cpu-baseline --no-graph
 # --no-held-out`, one launch, `-k regex:<kernel> -s 3 -c 1`).
-NCU_TRAFFIC = {"preprocess": 134_020_864}
+NCU_TRAFFIC = {"preprocess_backward_adam": 1_943_093_760, "preprocess": 134_020_864}
 
 
 # Algorithmic bytes per unit: what each kernel must move at minimum.
@@ -190,7 +190,9 @@ def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, pa
     return {
         # The preprocess backward fused with Adam: read the activated Gaussian 64, SH 180,
         # splat gradients 36 and visibility 4, raw parameters 56 and moments 472 (59 used
-        # slots); write SH 180, parameters 56, moments 472 and activated values 56.
+        # slots); write SH 180, parameters 56, moments 472 and activated values 56. The
+        # densification statistics it also updates (up to 48 B, for drawn Gaussians
+        # only) are not counted.
         "preprocess_backward_adam": 1576.0 * n,
         "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
         "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
