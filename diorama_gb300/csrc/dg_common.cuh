@@ -187,6 +187,48 @@ __host__ __device__ __forceinline__ float exp_blend(float x) {
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
+// Two float32 values in one 64-bit register, for Blackwell's packed FP32
+// instructions: each lane of add/mul/fma .rn.f32x2 rounds exactly as the scalar
+// add/mul/fma .rn.f32 does (subnormals kept), so two independent sums advance in
+// one instruction per step with the same results. Unlike the scalar forms, a
+// packed multiply whose result feeds a packed add may be contracted by the
+// assembler into one fused multiply-add: write f2_fma where a product is added.
+struct F2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ F2 f2_load(const float2* p) { return F2{*reinterpret_cast<const unsigned long long*>(p)}; }
+__device__ __forceinline__ void f2_store(float2* p, F2 a) { *reinterpret_cast<unsigned long long*>(p) = a.v; }
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+  F2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  F2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 f2_fma(F2 a, F2 b, F2 c) {
+  F2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+__device__ __forceinline__ float f2_lo(F2 a) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  return lo;
+}
+__device__ __forceinline__ float f2_hi(F2 a) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  return hi;
+}
+
 constexpr float SH_C0 = 0.28209479177387814f;
 constexpr float SH_C1 = 0.4886025119029199f;
 

@@ -9,9 +9,9 @@
 // once, and does the separable blurs in shared memory:
 //   ssim_kernel:     moments -> blur h -> blur v -> SSIM and its three partials
 //   gradient_kernel: partials -> blur h -> blur v -> dL/dpixel and the pixel loss
-// Sums run over the taps -5..5 in order; taps past the image add exactly 0 (the
-// halo holds zeros there), the same as the WGSL's skipping them, so the values
-// are the reference's float32 values.
+// Sums run over the taps -5..5 in order, one fused multiply-add per tap (two
+// sums per packed FP32 instruction where they pair up); taps past the image add
+// exactly 0 (the halo holds zeros there), the same as the WGSL's skipping them.
 //
 // The same ssim_kernel also measures held-out renders (PSNR and SSIM of the
 // 8-bit-quantized image, src/trainer.ts:371-386 and src/metrics.ts) on the GPU.
@@ -56,16 +56,21 @@ __device__ __forceinline__ float3 load_y(const uchar4* target, int w, int h, int
 }
 
 // Moments, both blurs and the SSIM partials for one 16x16 block. mode 0 (loss):
-// writes the three partials and S per channel to `partials` (12 floats per pixel:
-// dS/dmu_x rgb, dS/dE[x^2] rgb, dS/dE[xy] rgb, S rgb). mode 1 (metrics): the render
-// is quantized first, and each CTA adds its Σ S and Σ squared error to `sums`.
+// writes the three partials and S per channel to `partials` (12 floats per pixel,
+// laid out for the gradient pass's paired loads: (dS/dmu_x, dS/dE[x^2]) for r, g, b,
+// then dS/dE[xy] rgb, then S rgb). mode 1 (metrics): the render is quantized
+// first, and each CTA adds its Σ S and Σ squared error to `sums`.
+//
+// The x and y sums of each blur, and the x^2 and y^2 ones, run as pairs through
+// packed FP32 fused multiply-adds (F2): each lane is the scalar fmaf sum.
 __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ rendered,
                                                    const uchar4* const* __restrict__ target_slot, int w, int h,
                                                    Window win, float* __restrict__ partials, int mode,
                                                    double* __restrict__ sums) {
-  __shared__ float s_x[LS][LS][3];
-  __shared__ float s_y[LS][LS][3];
-  __shared__ float s_h[5][LS][LT][3];
+  __shared__ float2 s_xy[LS][LS][3];   // (x, y) per halo pixel and channel
+  __shared__ float2 s_h01[LS][LT][3];  // horizontal blurs of x and y
+  __shared__ float2 s_h23[LS][LT][3];  // of x^2 and y^2
+  __shared__ float s_h4[LS][LT][3];    // of xy
   __shared__ double s_red[2][8];
   const uchar4* target = *target_slot;
   const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
@@ -74,31 +79,32 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
     const int ly = k / LS, lx = k % LS;
     float3 xv = load_x(rendered, w, h, x0 + lx, y0 + ly, metrics);
     float3 yv = load_y(target, w, h, x0 + lx, y0 + ly, metrics);
-    s_x[ly][lx][0] = xv.x; s_x[ly][lx][1] = xv.y; s_x[ly][lx][2] = xv.z;
-    s_y[ly][lx][0] = yv.x; s_y[ly][lx][1] = yv.y; s_y[ly][lx][2] = yv.z;
+    s_xy[ly][lx][0] = make_float2(xv.x, yv.x);
+    s_xy[ly][lx][1] = make_float2(xv.y, yv.y);
+    s_xy[ly][lx][2] = make_float2(xv.z, yv.z);
   }
+  F2 wp[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) wp[k] = f2(win.w[k], win.w[k]);
   __syncthreads();
   // Horizontal pass over every halo row, for the 16 output columns.
   for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
     const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f;
+    F2 a01 = f2(0.f, 0.f), a23 = f2(0.f, 0.f);
+    float a4 = 0.f;
     // Taps past the image read the halo's zeros and add exactly 0: the same sums
     // as skipping them, without a branch per tap.
 #pragma unroll
     for (int t = -HALO; t <= HALO; t++) {
-      const float wt = win.w[t < 0 ? -t : t];
-      const float xv = s_x[row][col + HALO + t][ch], yv = s_y[row][col + HALO + t][ch];
-      a0 = a0 + wt * xv;
-      a1 = a1 + wt * yv;
-      a2 = a2 + wt * (xv * xv);
-      a3 = a3 + wt * (yv * yv);
-      a4 = a4 + wt * (xv * yv);
+      const int at = t < 0 ? -t : t;
+      const F2 xy = f2_load(&s_xy[row][col + HALO + t][ch]);
+      a01 = f2_fma(wp[at], xy, a01);                // x, y
+      a23 = f2_fma(wp[at], f2_mul(xy, xy), a23);    // x^2, y^2
+      a4 = fmaf(win.w[at], f2_lo(xy) * f2_hi(xy), a4);  // xy
     }
-    s_h[0][row][col][ch] = a0;
-    s_h[1][row][col][ch] = a1;
-    s_h[2][row][col][ch] = a2;
-    s_h[3][row][col][ch] = a3;
-    s_h[4][row][col][ch] = a4;
+    f2_store(&s_h01[row][col][ch], a01);
+    f2_store(&s_h23[row][col][ch], a23);
+    s_h4[row][col][ch] = a4;
   }
   __syncthreads();
   const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
@@ -109,26 +115,28 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
     float out[12];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
-      float m[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      F2 m01 = f2(0.f, 0.f), m23 = f2(0.f, 0.f);
+      float m4 = 0.f;
 #pragma unroll
       for (int t = -HALO; t <= HALO; t++) {  // rows past the image were blurred to 0
-        const float wt = win.w[t < 0 ? -t : t];
-#pragma unroll
-        for (int q = 0; q < 5; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
+        const int at = t < 0 ? -t : t;
+        m01 = f2_fma(wp[at], f2_load(&s_h01[ly + HALO + t][lx][ch]), m01);
+        m23 = f2_fma(wp[at], f2_load(&s_h23[ly + HALO + t][lx][ch]), m23);
+        m4 = fmaf(win.w[at], s_h4[ly + HALO + t][lx][ch], m4);
       }
-      const float mx = m[0], my = m[1];
-      const float vx = m[2] - mx * mx, vy = m[3] - my * my, cxy = m[4] - mx * my;
+      const float mx = f2_lo(m01), my = f2_hi(m01);
+      const float vx = f2_lo(m23) - mx * mx, vy = f2_hi(m23) - my * my, cxy = m4 - mx * my;
       const float a1 = 2.0f * mx * my + C1, a2 = 2.0f * cxy + C2;
       const float b1 = mx * mx + my * my + C1, b2 = vx + vy + C2;
       const float s = a1 * a2 / (b1 * b2);
-      out[ch] = s * (2.0f * my / a1 - 2.0f * my / a2 - 2.0f * mx / b1 + 2.0f * mx / b2);
-      out[3 + ch] = -s / b2;
+      out[2 * ch] = s * (2.0f * my / a1 - 2.0f * my / a2 - 2.0f * mx / b1 + 2.0f * mx / b2);
+      out[2 * ch + 1] = -s / b2;
       out[6 + ch] = 2.0f * s / a2;
       out[9 + ch] = s;
       if (metrics) {
         s_sum += (double)s;
-        const float xv = s_x[ly + HALO][lx + HALO][ch], yv = s_y[ly + HALO][lx + HALO][ch];
-        const double d = (double)xv - (double)yv;
+        const float2 xy = s_xy[ly + HALO][lx + HALO][ch];
+        const double d = (double)xy.x - (double)xy.y;
         se_sum += d * d;
       }
     }
@@ -163,37 +171,52 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
 }
 
 // Blurs the three partials and forms dL/dpixel and the pixel loss
-// (src/shaders/loss.wgsl:108-121).
+// (src/shaders/loss.wgsl:108-121). The first two partials' blurs run as a pair
+// of packed FP32 sums.
 __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict__ rendered,
                                                        const uchar4* const* __restrict__ target_slot, int w, int h,
                                                        Window win, const float* __restrict__ partials,
                                                        float4* __restrict__ pixel_grads, float* __restrict__ pixel_loss) {
-  __shared__ float s_p[3][LS][LS][3];
-  __shared__ float s_h[3][LS][LT][3];
+  __shared__ float2 s_p01[LS][LS][3];
+  __shared__ float s_p2[LS][LS][3];
+  __shared__ float2 s_h01[LS][LT][3];
+  __shared__ float s_h2[LS][LT][3];
   const uchar4* target = *target_slot;
   const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
   for (int k = threadIdx.x; k < LS * LS; k += 256) {
     const int ly = k / LS, lx = k % LS;
     const int gx = x0 + lx, gy = y0 + ly;
     const bool in = gx >= 0 && gy >= 0 && gx < w && gy < h;
-    const float* src = partials + ((size_t)gy * w + gx) * 12;
-#pragma unroll
-    for (int q = 0; q < 3; q++)
-#pragma unroll
-      for (int ch = 0; ch < 3; ch++) s_p[q][ly][lx][ch] = in ? src[q * 3 + ch] : 0.0f;
+    float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0, q2 = q0;
+    if (in) {
+      const float4* src = reinterpret_cast<const float4*>(partials + ((size_t)gy * w + gx) * 12);
+      q0 = src[0];
+      q1 = src[1];
+      q2 = src[2];
+    }
+    s_p01[ly][lx][0] = make_float2(q0.x, q0.y);
+    s_p01[ly][lx][1] = make_float2(q0.z, q0.w);
+    s_p01[ly][lx][2] = make_float2(q1.x, q1.y);
+    s_p2[ly][lx][0] = q1.z;
+    s_p2[ly][lx][1] = q1.w;
+    s_p2[ly][lx][2] = q2.x;
   }
+  F2 wp[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) wp[k] = f2(win.w[k], win.w[k]);
   __syncthreads();
   for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
     const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    float a[3] = {0.f, 0.f, 0.f};
+    F2 a01 = f2(0.f, 0.f);
+    float a2 = 0.f;
 #pragma unroll
     for (int t = -HALO; t <= HALO; t++) {  // the halo holds zeros past the image
-      const float wt = win.w[t < 0 ? -t : t];
-#pragma unroll
-      for (int q = 0; q < 3; q++) a[q] = a[q] + wt * s_p[q][row][col + HALO + t][ch];
+      const int at = t < 0 ? -t : t;
+      a01 = f2_fma(wp[at], f2_load(&s_p01[row][col + HALO + t][ch]), a01);
+      a2 = fmaf(win.w[at], s_p2[row][col + HALO + t][ch], a2);
     }
-#pragma unroll
-    for (int q = 0; q < 3; q++) s_h[q][row][col][ch] = a[q];
+    f2_store(&s_h01[row][col][ch], a01);
+    s_h2[row][col][ch] = a2;
   }
   __syncthreads();
   const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
@@ -210,15 +233,16 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
   float lsum = 0.0f;
 #pragma unroll
   for (int ch = 0; ch < 3; ch++) {
-    float m[3] = {0.f, 0.f, 0.f};
+    F2 m01 = f2(0.f, 0.f);
+    float m2 = 0.f;
 #pragma unroll
     for (int t = -HALO; t <= HALO; t++) {  // rows past the image were blurred to 0
-      const float wt = win.w[t < 0 ? -t : t];
-#pragma unroll
-      for (int q = 0; q < 3; q++) m[q] = m[q] + wt * s_h[q][ly + HALO + t][lx][ch];
+      const int at = t < 0 ? -t : t;
+      m01 = f2_fma(wp[at], f2_load(&s_h01[ly + HALO + t][lx][ch]), m01);
+      m2 = fmaf(win.w[at], s_h2[ly + HALO + t][lx][ch], m2);
     }
     const float x = xs[ch], y = ys[ch];
-    const float sg = m[0] + 2.0f * x * m[1] + y * m[2];
+    const float sg = f2_lo(m01) + 2.0f * x * f2_hi(m01) + y * m2;
     const float diff = x - y;
     const float sign = diff > 0.0f ? 1.0f : (diff < 0.0f ? -1.0f : 0.0f);
     grad[ch] = ((1.0f - LAMBDA) * sign - LAMBDA * sg) * scale;

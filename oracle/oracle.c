@@ -805,7 +805,9 @@ static void window_weights(float w[6]) {
 }
 
 /* One direction of the separable blur over `maps` planar float maps of w*h*3
- * (pixel-major, rgb): src/shaders/loss.wgsl:68-84. */
+ * (pixel-major, rgb): src/shaders/loss.wgsl:68-84. Each tap is one fused
+ * multiply-add (written out as fmaf, which the WGSL's `sum + w * v` permits):
+ * the GPU's blurs run two sums per packed FMA instruction. */
 static void blur(const float* in, float* out, int maps, int w, int h, int horizontal, const float wt[6]) {
   size_t n = (size_t)w * h;
   for (int m = 0; m < maps; m++) {
@@ -817,7 +819,7 @@ static void blur(const float* in, float* out, int maps, int w, int h, int horizo
           for (int k = -5; k <= 5; k++) {
             int ax = horizontal ? x + k : x, ay = horizontal ? y : y + k;
             if (ax >= 0 && ay >= 0 && ax < w && ay < h)
-              sum = sum + wt[k < 0 ? -k : k] * in[(m * n + (size_t)ay * w + ax) * 3 + ch];
+              sum = fmaf(wt[k < 0 ? -k : k], in[(m * n + (size_t)ay * w + ax) * 3 + ch], sum);
           }
           out[(m * n + (size_t)y * w + x) * 3 + ch] = sum;
         }
