@@ -187,6 +187,7 @@ __host__ __device__ __forceinline__ float exp_blend(float x) {
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
+#ifdef __CUDACC__  // device code below; host-only translation units skip it
 // Two float32 values in one 64-bit register, for Blackwell's packed FP32
 // instructions: each lane of add/mul/fma .rn.f32x2 rounds exactly as the scalar
 // add/mul/fma .rn.f32 does (subnormals kept), so two independent sums advance in
@@ -228,6 +229,27 @@ __device__ __forceinline__ float f2_hi(F2 a) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
   return hi;
 }
+
+// exp_blend_core of two values at once: the polynomial's fused multiply-adds run
+// as packed pairs, each lane the same fmaf as exp_blend_core's, so both results
+// are exp_blend_core's bit for bit.
+__device__ __forceinline__ void exp_blend_core2(float x0, float x1, float& e0, float& e1) {
+  const float n0 = rintf(x0 * 1.44269504088896341f), n1 = rintf(x1 * 1.44269504088896341f);
+  const F2 n = f2(n0, n1);
+  F2 r = f2_fma(n, f2(-0.693145751953125f, -0.693145751953125f), f2(x0, x1));
+  r = f2_fma(n, f2(-1.428606820309417232e-6f, -1.428606820309417232e-6f), r);
+  F2 p = f2(1.98412698412698413e-4f, 1.98412698412698413e-4f);
+  p = f2_fma(p, r, f2(1.38888888888888889e-3f, 1.38888888888888889e-3f));
+  p = f2_fma(p, r, f2(8.33333333333333333e-3f, 8.33333333333333333e-3f));
+  p = f2_fma(p, r, f2(4.16666666666666667e-2f, 4.16666666666666667e-2f));
+  p = f2_fma(p, r, f2(1.66666666666666667e-1f, 1.66666666666666667e-1f));
+  p = f2_fma(p, r, f2(0.5f, 0.5f));
+  p = f2_fma(p, r, f2(1.0f, 1.0f));
+  p = f2_fma(p, r, f2(1.0f, 1.0f));
+  e0 = f2_lo(p) * __int_as_float(((int32_t)n0 + 127) << 23);
+  e1 = f2_hi(p) * __int_as_float(((int32_t)n1 + 127) << 23);
+}
+#endif  // __CUDACC__
 
 constexpr float SH_C0 = 0.28209479177387814f;
 constexpr float SH_C1 = 0.4886025119029199f;

@@ -474,9 +474,12 @@ struct PixelBlend {
       for (uint32_t u = 0; u < 4; u++) alpha[u] = 0.0f;
       return false;
     }
+    float G[4];
+    exp_blend_core2(need[0] ? power[0] : 0.0f, need[1] ? power[1] : 0.0f, G[0], G[1]);
+    exp_blend_core2(need[2] ? power[2] : 0.0f, need[3] ? power[3] : 0.0f, G[2], G[3]);
 #pragma unroll
     for (uint32_t u = 0; u < 4; u++) {
-      const float a = fminf(0.99f, st.color[e[u]].w * exp_blend_core(need[u] ? power[u] : 0.0f));
+      const float a = fminf(0.99f, st.color[e[u]].w * G[u]);
       alpha[u] = need[u] && a >= 1.0f / 255.0f ? a : 0.0f;
     }
     return true;

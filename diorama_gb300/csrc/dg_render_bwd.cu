@@ -87,18 +87,24 @@ struct BlendTerm {
   bool blended;
 };
 
-__device__ __forceinline__ BlendTerm blend_term(const WarpStage& st, uint32_t e, bool eligible, float cx, float cy) {
-  BlendTerm t;
-  const float2 m = st.mean[e];
-  const float4 q = st.quad[e];
-  t.dx = cx - m.x;
-  t.dy = cy - m.y;
-  const float power = blend_power(q.x, q.y, q.z, t.dx, t.dy);
-  const bool need = eligible && power >= q.w && power <= 0.0f;
-  t.G = exp_blend_core(need ? power : 0.0f);
-  t.alpha = fminf(0.99f, __fmul_rn(st.color[e].w, t.G));
-  t.blended = need && t.alpha >= 1.0f / 255.0f;
-  return t;
+// The terms of two entries at once (their exps as one packed pair).
+__device__ __forceinline__ void blend_terms(const WarpStage& st, uint32_t e0, uint32_t e1, bool eligible0,
+                                            bool eligible1, float cx, float cy, BlendTerm& t0, BlendTerm& t1) {
+  const float2 m0 = st.mean[e0], m1 = st.mean[e1];
+  const float4 q0 = st.quad[e0], q1 = st.quad[e1];
+  t0.dx = cx - m0.x;
+  t0.dy = cy - m0.y;
+  t1.dx = cx - m1.x;
+  t1.dy = cy - m1.y;
+  const float power0 = blend_power(q0.x, q0.y, q0.z, t0.dx, t0.dy);
+  const float power1 = blend_power(q1.x, q1.y, q1.z, t1.dx, t1.dy);
+  const bool need0 = eligible0 && power0 >= q0.w && power0 <= 0.0f;
+  const bool need1 = eligible1 && power1 >= q1.w && power1 <= 0.0f;
+  exp_blend_core2(need0 ? power0 : 0.0f, need1 ? power1 : 0.0f, t0.G, t1.G);
+  t0.alpha = fminf(0.99f, __fmul_rn(st.color[e0].w, t0.G));
+  t1.alpha = fminf(0.99f, __fmul_rn(st.color[e1].w, t1.G));
+  t0.blended = need0 && t0.alpha >= 1.0f / 255.0f;
+  t1.blended = need1 && t1.alpha >= 1.0f / 255.0f;
 }
 
 // A pixel's state on its back-to-front walk: the transmittance in front of the
@@ -268,8 +274,8 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
         const uint32_t j0 = slot - 1, j1 = slot >= 2 ? slot - 2 : j0;
         const bool pair = slot >= 2;
         slot = pair ? slot - 2 : 0;
-        const BlendTerm t0 = blend_term(st, j0, inside && st.pos[j0] < last, cx, cy);
-        const BlendTerm t1 = blend_term(st, j1, pair && inside && st.pos[j1] < last, cx, cy);
+        BlendTerm t0, t1;
+        blend_terms(st, j0, j1, inside && st.pos[j0] < last, pair && inside && st.pos[j1] < last, cx, cy, t0, t1);
         if (!__any_sync(0xffffffffu, t0.blended || t1.blended)) continue;
         float v[2 * SPLAT_GRADS];
 #pragma unroll
