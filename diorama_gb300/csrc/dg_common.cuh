@@ -220,13 +220,13 @@ __device__ __forceinline__ F2 f2_fma(F2 a, F2 b, F2 c) {
   return r;
 }
 __device__ __forceinline__ float f2_lo(F2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  float lo;
+  asm("{\n\t.reg .b32 hi;\n\tmov.b64 {%0, hi}, %1;\n\t}" : "=f"(lo) : "l"(a.v));
   return lo;
 }
 __device__ __forceinline__ float f2_hi(F2 a) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+  float hi;
+  asm("{\n\t.reg .b32 lo;\n\tmov.b64 {lo, %0}, %1;\n\t}" : "=f"(hi) : "l"(a.v));
   return hi;
 }
 

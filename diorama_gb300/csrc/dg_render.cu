@@ -575,11 +575,13 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 // bit-identical to it; the split only decides who does the work:
 //
 // - Tiles with more entries than the plan's threshold (COOP_MIN unless tuned)
-//   come first, each block blended by a whole CTA. Its warps take consecutive
-//   32-entry windows, keep the splats that can reach the block and compute their
-//   alphas at the block's pixels, queueing those some pixel blends; warp 0 then
-//   applies the queued alphas of all the windows in list order. The costly part of each splat (power, exp, alpha) is
-//   spread over the CTA; only the short transmittance update stays serial.
+//   come first, each block blended by a whole CTA. Three of its warps take
+//   consecutive 32-entry windows, keep the splats that can reach the block and
+//   compute their alphas at the block's pixels, queueing those some pixel blends;
+//   warp 0 applies the queues in list order one round behind, so the alphas of the
+//   next 96 entries are computed while it blends. The costly part of each splat
+//   (power, exp, alpha) is spread over the CTA; only the short transmittance update
+//   stays serial, and it overlaps the rest.
 // - Every warp then takes the other blocks on its own, walking the list 32
 //   entries at a time.
 //
@@ -595,7 +597,12 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     uint32_t* __restrict__ pixel_last, float4* __restrict__ checkpoints, uint32_t* __restrict__ blend_mask,
     uint32_t* __restrict__ counters) {
   __shared__ WarpStage stages[FWD_WARPS];
-  __shared__ float s_alpha[FWD_WARPS][32][32];  // cooperative: alphas of each warp's queued entries
+  // Cooperative blending, double-buffered by round: each producer's queued entries
+  // (alpha per pixel, colour, position) and their count.
+  __shared__ float s_alpha[2][PRODUCERS][32][32];
+  __shared__ float4 s_qcolor[2][PRODUCERS][32];
+  __shared__ uint32_t s_qpos[2][PRODUCERS][32];
+  __shared__ uint32_t s_qlive[2][PRODUCERS];
   __shared__ uint32_t s_item, s_stop, s_done;  // s_done: warp 0's pixels that have stopped
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   WarpStage& st = stages[warp];
@@ -605,12 +612,19 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
   const uint32_t cooperative = plan[0], tiles = plan[1];
   const uint32_t* order = plan + PLAN_HEADER;
 
-  // Cooperative items: one block of a long tile per CTA.
+  // Cooperative items: one block of a long tile per CTA. Warps 1..PRODUCERS take
+  // consecutive 32-entry windows of round r (window pw of the round is producer
+  // pw's), keep the splats that can reach the block, compute their alphas at the
+  // 32 pixels and queue the entries some pixel blends into buffer r % 2; warp 0
+  // meanwhile applies round r - 1's queues, window by window in list order. One
+  // barrier per round hands the buffers over.
+  constexpr uint32_t STRIDE = 32u * PRODUCERS;  // entries per round
   while (true) {
     __syncthreads();  // everyone has read the previous s_item
     if (threadIdx.x == 0) {
       s_item = atomicAdd(&counters[0], 1u);
       s_done = 0;
+      s_stop = 0;
     }
     __syncthreads();
     const uint32_t item = s_item;
@@ -620,85 +634,75 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const uint2 run = it.run;
     PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
     uint32_t next_k = 1;  // the next checkpoint boundary (warp 0)
-    // Warp w takes windows w, w + FWD_WARPS, ...: this lane's entry of the window
-    // in flight and of the one after it.
+    const uint32_t pw = warp - 1u;  // producer index (warps >= 1)
+    // This producer lane's entry of the window in flight and of the one after it.
     uint32_t index = 0, next_index = 0;
-    {
-      const uint32_t k = run.x + 32u * warp + lane;
+    if (warp > 0) {
+      const uint32_t k = run.x + 32u * pw + lane;
       if (k < run.y) index = pair_splats[k];
       stage_issue(st, splats, index, k < run.y);
-      if (k + 32u * FWD_WARPS < run.y) next_index = pair_splats[k + 32u * FWD_WARPS];
+      if (k + STRIDE < run.y) next_index = pair_splats[k + STRIDE];
     }
-    for (uint32_t round = run.x; round < run.y; round += 32u * FWD_WARPS) {
-      const uint32_t start = round + 32u * warp;
-      if (start < run.y) {
-        const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
-        {
-          const uint32_t k = start + 32u * FWD_WARPS + lane;
-          stage_issue(st, splats, next_index, k < run.y);
-          index = next_index;
-          next_index = k + 32u * FWD_WARPS < run.y ? pair_splats[k + 32u * FWD_WARPS] : 0u;
-        }
-        // The alphas of the kept entries at the block's pixels; entries no pixel
-        // blends are dropped, the others queued with their alphas for warp 0 and
-        // marked in the blend mask (pixels warp 0 had stopped by the last round
-        // take no part).
-        uint32_t live = 0, blended = 0;
-        for (uint32_t j = 0; j < staged; j += 4) {
-          const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
-          float alpha[4];
-          if (!pb.alphas4(st, e, staged - j, it.inside && !((s_done >> lane) & 1u), alpha)) continue;
-          float4 color[4];
-          uint32_t pos[4];
-#pragma unroll
-          for (uint32_t u = 0; u < 4; u++) {
-            color[u] = st.color[e[u]];
-            pos[u] = st.pos[e[u]];
+    const uint32_t rounds = (run.y - run.x + STRIDE - 1u) / STRIDE;
+    for (uint32_t r = 0; r <= rounds; r++) {
+      const uint32_t buf = r & 1u;
+      if (warp > 0) {
+        const uint32_t start = run.x + r * STRIDE + 32u * pw;
+        if (r < rounds && start < run.y) {
+          const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
+          {
+            const uint32_t k = start + STRIDE + lane;
+            stage_issue(st, splats, next_index, k < run.y);
+            index = next_index;
+            next_index = k + STRIDE < run.y ? pair_splats[k + STRIDE] : 0u;
           }
-          __syncwarp();
-          // Queued entries are compacted in place (slot live <= j + u, whose own
-          // entry has been read): colour and position in list order, so warp 0
-          // reads them without going through an index.
+          // Pixels warp 0 has stopped take no part (it publishes the mask after
+          // each window it applies; the mask only grows, so a stale copy only
+          // keeps an entry that a fresh one would drop).
+          uint32_t live = 0, blended = 0;
+          for (uint32_t j = 0; j < staged; j += 4) {
+            const uint32_t e[4] = {j, min(j + 1, staged - 1), min(j + 2, staged - 1), min(j + 3, staged - 1)};
+            const uint32_t done_mask = *reinterpret_cast<volatile uint32_t*>(&s_done);
+            const bool active = it.inside && !((done_mask >> lane) & 1u);
+            float alpha[4];
+            if (!pb.alphas4(st, e, staged - j, active, alpha)) continue;
 #pragma unroll
-          for (uint32_t u = 0; u < 4; u++) {
-            if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
-              if (lane == 0) {
-                st.color[live] = color[u];
-                st.pos[live] = pos[u];
+            for (uint32_t u = 0; u < 4; u++) {
+              if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
+                if (lane == 0) {
+                  s_qcolor[buf][pw][live] = st.color[e[u]];
+                  s_qpos[buf][pw][live] = st.pos[e[u]];
+                }
+                s_alpha[buf][pw][live][lane] = alpha[u];
+                blended |= 1u << (st.pos[e[u]] - (start - run.x));
+                live++;
               }
-              s_alpha[warp][live][lane] = alpha[u];
-              blended |= 1u << (pos[u] - (start - run.x));
-              live++;
             }
           }
-          __syncwarp();
+          if (lane == 0) {
+            s_qlive[buf][pw] = live;
+            publish_blended(blend_mask, start, block, blended);
+          }
+        } else if (lane == 0) {
+          s_qlive[buf][pw] = 0;
         }
-        if (lane == 0) {
-          st.live_count = live;
-          publish_blended(blend_mask, start, block, blended);
-        }
-      } else if (lane == 0) {
-        st.live_count = 0;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        for (uint32_t w = 0; w < FWD_WARPS; w++) {
-          const uint32_t ws = round + 32u * w;
+      } else if (r > 0) {
+        // Warp 0: round r - 1, in list order.
+        const uint32_t prev = buf ^ 1u;
+        for (uint32_t w = 0; w < PRODUCERS; w++) {
+          const uint32_t ws = run.x + (r - 1u) * STRIDE + 32u * w;
           if (ws >= run.y) break;
           if (ws - run.x == next_k * CHUNK) {
             save_checkpoints(checkpoints, run.x, next_k, next_k + 1, block, lane, pb.T, pb.r, pb.g, pb.b);
             next_k++;
           }
-          const WarpStage& sw = stages[w];
-          const uint32_t n = sw.live_count;
+          const uint32_t n = s_qlive[prev][w];
 #pragma unroll 4
-          for (uint32_t m = 0; m < n; m++) pb.blend(s_alpha[w][m][lane], sw.color[m], sw.pos[m]);
+          for (uint32_t m = 0; m < n; m++) pb.blend(s_alpha[prev][w][m][lane], s_qcolor[prev][w][m], s_qpos[prev][w][m]);
+          const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
+          if (lane == 0) *reinterpret_cast<volatile uint32_t*>(&s_done) = done;
         }
-        const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
-        if (lane == 0) {
-          s_stop = done == 0xffffffffu;
-          s_done = done;
-        }
+        if (lane == 0) s_stop = s_done == 0xffffffffu;
       }
       __syncthreads();
       if (s_stop) break;

@@ -243,6 +243,7 @@ __device__ __forceinline__ bool rect_reachable(float A, float b, float C, float 
 // together; otherwise every warp takes items of its own.
 constexpr uint32_t FWD_THREADS = 128;
 constexpr uint32_t FWD_WARPS = FWD_THREADS / 32;
+constexpr uint32_t PRODUCERS = FWD_WARPS - 1;  // cooperative blending: warps computing alphas for warp 0
 constexpr uint32_t BWD_THREADS = 128;
 constexpr uint32_t BWD_WARPS = BWD_THREADS / 32;
 // The backward pass walks a tile's list in chunks of CHUNK entries, each starting
