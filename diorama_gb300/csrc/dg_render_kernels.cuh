@@ -251,7 +251,7 @@ constexpr uint32_t BWD_WARPS = BWD_THREADS / 32;
 // CHUNK entries). A multiple of the 32-entry window.
 constexpr uint32_t CHUNK = 512;
 // Tiles with more entries than this are blended by a whole CTA in the forward pass.
-constexpr uint32_t COOP_MIN = 512;
+constexpr uint32_t COOP_MIN = 128;
 // The frame's work plan (dg_render.cu, plan_kernel): a header of PLAN_HEADER
 // words (cooperative tiles, tiles, backward chunks, spare), the tiles in the
 // order the forward pass takes them, then the backward's (tile, chunk) pairs.

@@ -320,7 +320,7 @@ dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint3
   std::vector<uint32_t> batches;
   for (uint32_t b : {1u, 4u, 8u, 16u, 32u, count})
     if (b <= count && std::find(batches.begin(), batches.end(), b) == batches.end()) batches.push_back(b);
-  const uint32_t thresholds[] = {256u, 512u, 1024u, 2048u};
+  const uint32_t thresholds[] = {128u, 512u, 1024u, 2048u};
   cudaEvent_t start, stop;
   DG_CUDA(cudaEventCreate(&start));
   DG_CUDA(cudaEventCreate(&stop));

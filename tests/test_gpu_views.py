@@ -72,7 +72,7 @@ def test_views_match_single_view_renders(device, scene, batch, graph):
 def test_autotuned_views_match(device, scene):
     r, cams, colors, lasts, images = scene
     tuned = r.tuneViews(cams, BG)
-    assert tuned["batch"] in {1, 4, len(cams)} and tuned["coopMin"] in {256, 512, 1024, 2048}
+    assert tuned["batch"] in {1, 4, len(cams)} and tuned["coopMin"] in {128, 512, 1024, 2048}
     assert len(tuned["seconds"]) >= 4 and min(tuned["seconds"]) > 0
     assert r.viewBatching == {"batch": tuned["batch"], "coopMin": tuned["coopMin"]}
     _check(device, r, cams, colors, lasts, images, tuned["batch"])
