@@ -87,16 +87,8 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
 // with coalesced loads (45 floats per Gaussian; the odd stride makes the
 // per-thread reads conflict-free). All threads of the CTA take part.
 __device__ __forceinline__ void stage_sh(float* s_sh, const float* __restrict__ sh, uint32_t first, uint32_t n) {
-  const float* src = sh + (size_t)first * SH_REST_FLOATS;
-  const uint32_t floats = n * SH_REST_FLOATS;
-  if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-    const uint32_t vecs = floats / 4;
-    for (uint32_t k = threadIdx.x; k < vecs; k += blockDim.x)
-      reinterpret_cast<float4*>(s_sh)[k] = reinterpret_cast<const float4*>(src)[k];
-    for (uint32_t k = vecs * 4 + threadIdx.x; k < floats; k += blockDim.x) s_sh[k] = src[k];
-  } else {
-    for (uint32_t k = threadIdx.x; k < floats; k += blockDim.x) s_sh[k] = src[k];
-  }
+  stage_floats_async(s_sh, sh + (size_t)first * SH_REST_FLOATS, n * SH_REST_FLOATS);
+  cp_async_wait_all();
 }
 
 __device__ __forceinline__ void load_gaussian(const float* __restrict__ gaussians, uint32_t i, float (&g)[16]) {
@@ -129,12 +121,16 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
   const uint32_t block_start = blockIdx.x * PRE_THREADS;
-  if (basis_count > 0) stage_sh(s_sh, sh, block_start, min((uint32_t)PRE_THREADS, count - block_start));
-  __syncthreads();
   const uint32_t i = block_start + threadIdx.x;
-  if (i >= count) return;
+  // The SH copy and this thread's Gaussian record load at the same time.
+  if (basis_count > 0)
+    stage_floats_async(s_sh, sh + (size_t)block_start * SH_REST_FLOATS,
+                       min((uint32_t)PRE_THREADS, count - block_start) * SH_REST_FLOATS);
   float g[16];
-  load_gaussian(gaussians, i, g);
+  load_gaussian(gaussians, min(i, count - 1u), g);  // threads past the end load the last one and stop below
+  cp_async_wait_all();
+  __syncthreads();
+  if (i >= count) return;
   const Projected pr = preprocess_one(s_cam, g, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count,
                                       reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT));
   if (tile_counts) tile_counts[i] = pr.tiles;

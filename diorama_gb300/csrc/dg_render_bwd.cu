@@ -527,7 +527,8 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
   load_camera(s_cam, camera);
   const uint32_t block_start = blockIdx.x * PBWD_THREADS;
   const uint32_t here = min(PBWD_THREADS, count - block_start);
-  copy_floats(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  stage_floats_async(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  cp_async_wait_all();
   __syncthreads();
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
@@ -567,7 +568,8 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
   if (threadIdx.x == 0) s_ap = *adam;
   const uint32_t block_start = blockIdx.x * PBWD_THREADS;
   const uint32_t here = min(PBWD_THREADS, count - block_start);
-  copy_floats(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  stage_floats_async(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
+  cp_async_wait_all();
   __syncthreads();
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;

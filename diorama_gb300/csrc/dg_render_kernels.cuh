@@ -287,6 +287,20 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Starts copying n floats from global src to shared dst, spread over the CTA's
+// threads: every 16-byte chunk is issued at once (cp.async), instead of each
+// thread waiting for one load before issuing the next. The caller waits
+// (cp_async_wait_all) and synchronizes the CTA before reading dst.
+__device__ __forceinline__ void stage_floats_async(float* dst, const float* __restrict__ src, uint32_t n) {
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+    const uint32_t vecs = n / 4;
+    for (uint32_t k = threadIdx.x; k < vecs; k += blockDim.x) cp_async16(dst + 4 * k, src + 4 * k);
+    for (uint32_t k = vecs * 4 + threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+  } else {
+    for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+  }
+}
+
 // Starts copying the splat record of this lane's entry of a window into `raw`.
 __device__ __forceinline__ void stage_issue(WarpStage& st, const float* __restrict__ splats, uint32_t index,
                                             bool valid) {
