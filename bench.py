@@ -263,13 +263,21 @@ def run_ours(args, rank, world, local, group):
     camera_bytes, adam_bytes = 144, 48
     barrier(group)
     device.synchronize()
+    # The trainer copies each step's photo from pinned host memory itself (the
+    # next step's while the current one runs), and each step's loss is read back
+    # after the next step is launched, as a training loop logging its loss does.
+    trainer.setHostPhotos(pinned)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        k = trainer.nextView()
-        views[k].image.buffer.writePinned(pinned[k])
+    e2e_losses = []
+    for s in range(args.steps):
         trainer.step()
-        trainer.lossValue()
+        trainer.requestLoss()
+        if s > 0:
+            e2e_losses.append(trainer.takeLoss())
+    e2e_losses.append(trainer.takeLoss())
     e2e_s = reduce_max(group, time.perf_counter() - t0)
+    trainer.setHostPhotos(None)
+    assert len(e2e_losses) == args.steps and all(math.isfinite(v) for v in e2e_losses)
     barrier(group)
     e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * H * 4 + camera_bytes + adam_bytes
            + 8 + 16, "d2h_bytes_per_step": 8 + 4}

@@ -181,6 +181,9 @@ SIGNATURES = {
     "dg_trainer_densification": (None, [_P, c_uint32, POINTER(DensificationC)]),
     "dg_trainer_set_graph": (None, [_P, c_int32]),
     "dg_trainer_set_keep_gradients": (None, [_P, c_int32]),
+    "dg_trainer_request_loss": (None, [_P]),
+    "dg_trainer_set_host_photos": (None, [_P, c_void_p, c_uint32]),
+    "dg_trainer_take_loss": (None, [_P, c_int32, POINTER(c_double), POINTER(c_int32)]),
     "dg_trainer_save_checkpoint": (None, [_P, c_char_p]),
     "dg_trainer_resume": (None, [_P, c_char_p, c_void_p, c_uint32, c_void_p, POINTER(_P)]),
     "dg_parse_gaussian_ply": (None, [c_void_p, c_uint64, POINTER(c_uint32), POINTER(c_uint32), c_void_p, c_void_p]),

@@ -345,6 +345,22 @@ struct dg_trainer {
   // The captured optimize() step.
   bool graph_enabled = false;
   bool keep_gradients = false;  // store the Gaussian gradients Adam consumes in registers
+  // Loss values requested and not yet taken: [loss_tail, loss_head) of a ring of
+  // pinned slots, each with the event its copy completes.
+  static constexpr uint32_t LOSS_RING = 16;
+  double* loss_ring = nullptr;
+  cudaEvent_t loss_events[LOSS_RING] = {};
+  uint32_t loss_head = 0, loss_tail = 0;
+  // Photos from pinned host memory (set_host_photos): each step's photo is copied
+  // into one of two device slots on an upload stream, the next step's while the
+  // current one runs. slot_free[s]: the last step reading slot s is done;
+  // slot_ready[s]: its upload is done.
+  std::vector<const void*> host_photos;
+  dg_buffer* photo_slots[2] = {nullptr, nullptr};
+  cudaStream_t upload_stream = nullptr;
+  cudaEvent_t slot_free[2] = {}, slot_ready[2] = {};
+  int64_t prefetch_view = -1;  // the view already uploading into prefetch_slot
+  uint32_t prefetch_slot = 0, slot_used = 1;
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_launches = 0;
   struct Key {
@@ -404,6 +420,26 @@ static uint32_t next_view(dg_trainer* t) {
   uint32_t v = t->queue.back();
   t->queue.pop_back();
   return v;
+}
+
+// The view the next optimize() renders, without taking it (a new round is
+// shuffled first if needed, exactly as next_view would).
+static uint32_t peek_view(dg_trainer* t) {
+  if (t->queue.empty()) t->queue.push_back(next_view(t));
+  return t->queue.back();
+}
+
+// Copies view `view`'s host photo into slot `slot` on the upload stream, once
+// the last step that read the slot is done.
+static dg_status upload_photo(dg_trainer* t, uint32_t slot, uint32_t view) {
+  const uint64_t bytes = t->photo_slots[slot]->bytes;
+  DG_CUDA(cudaStreamWaitEvent(t->upload_stream, t->slot_free[slot], 0));
+  DG_CUDA(cudaMemcpyAsync(t->photo_slots[slot]->ptr, t->host_photos[view], bytes, cudaMemcpyHostToDevice,
+                          t->upload_stream));
+  DG_CUDA(cudaEventRecord(t->slot_ready[slot], t->upload_stream));
+  t->prefetch_view = view;
+  t->prefetch_slot = slot;
+  return DG_OK;
 }
 
 static dg_status launch_stats(dg_trainer* t) {
@@ -600,10 +636,24 @@ dg_status dg_trainer_optimize(dg_trainer* t) {
   if (it % s.sh_degree_interval == 0 && t->sh_degree < 3) DG_TRY(dg_renderer_set_sh_degree(r, ++t->sh_degree));
   const bool densifying = it < s.densify_until;
   const bool densify_now = densifying && it > s.densify_from && it % s.densify_interval == 0;
-  const dg_trainer::View& view = t->views[next_view(t)];
+  const uint32_t view_index = next_view(t);
+  const dg_trainer::View& view = t->views[view_index];
   // Uniforms of this step: camera, background, photo, learning rates.
   DG_TRY(renderer_prepare(r, &view.camera, s.background));
   const void* photo = view.image->ptr;
+  const bool from_host = !t->host_photos.empty();
+  uint32_t slot = 0;
+  if (from_host) {
+    if (t->prefetch_view == (int64_t)view_index) {
+      slot = t->prefetch_slot;
+    } else {
+      slot = t->slot_used ^ 1u;
+      DG_TRY(upload_photo(t, slot, view_index));
+    }
+    t->prefetch_view = -1;
+    DG_CUDA(cudaStreamWaitEvent(t->ctx->stream, t->slot_ready[slot], 0));
+    photo = t->photo_slots[slot]->ptr;
+  }
   DG_TRY(write_async(t->ctx, t->loss->target_slot->ptr, &photo, sizeof(photo)));
   if (!densify_now) t->adam_steps++;
   const double progress = std::min(1.0, it / s.position_lr_steps);
@@ -634,6 +684,13 @@ dg_status dg_trainer_optimize(dg_trainer* t) {
   DG_TRY(dg_tile_rasterizer_after_submit(tr, 0));
   t->due_densify = densify_now;
   t->due_reset = densifying && it % s.opacity_reset_interval == 0;
+  if (from_host) {
+    // This step's reads of the slot are enqueued; the next step's photo goes
+    // into the other slot while this one runs.
+    DG_CUDA(cudaEventRecord(t->slot_free[slot], t->ctx->stream));
+    t->slot_used = slot;
+    DG_TRY(upload_photo(t, slot ^ 1u, peek_view(t)));
+  }
   return DG_OK;
 }
 
@@ -982,6 +1039,67 @@ dg_status dg_trainer_loss_value(dg_trainer* t, double* out) {
   return DG_OK;
 }
 
+dg_status dg_trainer_set_host_photos(dg_trainer* t, const void* const* photos, uint32_t count) {
+  DG_REQUIRE(t, "NULL argument");
+  if (t->upload_stream) DG_CUDA(cudaStreamSynchronize(t->upload_stream));
+  t->host_photos.clear();
+  t->prefetch_view = -1;
+  if (!photos) return DG_OK;
+  DG_REQUIRE(count == t->views.size(), "one host photo per training view");
+  for (uint32_t k = 0; k < count; k++) DG_REQUIRE(photos[k], "NULL host photo");
+  const uint64_t bytes = (uint64_t)t->views[0].camera.viewport[0] * (uint64_t)t->views[0].camera.viewport[1] * 4;
+  if (!t->upload_stream) {
+    DG_CUDA(cudaStreamCreateWithFlags(&t->upload_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) {
+      DG_CUDA(cudaEventCreateWithFlags(&t->slot_free[k], cudaEventDisableTiming));
+      DG_CUDA(cudaEventCreateWithFlags(&t->slot_ready[k], cudaEventDisableTiming));
+      DG_TRY(storage(t, bytes, &t->photo_slots[k]));
+    }
+  }
+  // Nothing has read the slots yet: free as of now.
+  for (int k = 0; k < 2; k++) DG_CUDA(cudaEventRecord(t->slot_free[k], t->ctx->stream));
+  t->host_photos.assign(photos, photos + count);
+  return DG_OK;
+}
+
+dg_status dg_trainer_request_loss(dg_trainer* t) {
+  DG_REQUIRE(t, "NULL argument");
+  DG_REQUIRE(t->loss_head - t->loss_tail < dg_trainer::LOSS_RING,
+             "too many loss values requested and not taken (take some first)");
+  if (!t->loss_ring) {
+    DG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&t->loss_ring), dg_trainer::LOSS_RING * sizeof(double),
+                          cudaHostAllocDefault));
+    for (cudaEvent_t& e : t->loss_events) DG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const uint32_t slot = t->loss_head % dg_trainer::LOSS_RING;
+  DG_TRY(loss_sum_launch(t->loss));
+  DG_CUDA(cudaMemcpyAsync(&t->loss_ring[slot], typed<double>(t->loss->sum_scratch) + t->loss->sum_blocks, 8,
+                          cudaMemcpyDeviceToHost, t->ctx->stream));
+  DG_CUDA(cudaEventRecord(t->loss_events[slot], t->ctx->stream));
+  t->loss_head++;
+  return DG_OK;
+}
+
+dg_status dg_trainer_take_loss(dg_trainer* t, int32_t wait, double* out, int32_t* ready) {
+  DG_REQUIRE(t && out && ready, "NULL argument");
+  DG_REQUIRE(t->loss_tail < t->loss_head, "no loss value requested");
+  const uint32_t slot = t->loss_tail % dg_trainer::LOSS_RING;
+  if (wait) {
+    DG_CUDA(cudaEventSynchronize(t->loss_events[slot]));
+  } else {
+    const cudaError_t q = cudaEventQuery(t->loss_events[slot]);
+    if (q == cudaErrorNotReady) {
+      *ready = 0;
+      return DG_OK;
+    }
+    DG_CUDA(q);
+  }
+  *out = t->loss_ring[slot];
+  *ready = 1;
+  t->loss_tail++;
+  return DG_OK;
+}
+
 uint32_t dg_trainer_iteration(const dg_trainer* t) { return t ? t->iteration : 0; }
 dg_status dg_trainer_set_iteration(dg_trainer* t, uint32_t iteration) {
   DG_REQUIRE(t, "NULL argument");
@@ -1016,6 +1134,20 @@ dg_status dg_trainer_destroy(dg_trainer* t) {
   dg_renderer_destroy(t->renderer);
   dg_training_loss_destroy(t->loss);
   for (dg_buffer* b : {t->target, t->params, t->moments, t->stats, t->adam_params, t->ids, t->aux}) free_buffer(b);
+  if (t->loss_ring) {
+    for (cudaEvent_t e : t->loss_events)
+      if (e) cudaEventDestroy(e);
+    cudaFreeHost(t->loss_ring);
+  }
+  if (t->upload_stream) {
+    cudaStreamSynchronize(t->upload_stream);
+    cudaStreamDestroy(t->upload_stream);
+    for (int k = 0; k < 2; k++) {
+      cudaEventDestroy(t->slot_free[k]);
+      cudaEventDestroy(t->slot_ready[k]);
+      free_buffer(t->photo_slots[k]);
+    }
+  }
   delete t;
   return DG_OK;
 }

@@ -296,6 +296,28 @@ class Trainer:
         _lib.call("dg_trainer_loss_value", self.handle, ctypes.byref(out))
         return out.value
 
+    def setHostPhotos(self, photos) -> None:
+        """Read each step's photo from pinned host memory (one PinnedArray per view,
+        kept alive and unchanged by the caller), uploading the next step's while the
+        current one runs; None goes back to the views' images."""
+        if photos is None:
+            self._host_photos = None
+            _lib.call("dg_trainer_set_host_photos", self.handle, None, 0)
+            return
+        arr = (ctypes.c_void_p * len(photos))(*[p.pointer for p in photos])
+        self._host_photos = (list(photos), arr)
+        _lib.call("dg_trainer_set_host_photos", self.handle, arr, len(photos))
+
+    def requestLoss(self) -> None:
+        """Start reading the last step's loss without waiting for it (see takeLoss)."""
+        _lib.call("dg_trainer_request_loss", self.handle)
+
+    def takeLoss(self, wait: bool = True) -> float | None:
+        """The oldest requested loss; None if wait is False and it has not arrived."""
+        out, ready = c_double(), ctypes.c_int32()
+        _lib.call("dg_trainer_take_loss", self.handle, int(wait), ctypes.byref(out), ctypes.byref(ready))
+        return out.value if ready.value else None
+
     def nextView(self) -> int:
         """Index of the view the next optimize() renders."""
         out = ctypes.c_uint32()

@@ -274,6 +274,20 @@ dg_status dg_trainer_last_loss(dg_trainer* t, double* out);
 /* The same loss summed on the GPU in a fixed order (8 bytes come back instead of
  * one float per pixel). */
 dg_status dg_trainer_loss_value(dg_trainer* t, double* out);
+/* The same without waiting (no reference counterpart): request_loss enqueues the
+ * last step's sum and its 8-byte copy into pinned memory; take_loss returns the
+ * oldest requested value (*ready = 1), blocking until it has arrived when wait is
+ * nonzero, else setting *ready = 0 if it has not. At most 16 may be outstanding.
+ * A training loop that takes step k's loss after launching step k + 1 keeps the
+ * GPU busy while the host reads it. */
+dg_status dg_trainer_request_loss(dg_trainer* t);
+/* Photos from pinned host memory (no reference counterpart): photos[k] holds view
+ * k's rgba8 photo (viewport size, from dg_host_alloc; the caller keeps it alive
+ * and unchanged). Each step then copies its photo to the GPU itself, the next
+ * step's while the current one runs (two device slots, an upload stream), and the
+ * views' image buffers are not read. NULL goes back to the image buffers. */
+dg_status dg_trainer_set_host_photos(dg_trainer* t, const void* const* photos, uint32_t count);
+dg_status dg_trainer_take_loss(dg_trainer* t, int32_t wait, double* out, int32_t* ready);
 /* The index of the view the next optimize() renders (shuffling a new round first
  * if needed, exactly as optimize() would): lets a caller upload that view's photo
  * just in time. */

@@ -279,3 +279,67 @@ def test_evaluate_matches_cpu_metrics(device):
     t.destroy()
     for v in views:
         v.image.destroy()
+
+
+def test_requested_losses_arrive_in_order(device):
+    truth, random = truth_scene()
+    views = ring_views(device, truth)
+    params = scrambled_start(truth, random)
+    t = Trainer(device, RawGaussians(params, np.zeros(60 * 45, np.float32)), views,
+                replace(DEFAULT_SETTINGS, extent=3.85))
+    from diorama_gb300 import DioramaError
+    with pytest.raises(DioramaError, match="no loss value requested"):
+        t.takeLoss()
+    want = []
+    for _ in range(5):
+        t.step()
+        want.append(t.lossValue())
+        t.requestLoss()
+    got = [t.takeLoss() for _ in range(5)]
+    assert got == want  # the same sum in the same order
+    for _ in range(16):
+        t.requestLoss()
+    with pytest.raises(DioramaError, match="too many loss values"):
+        t.requestLoss()
+    taken = [t.takeLoss() for _ in range(16)]
+    assert all(v == want[-1] for v in taken)  # no step in between: the same loss
+    t.destroy()
+    for v in views:
+        v.image.destroy()
+
+
+def test_host_photos_match_device_images(device):
+    # Photos read from pinned host memory by the trainer itself give the same
+    # losses as the views' device images (the first steps' bit for bit).
+    from diorama_gb300.gpu import PinnedArray
+    truth, random = truth_scene()
+    views = ring_views(device, truth)
+    params = scrambled_start(truth, random)
+    settings = replace(DEFAULT_SETTINGS, extent=3.85)
+    a = Trainer(device, RawGaussians(params.copy(), np.zeros(60 * 45, np.float32)), views, settings)
+    b = Trainer(device, RawGaussians(params.copy(), np.zeros(60 * 45, np.float32)), views, settings)
+    pinned = []
+    for v in views:
+        p = PinnedArray((96 * 96 * 4,), np.uint8)
+        p.array[:] = v.image.read().reshape(-1)
+        pinned.append(p)
+    b.setHostPhotos(pinned)
+    la, lb = [], []
+    for _ in range(12):
+        assert a.nextView() == b.nextView()
+        a.step()
+        b.step()
+        la.append(a.lossValue())
+        lb.append(b.lossValue())
+    assert la[0] == lb[0]
+    assert np.allclose(la, lb, rtol=1e-4)
+    b.setHostPhotos(None)
+    b.step()
+    a.step()
+    assert abs(a.lossValue() - b.lossValue()) < 1e-3
+    a.destroy()
+    b.destroy()
+    for p in pinned:
+        p.free()
+    for v in views:
+        v.image.destroy()
