@@ -178,8 +178,13 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_views_kernel(
 // Tiles touched by the j-th splat in depth order, for the scan.
 __global__ void gather_counts_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
                                      uint32_t n, uint32_t* __restrict__ out) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < n) out[j] = counts[order[j]];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) out[j] = counts[order[j]];
+}
+
+// Enough CTAs of `threads` to keep every SM busy in a grid-stride loop over n
+// items (at most one CTA per `threads` items).
+inline uint32_t stride_grid(const dg_context* ctx, uint64_t n, uint32_t threads) {
+  return std::max(1u, std::min(ceil_div(n, threads), (uint32_t)ctx->sm_count * 8u));
 }
 
 // duplicate_kernel's warp-cooperative emission over splats in depth order: the
@@ -352,20 +357,35 @@ __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32
                                                                     uint32_t capacity, uint32_t tiles,
                                                                     uint2* __restrict__ ranges) {
   const uint32_t n = min(pair_total[0], capacity);
-  const uint32_t i = blockIdx.x * RANGE_THREADS + threadIdx.x;
-  if (i >= n) return;
-  const uint32_t tile = key_words[STRIDE * (size_t)i + (STRIDE - 1)];
-  if (tile >= tiles) return;  // only possible after a sort whose bounded wait gave up
-  if (i == 0) {
-    ranges[tile].x = 0;
-  } else {
-    const uint32_t prev = key_words[STRIDE * (size_t)(i - 1) + (STRIDE - 1)];
+  // Pair i with tile `tile` after pair i - 1 with tile `prev` (~0u for none).
+  auto edge = [&](uint32_t i, uint32_t tile, uint32_t prev) {
+    if (tile >= tiles) return;  // only possible after a sort whose bounded wait gave up
     if (tile != prev) {
-      if (prev < tiles) ranges[prev].y = i;
+      if (i > 0 && prev < tiles) ranges[prev].y = i;
       ranges[tile].x = i;
     }
+    if (i == n - 1) ranges[tile].y = n;
+  };
+  // A grid-stride loop over a few CTAs per SM (one thread per pair would spend
+  // more on launching tens of thousands of tiny CTAs than on the pairs); u32 keys
+  // come four at a time.
+  const uint32_t stride = gridDim.x * RANGE_THREADS, first = blockIdx.x * RANGE_THREADS + threadIdx.x;
+  if constexpr (STRIDE == 1) {
+    const uint32_t quads = n / 4;
+    for (uint32_t q = first; q < quads; q += stride) {
+      const uint4 k = reinterpret_cast<const uint4*>(key_words)[q];
+      const uint32_t i = 4 * q;
+      edge(i, k.x, i ? key_words[i - 1] : ~0u);
+      edge(i + 1, k.y, k.x);
+      edge(i + 2, k.z, k.y);
+      edge(i + 3, k.w, k.z);
+    }
+    for (uint32_t i = 4 * quads + first; i < n; i += stride) edge(i, key_words[i], i ? key_words[i - 1] : ~0u);
+  } else {
+    for (uint32_t i = first; i < n; i += stride)
+      edge(i, key_words[STRIDE * (size_t)i + (STRIDE - 1)],
+           i ? key_words[STRIDE * (size_t)(i - 1) + (STRIDE - 1)] : ~0u);
   }
-  if (i == n - 1) ranges[tile].y = n;
 }
 
 __device__ __forceinline__ unsigned char to_unorm8(float v) {
@@ -874,7 +894,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
       DG_TRY(sort_launch(ctx, tr->depth_plan, tr->depth_keys->ptr, order, tr->depth_keys_alt->ptr,
                          typed<uint32_t>(tr->depth_values_alt), nullptr, tr->depth_scratch->ptr));
       DG_LAUNCH(ctx, "gather_counts",
-                gather_counts_kernel<<<ceil_div(count, 256), 256, 0, st>>>(
+                gather_counts_kernel<<<stride_grid(ctx, count, 256), 256, 0, st>>>(
                     order, typed<uint32_t>(tr->tile_offsets), count, typed<uint32_t>(tr->counts_sorted)));
     }
     DG_TRY(scan_launch(ctx, typed<uint32_t>(tr->counts_sorted), count, nullptr, typed<uint32_t>(tr->scan_total),
@@ -888,7 +908,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
     DG_TRY(sort_launch(ctx, tr->tile_plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
                        typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
     DG_LAUNCH(ctx, "find_ranges",
-              find_ranges_kernel<1><<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0,
+              find_ranges_kernel<1><<<stride_grid(ctx, tr->pair_capacity, RANGE_THREADS), RANGE_THREADS, 0,
                                       st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
                                             tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
     tr->keys_are_tiles = true;
@@ -913,7 +933,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
   DG_TRY(sort_launch(ctx, tr->plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
                      typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
   DG_LAUNCH(ctx, "find_ranges",
-            find_ranges_kernel<2><<<std::max(1u, ceil_div(tr->pair_capacity, RANGE_THREADS)), RANGE_THREADS, 0,
+            find_ranges_kernel<2><<<stride_grid(ctx, tr->pair_capacity, RANGE_THREADS), RANGE_THREADS, 0,
                                     st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
                                           tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
   return launch_rasterize(tr, target);
@@ -976,7 +996,7 @@ dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32
 dg_status gather_counts_launch(dg_context* ctx, const uint32_t* order, const uint32_t* counts, uint32_t n,
                                uint32_t* out) {
   DG_LAUNCH(ctx, "gather_counts",
-            gather_counts_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(order, counts, n, out));
+            gather_counts_kernel<<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(order, counts, n, out));
   return DG_OK;
 }
 
@@ -992,7 +1012,7 @@ dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const f
 dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
                              uint32_t tiles, uint2* ranges) {
   DG_LAUNCH(ctx, "find_ranges",
-            find_ranges_kernel<1><<<std::max(1u, ceil_div(capacity, RANGE_THREADS)), RANGE_THREADS, 0, ctx->stream>>>(
+            find_ranges_kernel<1><<<stride_grid(ctx, capacity, RANGE_THREADS), RANGE_THREADS, 0, ctx->stream>>>(
                 tile_keys, pair_total, capacity, tiles, ranges));
   return DG_OK;
 }
