@@ -175,12 +175,6 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_views_kernel(
 // with ties by splat index: exactly the reference's order, from sorting N 32-bit
 // keys plus K 16-bit ones instead of K 48-bit ones.
 
-// Tiles touched by the j-th splat in depth order, for the scan.
-__global__ void gather_counts_kernel(const uint32_t* __restrict__ order, const uint32_t* __restrict__ counts,
-                                     uint32_t n, uint32_t* __restrict__ out) {
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) out[j] = counts[order[j]];
-}
-
 // Enough CTAs of `threads` to keep every SM busy in a grid-stride loop over n
 // items (at most one CTA per `threads` items).
 inline uint32_t stride_grid(const dg_context* ctx, uint64_t n, uint32_t threads) {
@@ -893,12 +887,11 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
     if (count > 0) {
       DG_TRY(sort_launch(ctx, tr->depth_plan, tr->depth_keys->ptr, order, tr->depth_keys_alt->ptr,
                          typed<uint32_t>(tr->depth_values_alt), nullptr, tr->depth_scratch->ptr));
-      DG_LAUNCH(ctx, "gather_counts",
-                gather_counts_kernel<<<stride_grid(ctx, count, 256), 256, 0, st>>>(
-                    order, typed<uint32_t>(tr->tile_offsets), count, typed<uint32_t>(tr->counts_sorted)));
     }
+    // The splats' tile counts in depth order, scanned: the scan gathers them
+    // through the sort's permutation as it loads them.
     DG_TRY(scan_launch(ctx, typed<uint32_t>(tr->counts_sorted), count, nullptr, typed<uint32_t>(tr->scan_total),
-                       tr->scan_scratch->ptr));
+                       tr->scan_scratch->ptr, count > 0 ? order : nullptr, typed<uint32_t>(tr->tile_offsets)));
     if (count > 0) {
       DG_LAUNCH(ctx, "duplicate",
                 duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
@@ -993,12 +986,6 @@ dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32
   return DG_OK;
 }
 
-dg_status gather_counts_launch(dg_context* ctx, const uint32_t* order, const uint32_t* counts, uint32_t n,
-                               uint32_t* out) {
-  DG_LAUNCH(ctx, "gather_counts",
-            gather_counts_kernel<<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(order, counts, n, out));
-  return DG_OK;
-}
 
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
                                   const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,

@@ -95,8 +95,6 @@ dg_status blend_forward(dg_context* ctx, const BlendForward& f);
 dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32_t views, const float* gaussians,
                                   const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
                                   uint32_t* tile_counts, uint2* depth_keys, uint32_t* order);
-dg_status gather_counts_launch(dg_context* ctx, const uint32_t* order, const uint32_t* counts, uint32_t n,
-                               uint32_t* out);
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
                                   const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,
                                   uint32_t* keys, uint32_t* values);

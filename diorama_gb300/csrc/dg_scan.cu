@@ -45,10 +45,13 @@ __device__ __forceinline__ uint32_t warp_inclusive(uint32_t v, int lane) {
   return v;
 }
 
+// With `gather`, value j is source[gather[j]] and data only receives the scan.
 __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict__ data, uint32_t capacity,
                                                           const uint32_t* __restrict__ count_ptr,
                                                           uint32_t* __restrict__ total, uint64_t* __restrict__ status,
-                                                          uint32_t* __restrict__ ticket, uint32_t* __restrict__ error) {
+                                                          uint32_t* __restrict__ ticket, uint32_t* __restrict__ error,
+                                                          const uint32_t* __restrict__ gather,
+                                                          const uint32_t* __restrict__ source) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warp[SCAN_THREADS / 32];
   __shared__ uint32_t s_prefix;
@@ -63,9 +66,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   // Each thread owns SCAN_ITEMS consecutive values.
   const uint64_t base = (uint64_t)tile * SCAN_TILE + (uint64_t)tid * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS];
-  const bool full = base + SCAN_ITEMS <= n && (reinterpret_cast<uintptr_t>(data) & 15) == 0;
+  const uint32_t* in = gather ? gather : data;
+  const bool full = base + SCAN_ITEMS <= n &&
+                    ((reinterpret_cast<uintptr_t>(data) | reinterpret_cast<uintptr_t>(in)) & 15) == 0;
   if (full) {
-    const uint4* p = reinterpret_cast<const uint4*>(data + base);
+    const uint4* p = reinterpret_cast<const uint4*>(in + base);
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS / 4; k++) {
       uint4 q = p[k];
@@ -73,7 +78,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = base + k < n ? data[base + k] : 0u;
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = base + k < n ? in[base + k] : 0u;
+  }
+  if (gather) {  // the 16 gathers of a thread go out together
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = base + k < n ? source[v[k]] : 0u;
   }
   uint32_t sum = 0;
 #pragma unroll
@@ -155,14 +164,14 @@ size_t scan_scratch_bytes(uint32_t capacity) {
 }
 
 dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const uint32_t* count, uint32_t* total,
-                      void* scratch) {
+                      void* scratch, const uint32_t* gather, const uint32_t* source) {
   uint32_t tiles = std::max(1u, ceil_div(capacity, SCAN_TILE));
   auto* ticket = static_cast<uint32_t*>(scratch);
   auto* status = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + 256);
   DG_CUDA(cudaMemsetAsync(scratch, 0, scan_scratch_bytes(capacity), ctx->stream));
   DG_LAUNCH(ctx, "scan",
             scan_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, total, status, ticket,
-                                                                 ctx->device_error));
+                                                                 ctx->device_error, gather, source));
   return DG_OK;
 }
 
@@ -225,7 +234,8 @@ extern "C" dg_status dg_prefix_sum_no_alloc(void* stream, uint32_t* data, uint32
   // call's tiles will read (the error word keeps any earlier give-up).
   DG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
   DG_CUDA(cudaMemsetAsync(status, 0, (size_t)tiles * sizeof(uint64_t), s));
-  scan_kernel<<<tiles, SCAN_THREADS, 0, s>>>(data, count, nullptr, total, status, ticket, error);
+  scan_kernel<<<tiles, SCAN_THREADS, 0, s>>>(data, count, nullptr, total, status, ticket, error, nullptr,
+                                                          nullptr);
   DG_CUDA(cudaGetLastError());
   return DG_OK;
 }

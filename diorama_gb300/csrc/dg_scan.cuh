@@ -7,10 +7,11 @@ namespace dg {
 
 // Exclusive scan of min(*count, capacity) values of data in place (count may be
 // NULL: all capacity values); total[0] gets the sum. scratch holds
-// scan_scratch_bytes(capacity) bytes and is cleared by each launch.
+// scan_scratch_bytes(capacity) bytes and is cleared by each launch. With gather,
+// value j is source[gather[j]] instead and data only receives the scan.
 size_t scan_scratch_bytes(uint32_t capacity);
 dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const uint32_t* count, uint32_t* total,
-                      void* scratch);
+                      void* scratch, const uint32_t* gather = nullptr, const uint32_t* source = nullptr);
 
 // Stable LSD radix sort with the reference's pass plan, in place in keys/values
 // (the scratch pair holds the odd passes). key_words = 1 for u32 keys, 2 for u64

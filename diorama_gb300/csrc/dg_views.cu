@@ -143,9 +143,8 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   DG_TRY(sort_launch(ctx, depth_plan, b->depth_keys->ptr, typed<uint32_t>(b->order), b->depth_keys_alt->ptr,
                      typed<uint32_t>(b->order_alt), nullptr, b->depth_scratch->ptr));
   uint32_t* order = depth_plan.passes & 1 ? typed<uint32_t>(b->order_alt) : typed<uint32_t>(b->order);
-  DG_TRY(gather_counts_launch(ctx, order, typed<uint32_t>(b->tile_counts), n, typed<uint32_t>(b->counts_sorted)));
   DG_TRY(scan_launch(ctx, typed<uint32_t>(b->counts_sorted), n, nullptr, typed<uint32_t>(b->scan_total),
-                     b->scan_scratch->ptr));
+                     b->scan_scratch->ptr, order, typed<uint32_t>(b->tile_counts)));
   DG_TRY(duplicate_sorted_launch(ctx, typed<Camera>(b->cameras), typed<float>(b->splats), order,
                                  typed<uint32_t>(b->counts_sorted), n, b->count, b->pair_capacity,
                                  typed<uint32_t>(b->keys), typed<uint32_t>(b->values)));
