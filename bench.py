@@ -331,10 +331,33 @@ def run_ours(args, rank, world, local, group):
                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 3), "peak_source": peak_source,
                     "algorithmic_bytes_per_launch": by, "launches_per_step": launches_per_step,
                     "traffic": NCU_TRAFFIC.get(dom_mem) if n == 1_100_000 else None}
-    blend = {}
+    # The blend's work: the splats each pixel walks, counted as the forward's
+    # pixel_last (the 1-based position of the last splat the pixel blended) summed
+    # over the last step's pixels, per second of each blend kernel.
+    last = trainer.renderer.pixelLastBuffer.read(np.uint32)[: W * H]
+    evaluations = int(last.astype(np.int64).sum())
+    blend = {"evaluations_per_step": evaluations}
     for k in ("rasterize", "rasterize_backward"):
         if k in kernels:
-            blend[k] = {"avg_us": round(kernels[k]["avg_us"], 1), "share": round(kernels[k]["share"], 3)}
+            blend[k] = {"avg_us": round(kernels[k]["avg_us"], 1), "share": round(kernels[k]["share"], 3),
+                        "evaluations_per_s": round(evaluations / (kernels[k]["avg_us"] * 1e-6), 1)}
+
+    # Densification's compaction at this size (after everything else: it changes
+    # the scene): count, scan and the two scatter kernels, timed with events, in
+    # GB/s of 748 B per input Gaussian + 812 B per output + 8 B per input.
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    before = trainer.count
+    trainer.densify(False)
+    dreport = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    after = trainer.count
+    d_us = 1000 * sum(t for name, (c, t) in dreport.items() if name.startswith("densify") or name == "scan")
+    d_bytes = 748.0 * before + 812.0 * after + 8.0 * before
+    compaction = {"gaussians_in": before, "gaussians_out": after, "kernels_us": round(d_us, 1),
+                  "gb_s": round(d_bytes / (d_us * 1e-6) / 1e9, 1),
+                  "frac_of_measured": round(d_bytes / (d_us * 1e-6) / 1e9 / hbm_peak, 3),
+                  "kernels": {k: round(1000 * t / c, 2) for k, (c, t) in dreport.items()}}
 
     result = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -346,7 +369,7 @@ def run_ours(args, rank, world, local, group):
         "kernels": {k: {"avg_us": round(v["avg_us"], 2), "share": round(v["share"], 4), "launches": v["launches"]}
                     for k, v in sorted(kernels.items(), key=lambda kv: -kv[1]["share"])},
         "dominant_kernel": dominant, "blend": blend, "pairs": pairs, "gaussians": n,
-        "uncaptured_step": uncaptured, "held_out": held_out,
+        "uncaptured_step": uncaptured, "held_out": held_out, "compaction": compaction,
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args, raw, sh, views_host(views), cams, samples=1)
@@ -522,13 +545,62 @@ def run_sort_stress(args, rank, local):
         return {"gb_s": round(b / (us * 1e-6) / 1e9, 1), "frac_of_measured": round(b / (us * 1e-6) / 1e9 / hbm, 3),
                 "us": round(us, 2)}
 
+    # The scan at 12M values too (at 1.1M it is launch-bound): PrefixSum over random
+    # tile counts, timed with CUDA events.
+    from diorama_gb300 import PrefixSum
+    big = 12_000_000
+    counts = np.random.default_rng(5).integers(0, 9, big).astype(np.uint32)
+    cbuf = device.upload(counts)
+    scan12 = PrefixSum(device, cbuf, big)
+    for _ in range(3):
+        cbuf.write(counts)
+        scan12.encode()
+    t_scan = 0.0
+    for _ in range(args.steps):
+        cbuf.write(counts)
+        e0, e1 = device.event(), device.event()
+        e0.record()
+        scan12.encode()
+        e1.record()
+        device.synchronize()
+        t_scan += e0.elapsed_ms(e1)
+    scan12_us = 1000 * t_scan / args.steps
+    scan12.destroy()
+    cbuf.destroy()
+
+    # CPU numbers for the same primitives, the reference's algorithms: the oracle's
+    # stable LSD radix sort of (tile << 32 | depth bits) keys and its sequential
+    # exclusive scan (single thread), and numpy's stable argsort, on samples.
+    rng = np.random.default_rng(6)
+    sample = 2_000_000
+    sk = (rng.integers(0, tiles, sample).astype(np.uint64) << np.uint64(32)) | \
+        rng.integers(0, 2**32, sample).astype(np.uint64)
+    sv = np.arange(sample, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.lib().or_radix_sort(sk.copy(), sv.copy(), sample, 16)
+    cpu_sort = sample / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    np.argsort(sk, kind="stable")
+    cpu_argsort = sample / (time.perf_counter() - t0)
+    sc = counts[:n].copy()
+    t0 = time.perf_counter()
+    oracle.lib().or_exclusive_scan(sc, n)
+    cpu_scan = n / (time.perf_counter() - t0)
+
     result = {
         "metric": "config 2 sort/scan/ranges", "workload": "config 2: 1.1M Gaussians in [-3,3]^3 at 1960x1090, "
         "16x16 tiles, reference-structured tile stage", "keys": keys, "gaussians": n, "tiles": tiles,
         "steps": args.steps, "peak_hbm_gbs": hbm,
         "sort": frac(sort_bytes, sort_us), "scan": frac(scan_bytes, per.get("scan", 0.0)),
+        "scan_12M": frac(8.0 * big, scan12_us),
         "find_ranges": frac(ranges_bytes, per.get("find_ranges", 0.0)),
         "kernels": {k: {"avg_us": round(v, 2), "launches_per_frame": launches[k]} for k, v in per.items()},
+        "gpu_keys_per_s": round(keys / (sort_us * 1e-6), 1),
+        "cpu_baseline": {
+            "sort_keys_per_s": round(cpu_sort, 1), "sort_kind": "the oracle's stable 6-pass LSD radix sort, 1 thread",
+            "argsort_keys_per_s": round(cpu_argsort, 1), "argsort_kind": "numpy stable argsort of u64 keys, 1 thread",
+            "scan_values_per_s": round(cpu_scan, 1), "scan_kind": "the oracle's sequential exclusive scan, 1 thread",
+            "sample": f"{sample:,} random (tile < {tiles}) << 32 | depth-bits keys; {n:,} counts", "cores": 1},
     }
     tr.destroy()
     camera_buf.destroy()

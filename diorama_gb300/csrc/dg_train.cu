@@ -39,14 +39,6 @@ __device__ __forceinline__ float activated(uint32_t k, float raw) {
   return raw;
 }
 
-// src/shaders/adam.wgsl:74-77, one thread per raw float.
-__global__ void activate_kernel(const float* __restrict__ params, float* __restrict__ gaussians, uint32_t count) {
-  const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (uint64_t)count * FLOATS_PER_GAUSSIAN) return;
-  const uint32_t k = (uint32_t)(e % FLOATS_PER_GAUSSIAN);
-  if (k == 7 || k == 15) return;
-  gaussians[e] = activated(k, params[e]);
-}
 
 // src/shaders/adam.wgsl:112-121
 __global__ void reset_opacity_kernel(float* __restrict__ params, float2* __restrict__ moments,
@@ -94,15 +86,23 @@ __global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, co
                                                             const float4* __restrict__ stats,
                                                             const uint8_t* __restrict__ veto, uint32_t count,
                                                             uint32_t* __restrict__ outputs,
+                                                            uint8_t* __restrict__ actions,
                                                             uint32_t* __restrict__ counters) {
   __shared__ uint32_t local[4];
   if (threadIdx.x < 4) local[threadIdx.x] = 0;
   __syncthreads();
   const uint32_t i = blockIdx.x * 256 + threadIdx.x;
+  uint32_t a = 4;  // none
   if (i < count) {
-    const uint32_t a = densify_action(dp, params, stats, i, veto);
+    a = densify_action(dp, params, stats, i, veto);
     outputs[i] = a == 0 ? 0u : (a >= 2 ? 2u : 1u);
-    atomicAdd(&local[a], 1u);
+    actions[i] = (uint8_t)a;  // for the copy and place kernels, decided once
+  }
+  // One shared-memory atomic per warp and action instead of one per thread.
+#pragma unroll
+  for (uint32_t v = 0; v < 4; v++) {
+    const uint32_t votes = __ballot_sync(0xffffffffu, a == v);
+    if ((threadIdx.x & 31u) == 0 && votes) atomicAdd(&local[v], (uint32_t)__popc(votes));
   }
   __syncthreads();
   if (threadIdx.x < 4 && local[threadIdx.x]) atomicAdd(&counters[threadIdx.x], local[threadIdx.x]);
@@ -116,30 +116,16 @@ __device__ __forceinline__ uint32_t pcg(uint32_t v) {
 
 __device__ __forceinline__ float unit_of(uint32_t h) { return ((float)(h >> 8u) + 0.5f) / 16777216.0f; }
 
-// src/shaders/densify.wgsl:148-180, split in two for coalescing. This kernel runs
-// one thread per (Gaussian, moment slot) and copies the Adam moments (kept for a
-// kept Gaussian and a clone's original, zero for new ones), the raw parameters
-// and the SH coefficients; densify_place_kernel then places split children.
-// The identity of each output Gaussian and its learned-densification statistics
-// travel along (slot 0's thread): a kept Gaussian and a clone's original keep
-// theirs, a new Gaussian gets identity first_id + its output index and zeros.
-__global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
-                                                           const float4* __restrict__ stats,
-                                                           const uint8_t* __restrict__ veto,
-                                                           const float* __restrict__ sh,
-                                                           const float2* __restrict__ moments,
-                                                           const uint32_t* __restrict__ ids,
-                                                           const float2* __restrict__ aux,
-                                                           const uint32_t* __restrict__ outputs, uint32_t count,
-                                                           uint32_t first_id, float* __restrict__ new_params,
-                                                           float* __restrict__ new_sh,
-                                                           float2* __restrict__ new_moments,
-                                                           uint32_t* __restrict__ new_ids,
-                                                           float2* __restrict__ new_aux) {
-  const uint32_t e = blockIdx.x * 256 + threadIdx.x;
-  if (e >= count * MOMENT_SLOTS) return;
+__device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const float* __restrict__ params,
+                                                  const uint8_t* __restrict__ actions, const float* __restrict__ sh,
+                                                  const float2* __restrict__ moments, const uint32_t* __restrict__ ids,
+                                                  const float2* __restrict__ aux, const uint32_t* __restrict__ outputs,
+                                                  uint32_t first_id, float* __restrict__ new_params,
+                                                  float* __restrict__ new_sh, float2* __restrict__ new_moments,
+                                                  uint32_t* __restrict__ new_ids, float2* __restrict__ new_aux,
+                                                  float* __restrict__ new_gaussians, uint32_t e) {
   const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
-  const uint32_t a = densify_action(dp, params, stats, i, veto);
+  const uint32_t a = actions[i];
   if (a == 0) return;
   const uint32_t o = outputs[i];
   const uint32_t copies = a == 1 ? 1u : 2u;
@@ -173,20 +159,51 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
         if (k == 15) v = (float)dp.seed;
       }
       new_params[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = v;
+      // The activated copy (src/shaders/adam.wgsl:74-77; a split child's position
+      // is replaced by densify_place_kernel, in both).
+      if (k != 7 && k != 15) new_gaussians[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = activated(k, v);
     } else {
       new_sh[(size_t)dst * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)] = value;
     }
   }
 }
 
+// src/shaders/densify.wgsl:148-180, split in two for coalescing. This kernel takes
+// one (Gaussian, moment slot) at a time per thread and copies the Adam moments (kept for a
+// kept Gaussian and a clone's original, zero for new ones), the raw parameters
+// and the SH coefficients; densify_place_kernel then places split children.
+// The identity of each output Gaussian and its learned-densification statistics
+// travel along (slot 0's thread): a kept Gaussian and a clone's original keep
+// theirs, a new Gaussian gets identity first_id + its output index and zeros.
+__global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
+                                                           const uint8_t* __restrict__ actions,
+                                                           const float* __restrict__ sh,
+                                                           const float2* __restrict__ moments,
+                                                           const uint32_t* __restrict__ ids,
+                                                           const float2* __restrict__ aux,
+                                                           const uint32_t* __restrict__ outputs, uint32_t count,
+                                                           uint32_t first_id, float* __restrict__ new_params,
+                                                           float* __restrict__ new_sh,
+                                                           float2* __restrict__ new_moments,
+                                                           uint32_t* __restrict__ new_ids,
+                                                           float2* __restrict__ new_aux,
+                                                           float* __restrict__ new_gaussians) {
+  // A grid-stride loop over (Gaussian, slot): one thread per slot would spend more
+  // on launching a quarter of a million tiny CTAs than on the copy.
+  const uint32_t slots = count * MOMENT_SLOTS;
+  for (uint32_t e = blockIdx.x * 256 + threadIdx.x; e < slots; e += gridDim.x * 256)
+    densify_copy_slot(dp, params, actions, sh, moments, ids, aux, outputs, first_id, new_params, new_sh, new_moments,
+                      new_ids, new_aux, new_gaussians, e);
+}
+
 // Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and Box-Muller.
 __global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__ params,
-                                     const float4* __restrict__ stats, const uint8_t* __restrict__ veto,
-                                     const uint32_t* __restrict__ outputs, uint32_t count,
-                                     float* __restrict__ new_params) {
+                                     const uint8_t* __restrict__ actions, const uint32_t* __restrict__ outputs,
+                                     uint32_t count, float* __restrict__ new_params,
+                                     float* __restrict__ new_gaussians) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
-  if (densify_action(dp, params, stats, i, veto) != 3) return;
+  if (actions[i] != 3) return;
   const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
   // rotation_matrix (src/shaders/gaussianMath.wgsl:13-25)
   float dot = p[8] * p[8];
@@ -215,12 +232,14 @@ __global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__
     const float n0 = r1 * cosf(tau * unit_of(h2)), n1 = r1 * sinf(tau * unit_of(h2)), n2 = r2 * cosf(tau * unit_of(h4));
     const float sv[3] = {expf(p[4]) * n0, expf(p[5]) * n1, expf(p[6]) * n2};
     float* out = new_params + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
+    float* act = new_gaussians + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
 #pragma unroll
     for (int row = 0; row < 3; row++) {
       float v = r[0][row] * sv[0];
       v = v + r[1][row] * sv[1];
       v = v + r[2][row] * sv[2];
       out[row] = p[row] + v;
+      act[row] = out[row];  // positions activate to themselves
     }
   }
 }
@@ -733,6 +752,8 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   dg_buffer *outputs = nullptr, *counters = nullptr, *scratch = nullptr;
   dg_buffer *features = nullptr, *survive = nullptr, *veto = nullptr, *tallies = nullptr;
   if (st == DG_OK) st = temp((size_t)count * 4 + 4, &outputs);  // + the scan total
+  dg_buffer* actions = nullptr;
+  if (st == DG_OK) st = temp(count, &actions);
   if (st == DG_OK) st = temp(16, &counters);
   if (st == DG_OK) st = temp(scan_scratch_bytes(count), &scratch);
   // The learned proposal's inputs, and its decision on the plain rule's candidates.
@@ -771,7 +792,7 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   DG_LAUNCH(ctx, "densify_count",
             densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
                 dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, count, typed<uint32_t>(outputs),
-                typed<uint32_t>(counters)));
+                typed<uint8_t>(actions), typed<uint32_t>(counters)));
   uint32_t* total_ptr = typed<uint32_t>(outputs) + count;
   st = scan_launch(ctx, typed<uint32_t>(outputs), count, nullptr, total_ptr, scratch->ptr);
   uint32_t readback[5];
@@ -840,19 +861,16 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   dg_renderer* r = t->renderer;
   const uint64_t elements = (uint64_t)count * MOMENT_SLOTS;
   DG_LAUNCH(ctx, "densify_copy",
-            densify_copy_kernel<<<(uint32_t)((elements + 255) / 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, typed<float>(r->sh),
+            densify_copy_kernel<<<std::max(1u, std::min((uint32_t)((elements + 255) / 256), (uint32_t)ctx->sm_count * 8u)),
+                                  256, 0, ctx->stream>>>(
+                dp, typed<float>(t->params), typed<uint8_t>(actions), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),
                 count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
-                typed<uint32_t>(ids), typed<float2>(aux)));
+                typed<uint32_t>(ids), typed<float2>(aux), typed<float>(gaussians)));
   DG_LAUNCH(ctx, "densify_place",
             densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, typed<uint32_t>(outputs), count,
-                typed<float>(params)));
-  const uint64_t floats = (uint64_t)new_count * FLOATS_PER_GAUSSIAN;
-  DG_LAUNCH(ctx, "activate",
-            activate_kernel<<<(uint32_t)((floats + 255) / 256), 256, 0, ctx->stream>>>(
-                typed<float>(params), typed<float>(gaussians), new_count));
+                dp, typed<float>(t->params), typed<uint8_t>(actions), typed<uint32_t>(outputs), count,
+                typed<float>(params), typed<float>(gaussians)));
   // Hand the new set to the renderer; the old buffers go once the work above is done.
   drop_graph(t);
   st = dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree);
