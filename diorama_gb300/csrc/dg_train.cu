@@ -116,18 +116,17 @@ __device__ __forceinline__ uint32_t pcg(uint32_t v) {
 
 __device__ __forceinline__ float unit_of(uint32_t h) { return ((float)(h >> 8u) + 0.5f) / 16777216.0f; }
 
+// Slot k of Gaussian i, whose action is a (1 keep, 2 clone, 3 split) and whose
+// first output is o.
 __device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const float* __restrict__ params,
-                                                  const uint8_t* __restrict__ actions, const float* __restrict__ sh,
-                                                  const float2* __restrict__ moments, const uint32_t* __restrict__ ids,
-                                                  const float2* __restrict__ aux, const uint32_t* __restrict__ outputs,
+                                                  const float* __restrict__ sh, const float2* __restrict__ moments,
+                                                  const uint32_t* __restrict__ ids, const float2* __restrict__ aux,
                                                   uint32_t first_id, float* __restrict__ new_params,
                                                   float* __restrict__ new_sh, float2* __restrict__ new_moments,
                                                   uint32_t* __restrict__ new_ids, float2* __restrict__ new_aux,
-                                                  float* __restrict__ new_gaussians, uint32_t e) {
-  const uint32_t i = e / MOMENT_SLOTS, k = e % MOMENT_SLOTS;
-  const uint32_t a = actions[i];
-  if (a == 0) return;
-  const uint32_t o = outputs[i];
+                                                  float* __restrict__ new_gaussians, uint32_t i, uint32_t k,
+                                                  uint32_t a, uint32_t o) {
+  const uint32_t e = i * MOMENT_SLOTS + k;
   const uint32_t copies = a == 1 ? 1u : 2u;
   if (k == 0) {
     for (uint32_t c = 0; c < copies; c++) {
@@ -169,7 +168,7 @@ __device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const
 }
 
 // src/shaders/densify.wgsl:148-180, split in two for coalescing. This kernel takes
-// one (Gaussian, moment slot) at a time per thread and copies the Adam moments (kept for a
+// one Gaussian per warp, a moment slot per lane, and copies the Adam moments (kept for a
 // kept Gaussian and a clone's original, zero for new ones), the raw parameters
 // and the SH coefficients; densify_place_kernel then places split children.
 // The identity of each output Gaussian and its learned-densification statistics
@@ -188,12 +187,19 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
                                                            uint32_t* __restrict__ new_ids,
                                                            float2* __restrict__ new_aux,
                                                            float* __restrict__ new_gaussians) {
-  // A grid-stride loop over (Gaussian, slot): one thread per slot would spend more
-  // on launching a quarter of a million tiny CTAs than on the copy.
-  const uint32_t slots = count * MOMENT_SLOTS;
-  for (uint32_t e = blockIdx.x * 256 + threadIdx.x; e < slots; e += gridDim.x * 256)
-    densify_copy_slot(dp, params, actions, sh, moments, ids, aux, outputs, first_id, new_params, new_sh, new_moments,
-                      new_ids, new_aux, new_gaussians, e);
+  // A warp per Gaussian, grid-stride: the action and output offset are read once
+  // per Gaussian, and the 61 slots (lanes l and l + 32) are contiguous runs.
+  const uint32_t lane = threadIdx.x & 31u, warps = gridDim.x * (256u / 32u);
+  for (uint32_t i = blockIdx.x * (256u / 32u) + (threadIdx.x >> 5); i < count; i += warps) {
+    const uint32_t a = actions[i];
+    if (a == 0) continue;
+    const uint32_t o = outputs[i];
+    densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids, new_aux,
+                      new_gaussians, i, lane, a, o);
+    if (lane + 32u < MOMENT_SLOTS)
+      densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids,
+                        new_aux, new_gaussians, i, lane + 32u, a, o);
+  }
 }
 
 // Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and Box-Muller.
@@ -859,10 +865,9 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
     return st;
   }
   dg_renderer* r = t->renderer;
-  const uint64_t elements = (uint64_t)count * MOMENT_SLOTS;
   DG_LAUNCH(ctx, "densify_copy",
-            densify_copy_kernel<<<std::max(1u, std::min((uint32_t)((elements + 255) / 256), (uint32_t)ctx->sm_count * 8u)),
-                                  256, 0, ctx->stream>>>(
+            densify_copy_kernel<<<std::max(1u, std::min(ceil_div(count, 8), (uint32_t)ctx->sm_count * 8u)), 256, 0,
+                                  ctx->stream>>>(
                 dp, typed<float>(t->params), typed<uint8_t>(actions), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),
                 count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
