@@ -1,6 +1,6 @@
 """Benchmark: training steps/s at 1.1M Gaussians.
 
-Workload (BASELINE configs 1 and 3): config 1's synthetic scene of 40 random
+Workload: a seeded synthetic scene of 40 random
 planes and boxes grown to 1.1M Gaussians (SH degree 3), trained against
 photos rendered from a 500k-Gaussian ground truth on the same surfaces, seen
 by 263 training cameras on a jittered ring at 980x545 (fov 55 deg). One step
@@ -58,8 +58,8 @@ def parse():
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
     ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn"],
-                    help="train: the headline training step; sort: config 2's sort/scan/ranges stress "
-                         "(1.1M Gaussians at 1960x1090, the reference's 6-pass sort); densify: config 1/4, "
+                    help="train: the headline training step; sort: the sort/scan/ranges stress "
+                         "(1.1M random Gaussians at 1960x1090, the reference's 6-pass sort); densify: "
                          "plain vs learned densification on the planes-and-boxes scene (minutes); knn: the "
                          "starting Gaussians' nearest-neighbour distances of a point cloud")
     ap.add_argument("--knn-points", type=int, default=1_100_000, help="knn workload: points in the cloud")
@@ -104,7 +104,7 @@ def barrier(group):
 
 def config(args, world):
     return {
-        "workload": "config 3: config-1 planes-and-boxes scene grown to 1.1M Gaussians, one optimize() step per 980x545 "
+        "workload": "planes-and-boxes scene grown to 1.1M Gaussians, one optimize() step per 980x545 "
                     "training view, full step as one CUDA graph",
         "gaussians": args.gaussians,
         "viewport": [980, 545],
@@ -282,8 +282,8 @@ def run_ours(args, rank, world, local, group):
     e2e = {"value": world * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": W * H * 4 + camera_bytes + adam_bytes
            + 8 + 16, "d2h_bytes_per_step": 8 + 4}
 
-    # The same steps without graph replay (config 3 reports the captured step
-    # against the uncaptured one).
+    # The same steps without graph replay (the captured step is reported against
+    # the uncaptured one).
     trainer.setGraph(False)
     trainer.step()
     device.synchronize()
@@ -417,6 +417,19 @@ def measure_held_out(device, renderer, held, repeats: int) -> dict:
             renderer.encode(None, tex, cam, bg)
     end.record()
     per_view = n * reps / (start.elapsed_ms(end) / 1000.0)
+    # Where a batched render's time goes: one render launched directly (no graph),
+    # each kernel bracketed by events.
+    renderer.setViewBatching(tuned["batch"], tuned["coopMin"], False)
+    renderer.renderViews(held, bg, targets)
+    device.synchronize()
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    renderer.renderViews(held, bg, targets)
+    report = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    renderer.setViewBatching(tuned["batch"], tuned["coopMin"], True)
+    kernels = {k: {"us": round(t * 1000, 1), "launches": c} for k, (c, t) in
+               sorted(report.items(), key=lambda kv: -kv[1][1])}
     # The last view's image both ways.
     renderer.encode(None, tex, held[-1], bg)
     renderer.afterSubmit()
@@ -425,7 +438,7 @@ def measure_held_out(device, renderer, held, repeats: int) -> dict:
     targets.destroy()
     return {"views": n, "frames_per_s": round(batched, 1), "per_view_frames_per_s": round(per_view, 1),
             "batch": tuned["batch"], "coop_min": tuned["coopMin"], "tuner_candidates": len(tuned["seconds"]),
-            "last_view_identical": same}
+            "last_view_identical": same, "kernels_one_batch": kernels}
 
 
 def views_host(views):
@@ -497,17 +510,17 @@ def run_reference(args, rank, world, group):
 
 
 def run_sort_stress(args, rank, local):
-    """Config 2 through the reference-structured TileRasterizer: tile counts, the
-    exclusive scan, 64-bit (tile, depth) keys, the 6-pass radix sort and the
+    """1.1M random Gaussians over [-3, 3]^3 at 1960x1090 through the
+    reference-structured TileRasterizer: tile counts, the exclusive scan, 64-bit (tile, depth) keys, the 6-pass radix sort and the
     ranges, each kernel timed with CUDA events; GB/s of the algorithmic bytes
     against the measured HBM peak. (The keys, permutation and ranges are checked
-    bit for bit against the oracle by tests/test_gpu_configs.py.)"""
+    bit for bit against the oracle by tests/test_gpu_workloads.py.)"""
     if rank != 0:
         return None
     from diorama_gb300 import Device, GaussianRenderer, TileRasterizer, scenes
     import oracle
 
-    raw, sh, camera = scenes.config2(0)
+    raw, sh, camera = scenes.random_scene_1m(0)
     act = scenes.activate64(raw).astype(np.float32)
     device = Device(local)
     r = GaussianRenderer(device)
@@ -588,7 +601,7 @@ def run_sort_stress(args, rank, local):
     cpu_scan = n / (time.perf_counter() - t0)
 
     result = {
-        "metric": "config 2 sort/scan/ranges", "workload": "config 2: 1.1M Gaussians in [-3,3]^3 at 1960x1090, "
+        "metric": "sort/scan/ranges keys/s", "workload": "1.1M random Gaussians in [-3,3]^3 at 1960x1090, "
         "16x16 tiles, reference-structured tile stage", "keys": keys, "gaussians": n, "tiles": tiles,
         "steps": args.steps, "peak_hbm_gbs": hbm,
         "sort": frac(sort_bytes, sort_us), "scan": frac(scan_bytes, per.get("scan", 0.0)),
@@ -675,7 +688,7 @@ def run_knn(args, rank, local):
 
 
 def run_densify_experiment(args, rank, local):
-    """Configs 1 and 4: the planes-and-boxes scene (500k ground-truth Gaussians,
+    """The planes-and-boxes scene (500k ground-truth Gaussians,
     263 training and 37 held-out 980x545 views), trained from 100k noisy surface
     samples. Seeded plain runs log each clone/split candidate's features and
     whether its children survive pruning 1,000 steps later; the model (MLP 12 ->
@@ -793,7 +806,7 @@ def run_densify_experiment(args, rank, local):
     device.destroy()
     return {
         "metric": "time to held-out PSNR, learned vs plain densify", "unit": "s",
-        "workload": "configs 1/4: planes-and-boxes scene (500k ground truth), 263 + 37 views at 980x545, "
+        "workload": "planes-and-boxes scene (500k ground truth), 263 + 37 views at 980x545, "
                     f"{steps} steps from 100k noisy surface samples", "target_psnr": round(target, 3),
         "plain_runs_logged": logged, "samples": int(labels.size), "survived_rate": float(labels.mean()),
         "mlp": {"epochs": 5, "batch": 1024, "lr": 1e-3, "weight_decay": 0.01, "balanced_classes": not args.unbalanced,

@@ -184,14 +184,14 @@ inline uint32_t stride_grid(const dg_context* ctx, uint64_t n, uint32_t threads)
 // duplicate_kernel's warp-cooperative emission over splats in depth order: the
 // pairs of 32 consecutive sorted splats are one contiguous run of slots. Keys are
 // the tile index alone (u32), values the splat index. For a batch of views
-// (splat v * per_view + i is Gaussian i in view v), the tiles of view v are
-// numbered after those of the views before it.
+// (splat v * per_view + i is Gaussian i in view v), the key of a tile of view v
+// is v << view_shift | its tile index within the view.
 __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Camera* __restrict__ camera,
                                                                        const float* __restrict__ splats,
                                                                        const uint32_t* __restrict__ order,
                                                                        const uint32_t* __restrict__ offsets,
                                                                        uint32_t count, uint32_t per_view,
-                                                                       uint32_t capacity,
+                                                                       uint32_t view_shift, uint32_t capacity,
                                                                        uint32_t* __restrict__ keys,
                                                                        uint32_t* __restrict__ values) {
   __shared__ uint32_t s_excl[DUP_THREADS];
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   __shared__ uint32_t s_y0[DUP_THREADS];
   __shared__ uint32_t s_w[DUP_THREADS];
   __shared__ uint32_t s_index[DUP_THREADS];
-  __shared__ uint32_t s_base[DUP_THREADS];  // the first tile number of the splat's view
+  __shared__ uint32_t s_base[DUP_THREADS];  // the splat's view, shifted into place
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t j = blockIdx.x * DUP_THREADS + threadIdx.x;
   const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   s_y0[threadIdx.x] = rect.y;
   s_w[threadIdx.x] = rect.z - rect.x;
   s_index[threadIdx.x] = index;
-  s_base[threadIdx.x] = (index / per_view) * (tiles.x * tiles.y);
+  s_base[threadIdx.x] = (index / per_view) << view_shift;
   __syncwarp();
   for (uint32_t k = lane; k < total; k += 32) {
     int lo = 0;
@@ -349,10 +349,17 @@ template <int STRIDE>
 __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32_t* __restrict__ key_words,
                                                                     const uint32_t* __restrict__ pair_total,
                                                                     uint32_t capacity, uint32_t tiles,
+                                                                    uint32_t view_shift, uint32_t tiles_per_view,
                                                                     uint2* __restrict__ ranges) {
   const uint32_t n = min(pair_total[0], capacity);
-  // Pair i with tile `tile` after pair i - 1 with tile `prev` (~0u for none).
-  auto edge = [&](uint32_t i, uint32_t tile, uint32_t prev) {
+  // A key's tile: view * tiles_per_view + local tile for a batch of views keyed
+  // view << view_shift | local tile; the key itself when view_shift is 0 and
+  // tiles_per_view 1.
+  const uint32_t local_mask = (1u << view_shift) - 1u;
+  auto tile_of = [&](uint32_t key) { return (key >> view_shift) * tiles_per_view + (key & local_mask); };
+  // Pair i with key `key` after pair i - 1 with key `prev_key` (none for i = 0).
+  auto edge = [&](uint32_t i, uint32_t key, uint32_t prev_key) {
+    const uint32_t tile = tile_of(key), prev = i ? tile_of(prev_key) : ~0u;
     if (tile >= tiles) return;  // only possible after a sort whose bounded wait gave up
     if (tile != prev) {
       if (i > 0 && prev < tiles) ranges[prev].y = i;
@@ -369,16 +376,16 @@ __global__ void __launch_bounds__(RANGE_THREADS) find_ranges_kernel(const uint32
     for (uint32_t q = first; q < quads; q += stride) {
       const uint4 k = reinterpret_cast<const uint4*>(key_words)[q];
       const uint32_t i = 4 * q;
-      edge(i, k.x, i ? key_words[i - 1] : ~0u);
+      edge(i, k.x, i ? key_words[i - 1] : 0u);
       edge(i + 1, k.y, k.x);
       edge(i + 2, k.z, k.y);
       edge(i + 3, k.w, k.z);
     }
-    for (uint32_t i = 4 * quads + first; i < n; i += stride) edge(i, key_words[i], i ? key_words[i - 1] : ~0u);
+    for (uint32_t i = 4 * quads + first; i < n; i += stride) edge(i, key_words[i], i ? key_words[i - 1] : 0u);
   } else {
     for (uint32_t i = first; i < n; i += stride)
       edge(i, key_words[STRIDE * (size_t)i + (STRIDE - 1)],
-           i ? key_words[STRIDE * (size_t)(i - 1) + (STRIDE - 1)] : ~0u);
+           i ? key_words[STRIDE * (size_t)(i - 1) + (STRIDE - 1)] : 0u);
   }
 }
 
@@ -895,7 +902,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
     if (count > 0) {
       DG_LAUNCH(ctx, "duplicate",
                 duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
-                    cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count, count,
+                    cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count, count, 0u,
                     tr->pair_capacity, typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values)));
     }
     DG_TRY(sort_launch(ctx, tr->tile_plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
@@ -903,7 +910,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
     DG_LAUNCH(ctx, "find_ranges",
               find_ranges_kernel<1><<<stride_grid(ctx, tr->pair_capacity, RANGE_THREADS), RANGE_THREADS, 0,
                                       st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
-                                            tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+                                            tr->pair_capacity, tr->tiles_x * tr->tiles_y, 0u, 1u, typed<uint2>(tr->ranges)));
     tr->keys_are_tiles = true;
     return launch_rasterize(tr, target);
   }
@@ -928,7 +935,8 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
   DG_LAUNCH(ctx, "find_ranges",
             find_ranges_kernel<2><<<stride_grid(ctx, tr->pair_capacity, RANGE_THREADS), RANGE_THREADS, 0,
                                     st>>>(typed<uint32_t>(tr->keys), typed<uint32_t>(tr->scan_total),
-                                          tr->pair_capacity, tr->tiles_x * tr->tiles_y, typed<uint2>(tr->ranges)));
+                                          tr->pair_capacity, tr->tiles_x * tr->tiles_y, 0u, 1u,
+                                          typed<uint2>(tr->ranges)));
   return launch_rasterize(tr, target);
 }
 
@@ -988,11 +996,11 @@ dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32
 
 
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
-                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,
-                                  uint32_t* keys, uint32_t* values) {
+                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t view_shift,
+                                  uint32_t capacity, uint32_t* keys, uint32_t* values) {
   DG_LAUNCH(ctx, "duplicate",
             duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, ctx->stream>>>(
-                camera, splats, order, offsets, count, per_view, capacity, keys, values));
+                camera, splats, order, offsets, count, per_view, view_shift, capacity, keys, values));
   return DG_OK;
 }
 
@@ -1000,7 +1008,16 @@ dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const u
                              uint32_t tiles, uint2* ranges) {
   DG_LAUNCH(ctx, "find_ranges",
             find_ranges_kernel<1><<<stride_grid(ctx, capacity, RANGE_THREADS), RANGE_THREADS, 0, ctx->stream>>>(
-                tile_keys, pair_total, capacity, tiles, ranges));
+                tile_keys, pair_total, capacity, tiles, 0u, 1u, ranges));
+  return DG_OK;
+}
+
+dg_status find_view_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total,
+                                  uint32_t capacity, uint32_t view_shift, uint32_t tiles_per_view, uint32_t tiles,
+                                  uint2* ranges) {
+  DG_LAUNCH(ctx, "find_ranges",
+            find_ranges_kernel<1><<<stride_grid(ctx, capacity, RANGE_THREADS), RANGE_THREADS, 0, ctx->stream>>>(
+                tile_keys, pair_total, capacity, tiles, view_shift, tiles_per_view, ranges));
   return DG_OK;
 }
 

@@ -96,10 +96,14 @@ dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32
                                   const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
                                   uint32_t* tile_counts, uint2* depth_keys, uint32_t* order);
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
-                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t capacity,
-                                  uint32_t* keys, uint32_t* values);
+                                  const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t view_shift,
+                                  uint32_t capacity, uint32_t* keys, uint32_t* values);
 dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
                              uint32_t tiles, uint2* ranges);
+// The same for a batch of views whose pair keys are view << view_shift | local tile.
+dg_status find_view_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total,
+                                  uint32_t capacity, uint32_t view_shift, uint32_t tiles_per_view, uint32_t tiles,
+                                  uint2* ranges);
 dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr);
 }  // namespace dg
 

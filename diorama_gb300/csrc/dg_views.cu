@@ -24,6 +24,11 @@ uint32_t bits_for(uint32_t n) {
   return b;
 }
 
+// Where a batch's pair keys hold the view: above the whole 8-bit digits that
+// number a view's tiles, so the tile sort's passes never read it. A batch holds
+// fewer than 2^24 tiles, so the view always fits above them.
+uint32_t view_shift_for(uint32_t tiles_per_view) { return (bits_for(tiles_per_view) + 7) / 8 * 8; }
+
 dg_status ensure(dg_context* ctx, dg_buffer** buf, size_t bytes) {
   if (*buf && (*buf)->bytes >= bytes) return DG_OK;
   free_buffer(*buf);
@@ -78,7 +83,7 @@ namespace {
 
 dg_status grow_pairs(dg_view_batch* b, uint32_t capacity) {
   dg_context* ctx = b->ctx;
-  const SortPlan tile_plan = sort_plan_digits(capacity, 1, bits_for(b->views * b->tiles_per_view));
+  const SortPlan tile_plan = sort_plan_digits(capacity, 1, bits_for(b->tiles_per_view));
   DG_TRY(ensure(ctx, &b->keys, (size_t)capacity * 4));
   DG_TRY(ensure(ctx, &b->keys_alt, (size_t)capacity * 4));
   DG_TRY(ensure(ctx, &b->values, (size_t)capacity * 4));
@@ -145,18 +150,22 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   uint32_t* order = depth_plan.passes & 1 ? typed<uint32_t>(b->order_alt) : typed<uint32_t>(b->order);
   DG_TRY(scan_launch(ctx, typed<uint32_t>(b->counts_sorted), n, nullptr, typed<uint32_t>(b->scan_total),
                      b->scan_scratch->ptr, order, typed<uint32_t>(b->tile_counts)));
+  // Pairs in depth order, view-major, keyed view << shift | local tile: a stable
+  // sort on the local tile's bits alone leaves every (view, tile) run contiguous
+  // and in depth order, an 8-bit pass fewer than sorting global tile numbers.
+  const uint32_t shift = view_shift_for(b->tiles_per_view);
   DG_TRY(duplicate_sorted_launch(ctx, typed<Camera>(b->cameras), typed<float>(b->splats), order,
-                                 typed<uint32_t>(b->counts_sorted), n, b->count, b->pair_capacity,
+                                 typed<uint32_t>(b->counts_sorted), n, b->count, shift, b->pair_capacity,
                                  typed<uint32_t>(b->keys), typed<uint32_t>(b->values)));
-  const SortPlan tile_plan = sort_plan_digits(b->pair_capacity, 1, bits_for(tiles));
+  const SortPlan tile_plan = sort_plan_digits(b->pair_capacity, 1, bits_for(b->tiles_per_view));
   DG_TRY(sort_launch(ctx, tile_plan, b->keys->ptr, typed<uint32_t>(b->values), b->keys_alt->ptr,
                      typed<uint32_t>(b->values_alt), typed<uint32_t>(b->scan_total), b->sort_scratch->ptr));
   const bool odd = tile_plan.passes & 1;
   const uint32_t* tile_keys = typed<uint32_t>(odd ? b->keys_alt : b->keys);
   const uint32_t* pair_splats = typed<uint32_t>(odd ? b->values_alt : b->values);
   DG_CUDA(cudaMemsetAsync(b->ranges->ptr, 0, (size_t)tiles * 8, ctx->stream));
-  DG_TRY(find_ranges_launch(ctx, tile_keys, typed<uint32_t>(b->scan_total), b->pair_capacity, tiles,
-                            typed<uint2>(b->ranges)));
+  DG_TRY(find_view_ranges_launch(ctx, tile_keys, typed<uint32_t>(b->scan_total), b->pair_capacity, shift,
+                                 b->tiles_per_view, tiles, typed<uint2>(b->ranges)));
   BlendForward f{};
   f.camera = typed<Camera>(b->cameras);
   f.raster_params = typed<float4>(b->raster_params);

@@ -1,8 +1,8 @@
-"""Seeded synthetic scenes of the benchmark configurations.
+"""Seeded synthetic scenes of the benchmark workloads.
 
 The reference trains on the Tanks and Temples "train" photos, which are not
 available here; these seeded scenes stand in for them with the shapes, sizes and
-value distributions the configurations name. Everything is drawn with
+value distributions of the workloads. Everything is drawn with
 numpy.random.default_rng(seed) in float64 and cast to float32, so every machine
 gets the same bits.
 
@@ -11,7 +11,7 @@ gets the same bits.
   the 15 higher coefficients N(0, 0.05) (raw training parameters).
 - sphere_camera: a pinhole camera on a radius-4 sphere looking at the origin.
 - surface_scene: Gaussians clustered on random planes and boxes, with a ring of
-  cameras at radius 3-5 around them, for the full training configuration.
+  cameras at radius 3-5 around them, for the full training workload.
 """
 
 from __future__ import annotations
@@ -28,7 +28,7 @@ SH_C0 = 0.28209479177387814
 
 
 def random_gaussians(count: int, seed: int, half_extent: float = 1.0):
-    """Raw parameters (16 floats each) and SH rest (45 each) of config 0's distribution."""
+    """Raw parameters (16 floats each) and SH rest (45 each) of the random scenes' distribution."""
     rng = np.random.default_rng(seed)
     raw = np.zeros((count, FLOATS_PER_GAUSSIAN), np.float64)
     raw[:, 0:3] = rng.uniform(-half_extent, half_extent, (count, 3))
@@ -54,7 +54,7 @@ def activate64(raw: np.ndarray) -> np.ndarray:
 
 
 def sphere_camera(seed: int, width: int = 256, height: int = 256, fov_deg: float = 60.0, radius: float = 4.0):
-    """Config 0's camera: a seeded direction on a radius-4 sphere, looking at the origin."""
+    """A seeded direction on a radius-4 sphere, looking at the origin."""
     rng = np.random.default_rng(seed + 1000)
     d = rng.normal(size=3)
     d = d / np.linalg.norm(d)
@@ -65,20 +65,20 @@ def sphere_camera(seed: int, width: int = 256, height: int = 256, fov_deg: float
     return CameraData(view=view, proj=proj, viewport=(width, height))
 
 
-def config0(seed: int = 0):
-    """Config 0: 16,384 Gaussians, 256x256, fov 60 deg, black background, SH degree 3."""
+def random_scene_16k(seed: int = 0):
+    """16,384 random Gaussians in [-1, 1]^3 seen at 256x256, fov 60 deg (black background, SH degree 3)."""
     raw, sh = random_gaussians(16384, seed)
     return raw, sh, sphere_camera(seed)
 
 
-def config2(seed: int = 0):
-    """Config 2: 1.1M Gaussians of config 0's distribution over [-3, 3]^3 at 1960x1090."""
+def random_scene_1m(seed: int = 0):
+    """1.1M random Gaussians of the same distribution over [-3, 3]^3, seen at 1960x1090."""
     raw, sh = random_gaussians(1_100_000, seed, half_extent=3.0)
     return raw, sh, sphere_camera(seed, 1960, 1090)
 
 
 def surface_scene(count: int, seed: int, noise: float = 0.0, shape_seed: int = 7):
-    """Gaussians on config 1's 40 planes and boxes (raw params, SH rest). The shapes
+    """Gaussians on 40 seeded planes and boxes (raw params, SH rest). The shapes
     come from shape_seed, so ground truth and initial points share surfaces."""
     shape_rng = np.random.default_rng(shape_seed)
     pts_rng = np.random.default_rng(seed)
@@ -121,7 +121,7 @@ def _surface_points_shared(shape_rng, pts_rng, count: int, shapes: int = 40):
 
 
 def ring_cameras(count: int = 300, seed: int = 3, width: int = 980, height: int = 545, fov_deg: float = 55.0):
-    """Config 1's cameras: a jittered ellipse ring of radius 3-5 around the origin.
+    """The 300-photo scene's cameras: a jittered ellipse ring of radius 3-5 around the origin.
     Every 8th (i % 8 == 7) is held out: 263 training views and 37 held-out ones."""
     rng = np.random.default_rng(seed)
     cams = []

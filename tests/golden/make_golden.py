@@ -10,7 +10,7 @@ oracles. Run here, where the reference is mounted (it is not on GPU machines):
 2. oracle/chunked.py (the tile-chunked float64 renderer) is checked against the
    reference's dense render() on the backward fixture scene and on a 64x48,
    300-Gaussian scene: images and gradients must agree to 1e-10.
-3. config0.npz: the config-0 scene (16,384 Gaussians of seed 0, 256x256, SH
+3. random_16k.npz: the 16,384-Gaussian random scene (16,384 Gaussians of seed 0, 256x256, SH
    degree 3, black background) against a photo rendered from seed 1 and
    quantized to rgba8: the float64 image, loss_reference.loss, and autograd
    gradients with respect to the activated parameters.
@@ -108,9 +108,9 @@ def check_chunked(br) -> None:
         assert err < 1e-10 and gerr < 1e-10
 
 
-def make_config0(lr) -> None:
+def make_random_16k(lr) -> None:
     torch.set_default_dtype(torch.float64)
-    raw, sh, cam = scenes.config0(seed=0)
+    raw, sh, cam = scenes.random_scene_16k(seed=0)
     raw_t, sh_t = scenes.random_gaussians(16384, seed=1)
     view, proj = chunked.as_matrix(cam.view), chunked.as_matrix(cam.proj)
     W, H = cam.viewport
@@ -133,10 +133,10 @@ def make_config0(lr) -> None:
     y = torch.from_numpy(target[:, :3].astype(np.float64) / 255).reshape(H, W, 3).permute(2, 0, 1)
     value = lr.loss(render, y)
     value.backward()
-    print(f"config 0: loss {value.item():.10f} in {time.time() - start:.1f} s")
+    print(f"random 16k scene: loss {value.item():.10f} in {time.time() - start:.1f} s")
     names = ["position", "scale", "rotation", "opacity", "color", "sh"]
     np.savez_compressed(
-        HERE / "config0.npz",
+        HERE / "random_16k.npz",
         target_rgba8=target.reshape(H, W, 4),
         image=image.detach().numpy().astype(np.float32),
         loss=np.float64(value.item()),
@@ -147,7 +147,7 @@ def make_config0(lr) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--skip-config0", action="store_true")
+    ap.add_argument("--skip-random-16k", action="store_true")
     args = ap.parse_args()
     ref = Path(args.reference)
     fixtures = ref / "src" / "checks" / "fixtures"
@@ -158,8 +158,8 @@ def main() -> None:
     w = regenerate(lr, fixtures / "loss.json", HERE / "loss.json")
     print(f"loss.json reproduces the reference fixture to {w:.1e}")
     check_chunked(br)
-    if not args.skip_config0:
-        make_config0(lr)
+    if not args.skip_random_16k:
+        make_random_16k(lr)
 
 
 if __name__ == "__main__":

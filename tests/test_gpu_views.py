@@ -18,10 +18,9 @@ pytestmark = pytest.mark.gpu
 BG = (0.1, 0.2, 0.3)
 
 
-@pytest.fixture(scope="module")
-def scene(device):
+def _render_singly(device, size):
     raw, sh = scenes.surface_scene(200_000, 22, noise=0.01)
-    _train, held = scenes.ring_cameras()
+    _train, held = scenes.ring_cameras(**size)
     r = GaussianRenderer(device)
     r.setGaussians(activate(raw), {"rest": sh.reshape(-1), "degree": 3})
     cams = held[:6]
@@ -36,8 +35,23 @@ def scene(device):
         lasts.append(r.pixelLastBuffer.read(np.uint32)[: W * H].copy())
         images.append(tex.buffer.read(np.uint8)[: W * H * 4].copy())
     tex.destroy()
-    yield r, cams, colors, lasts, images
-    r.destroy()
+    return r, cams, colors, lasts, images
+
+
+@pytest.fixture(scope="module")
+def scene(device):
+    # 980 x 545: 62 x 35 tiles a view, keys view << 16 | tile.
+    s = _render_singly(device, {})
+    yield s
+    s[0].destroy()
+
+
+@pytest.fixture(scope="module")
+def small_scene(device):
+    # 200 x 150: 13 x 10 tiles a view, keys view << 8 | tile.
+    s = _render_singly(device, {"width": 200, "height": 150})
+    yield s
+    s[0].destroy()
 
 
 def _check(device, r, cams, colors, lasts, images, batch):
@@ -66,6 +80,14 @@ def test_views_match_single_view_renders(device, scene, batch, graph):
     r.setViewBatching(batch, 0, graph)
     _check(device, r, cams, colors, lasts, images, batch)
     _check(device, r, cams, colors, lasts, images, batch)  # replays the captured batch
+    assert device.check() == 0
+
+
+@pytest.mark.parametrize("batch", [0, 4])
+def test_small_views_match_single_view_renders(device, small_scene, batch):
+    r, cams, colors, lasts, images = small_scene
+    r.setViewBatching(batch, 0, True)
+    _check(device, r, cams, colors, lasts, images, batch)
     assert device.check() == 0
 
 

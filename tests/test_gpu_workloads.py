@@ -1,11 +1,11 @@
-"""The benchmark configurations on the GPU.
+"""The two random-scene workloads on the GPU.
 
-Config 0 (16,384 Gaussians, 256x256, SH degree 3): one forward + loss + backward
+16,384 Gaussians at 256x256 (SH degree 3): one forward + loss + backward
 against the reference's float64 PyTorch oracle (golden vectors in
-tests/golden/config0.npz; image within 1e-5 max-abs, gradients within 1e-4 of
+tests/golden/random_16k.npz; image within 1e-5 max-abs, gradients within 1e-4 of
 each group's largest) and bit for bit against the oracle's forward.
 
-Config 2 (1.1M Gaussians over [-3, 3]^3 at 1960x1090, ~12M keys): splats, the
+1.1M Gaussians over [-3, 3]^3 at 1960x1090 (~12M keys): splats, the
 scan of tile counts, the sorted (tile, depth) keys, the permutation and the
 per-tile ranges bit for bit against the oracle."""
 
@@ -21,9 +21,9 @@ from helpers import GOLDEN, cam_array, group_errors
 pytestmark = pytest.mark.gpu
 
 
-def test_config0_forward_loss_backward(device):
-    g = np.load(GOLDEN / "config0.npz")
-    raw, sh, camera = scenes.config0(0)
+def test_random_16k_forward_loss_backward(device):
+    g = np.load(GOLDEN / "random_16k.npz")
+    raw, sh, camera = scenes.random_scene_16k(0)
     act = scenes.activate64(raw).astype(np.float32)
     W, H = camera.viewport
     r = GaussianRenderer(device)
@@ -56,8 +56,8 @@ def test_config0_forward_loss_backward(device):
     r.destroy()
 
 
-def test_config2_sort_scan_ranges_bit_exact(device):
-    raw, sh, camera = scenes.config2(0)
+def test_random_1m_sort_scan_ranges_bit_exact(device):
+    raw, sh, camera = scenes.random_scene_1m(0)
     act = scenes.activate64(raw).astype(np.float32)
     r = GaussianRenderer(device)
     r.setGaussians(act.reshape(-1), {"rest": sh.reshape(-1), "degree": 3})

@@ -1,7 +1,7 @@
 """The oracle (a float32 C restatement of the reference's path) against the
 reference's own golden vectors: the fixtures its PyTorch float64 oracles write
-(reference/backward_reference.py, reference/loss_reference.py) and the config-0
-vectors of tests/golden/make_golden.py. CPU only."""
+(reference/backward_reference.py, reference/loss_reference.py) and the 16,384-Gaussian
+random scene's vectors of tests/golden/make_golden.py. CPU only."""
 
 from __future__ import annotations
 
@@ -53,9 +53,9 @@ def test_cpu_ssim_rebuilds_the_loss():
     assert abs(cpu - f["loss"]) <= 1e-6
 
 
-def test_config0_against_reference_golden():
-    g = np.load(GOLDEN / "config0.npz")
-    raw, sh, camera = scenes.config0(0)
+def test_random_16k_against_reference_golden():
+    g = np.load(GOLDEN / "random_16k.npz")
+    raw, sh, camera = scenes.random_scene_16k(0)
     act = scenes.activate64(raw).astype(np.float32)
     cam = cam_array(camera)
     W, H = camera.viewport
