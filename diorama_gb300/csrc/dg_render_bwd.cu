@@ -293,7 +293,10 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
   }
 }
 
-constexpr uint32_t PBWD_THREADS = 128;
+#ifndef DG_PBWD_THREADS
+#define DG_PBWD_THREADS 128
+#endif
+constexpr uint32_t PBWD_THREADS = DG_PBWD_THREADS;  // a multiple of 32
 
 // Copies n floats between global and shared memory, 16 bytes at a time where both
 // ends allow it; all threads of the CTA take part.
@@ -543,6 +546,25 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
   copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
 }
 
+// The fused kernel's tuning (measured at 1.1M Gaussians: 128 threads, 9 and 8
+// slots, and no minimum of resident CTAs are the fastest of the sizes tried).
+// Slots a thread loads before stepping them in the Adam passes (SH: 45 slots per
+// thread in a full CTA; parameters: 16).
+#ifndef DG_ADAM_SH_BATCH
+#define DG_ADAM_SH_BATCH 9
+#endif
+#ifndef DG_ADAM_P_BATCH
+#define DG_ADAM_P_BATCH 8
+#endif
+// A minimum of resident CTAs per SM caps the registers (without one ptxas
+// settles at 96 a thread, 5 CTAs of 128 per SM; an explicit minimum of 1 lets it
+// take 141).
+#ifdef DG_PBWD_MIN_BLOCKS
+#define DG_PBWD_BOUNDS __launch_bounds__(PBWD_THREADS, DG_PBWD_MIN_BLOCKS)
+#else
+#define DG_PBWD_BOUNDS __launch_bounds__(PBWD_THREADS)
+#endif
+
 // The training step's preprocess backward with Adam applied at once
 // (src/shaders/preprocessBackward.wgsl:28-181, then src/shaders/adam.wgsl:80-107):
 // the CTA computes its 128 Gaussians' gradients into shared memory (the SH
@@ -553,7 +575,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
 // Each thread also adds its Gaussian's densification statistics
 // (src/shaders/adam.wgsl:126-134).
 // gaussian_grads and sh_grads (may be NULL) also receive the gradients.
-__global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
+__global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
     const Camera* __restrict__ camera, float* __restrict__ gaussians, float* __restrict__ sh, uint32_t count,
     const uint32_t* __restrict__ scene_params, const float* __restrict__ splats, const float* __restrict__ splat_grads,
     const AdamParams* __restrict__ adam, float* __restrict__ params, float2* __restrict__ moments,
@@ -589,7 +611,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
   // The SH slots (moment slots 16-60 of each record): each thread loads a batch of
   // slots before stepping them, so that enough reads are in flight to cover DRAM
   // latency at this kernel's occupancy.
-  constexpr uint32_t SH_BATCH = 9;  // 45 slots per thread in a full CTA = 5 batches
+  constexpr uint32_t SH_BATCH = DG_ADAM_SH_BATCH;
   float* sh_block = sh + (size_t)block_start * SH_REST_FLOATS;
   float2* sh_moments = moments + (size_t)block_start * MOMENT_SLOTS + FLOATS_PER_GAUSSIAN;
   const uint32_t sh_total = here * SH_REST_FLOATS;
@@ -618,7 +640,7 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_adam_kernel(
   }
   // The raw parameter slots (0-15 but 7 and 15) and their activated values, all
   // of a thread's slots loaded at once (16 per thread in a full CTA).
-  constexpr uint32_t P_BATCH = 8;
+  constexpr uint32_t P_BATCH = DG_ADAM_P_BATCH;
   float* p_block = params + (size_t)block_start * FLOATS_PER_GAUSSIAN;
   float* a_block = gaussians + (size_t)block_start * FLOATS_PER_GAUSSIAN;
   float2* p_moments = moments + (size_t)block_start * MOMENT_SLOTS;
