@@ -60,19 +60,27 @@ __device__ __forceinline__ float adam_param_slot(const AdamParams& ap, uint32_t 
 // length of its screen-space mean gradient in pixels, a count and the largest
 // radius go into stats; aux (the learned densification's extra statistics) gets
 // the squared length and the count of steps seen over the Gaussian's life.
-__device__ __forceinline__ void accumulate_stats_one(const float* __restrict__ viewport,
-                                                     const float* __restrict__ splats,
-                                                     const float* __restrict__ splat_grads, float4* __restrict__ stats,
-                                                     float2* __restrict__ aux, uint32_t i) {
-  const float radius = splats[(size_t)i * FLOATS_PER_SPLAT + 3];
+// The same from the values: the splat's radius and its mean's two gradients.
+__device__ __forceinline__ void accumulate_stats_values(const float* __restrict__ viewport, float radius,
+                                                        float mean_grad_x, float mean_grad_y,
+                                                        float4* __restrict__ stats, float2* __restrict__ aux,
+                                                        uint32_t i) {
   if (radius == 0.0f) return;
-  const float gx = splat_grads[(size_t)i * SPLAT_GRADS] * viewport[0] * 0.5f;
-  const float gy = splat_grads[(size_t)i * SPLAT_GRADS + 1] * viewport[1] * 0.5f;
+  const float gx = mean_grad_x * viewport[0] * 0.5f;
+  const float gy = mean_grad_y * viewport[1] * 0.5f;
   const float len = sqrtf(gx * gx + gy * gy);
   const float4 s = stats[i];
   stats[i] = make_float4(s.x + len, s.y + 1.0f, fmaxf(s.z, radius), 0.0f);
   const float2 a = aux[i];
   aux[i] = make_float2(a.x + len * len, a.y + 1.0f);
+}
+
+__device__ __forceinline__ void accumulate_stats_one(const float* __restrict__ viewport,
+                                                     const float* __restrict__ splats,
+                                                     const float* __restrict__ splat_grads, float4* __restrict__ stats,
+                                                     float2* __restrict__ aux, uint32_t i) {
+  accumulate_stats_values(viewport, splats[(size_t)i * FLOATS_PER_SPLAT + 3], splat_grads[(size_t)i * SPLAT_GRADS],
+                          splat_grads[(size_t)i * SPLAT_GRADS + 1], stats, aux, i);
 }
 
 }  // namespace dg

@@ -314,23 +314,24 @@ __device__ __forceinline__ void copy_floats(float* __restrict__ dst, const float
 // src/shaders/preprocessBackward.wgsl:28-181 for one Gaussian: the 16-float
 // Gaussian gradient (slots 7 and 15 zero) to out, and the 45 SH gradients over
 // its 45 SH coefficients in shv (shared memory).
-__device__ __forceinline__ void preprocess_backward_one(const Camera& cam, uint32_t i, const float* __restrict__ gaussians,
-                                                        float* shv, uint32_t basis_count,
-                                                        const float* __restrict__ splats,
-                                                        const float* __restrict__ splat_grads, float (&out)[16]) {
+// gaussian: the Gaussian's 16 activated floats (16-byte aligned); radius: its
+// splat's radius (0 when it was not drawn); grads: its 9 splat gradients. shv
+// holds its SH coefficients and receives their gradients.
+__device__ __forceinline__ void preprocess_backward_one(const Camera& cam, const float* __restrict__ gaussian,
+                                                        float* shv, uint32_t basis_count, float radius,
+                                                        const float* __restrict__ grads, float (&out)[16]) {
 #pragma unroll
   for (int k = 0; k < 16; k++) out[k] = 0.0f;
-  const bool visible = splats[(size_t)i * FLOATS_PER_SPLAT + 3] != 0.0f;
-  if (!visible) {
+  if (radius == 0.0f) {
     for (uint32_t k = 0; k < SH_REST_FLOATS; k++) shv[k] = 0.0f;
     return;
   }
   float grad[9];
 #pragma unroll
-  for (int k = 0; k < 9; k++) grad[k] = splat_grads[(size_t)i * SPLAT_GRADS + k];
+  for (int k = 0; k < 9; k++) grad[k] = grads[k];
   float g[16];
   {
-    const float4* gp = reinterpret_cast<const float4*>(gaussians + (size_t)i * FLOATS_PER_GAUSSIAN);
+    const float4* gp = reinterpret_cast<const float4*>(gaussian);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       float4 q = gp[k];
@@ -538,8 +539,9 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
   const uint32_t i = block_start + threadIdx.x;
   if (i < count) {
     float out[16];
-    preprocess_backward_one(s_cam, i, gaussians, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count, splats, splat_grads,
-                            out);
+    preprocess_backward_one(s_cam, gaussians + (size_t)i * FLOATS_PER_GAUSSIAN, s_sh + threadIdx.x * SH_REST_FLOATS,
+                            basis_count, splats[(size_t)i * FLOATS_PER_SPLAT + 3],
+                            splat_grads + (size_t)i * SPLAT_GRADS, out);
     store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);
   }
   __syncthreads();
@@ -598,8 +600,9 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
   const uint32_t i = block_start + threadIdx.x;
   if (i < count) {
     float out[16];
-    preprocess_backward_one(s_cam, i, gaussians, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count, splats, splat_grads,
-                            out);
+    preprocess_backward_one(s_cam, gaussians + (size_t)i * FLOATS_PER_GAUSSIAN, s_sh + threadIdx.x * SH_REST_FLOATS,
+                            basis_count, splats[(size_t)i * FLOATS_PER_SPLAT + 3],
+                            splat_grads + (size_t)i * SPLAT_GRADS, out);
 #pragma unroll
     for (int k = 0; k < 16; k++) s_pg[threadIdx.x * GP + k] = out[k];
     if (gaussian_grads) store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);

@@ -36,7 +36,10 @@ constexpr uint32_t FLAG_MASK = 3u << 30;
 constexpr uint32_t VALUE_MASK = (1u << 30) - 1;
 constexpr int HIST_THREADS = 256;
 constexpr int MAX_PASSES = 8;
-constexpr int LOOK_WIDTH = 4;  // predecessors read per look-back step
+#ifndef DG_SORT_LOOK_WIDTH
+#define DG_SORT_LOOK_WIDTH 4
+#endif
+constexpr int LOOK_WIDTH = DG_SORT_LOOK_WIDTH;  // predecessors read per look-back step (4-32 measured: 4-8 best)
 
 template <int KW>
 struct KeyOf;
