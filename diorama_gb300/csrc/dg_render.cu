@@ -70,10 +70,16 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
     off[2] = g[2] - campos[2];
     normalize3(off, dir);
     sh_basis(dir, basis);
-    for (uint32_t k = 0; k < basis_count; k++) {
-      color[0] = color[0] + basis[k] * shv[k * 3 + 0];
-      color[1] = color[1] + basis[k] * shv[k * 3 + 1];
-      color[2] = color[2] + basis[k] * shv[k * 3 + 2];
+    // Unrolled over all 15 terms (the ones past basis_count skipped), so the
+    // basis stays in registers; the sums run in the same order as a loop to
+    // basis_count.
+#pragma unroll
+    for (uint32_t k = 0; k < 15; k++) {
+      if (k < basis_count) {
+        color[0] = color[0] + basis[k] * shv[k * 3 + 0];
+        color[1] = color[1] + basis[k] * shv[k * 3 + 1];
+        color[2] = color[2] + basis[k] * shv[k * 3 + 2];
+      }
     }
   }
   out[0] = make_float4(mx, my, p.depth, radius);
@@ -107,6 +113,12 @@ __device__ __forceinline__ void load_gaussian(const float* __restrict__ gaussian
 // splat touches are written too (src/shaders/tiles.wgsl:24-35, fused); when
 // depth_keys is given, the depth's bits (0 when culled) and the splat's index,
 // the input of the depth sort.
+//
+// Persistent CTAs over blocks of PRE_THREADS Gaussians: while a CTA projects one
+// block, the next block's SH coefficients are already copying into the other
+// half of s_sh (cp.async) and its Gaussian records loading into registers, so
+// the loads of one block wait behind the arithmetic of the previous one instead
+// of in front of it.
 __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* __restrict__ camera,
                                                                  const float* __restrict__ gaussians,
                                                                  const float* __restrict__ sh, uint32_t count,
@@ -116,26 +128,53 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
                                                                  uint32_t* __restrict__ depth_keys,
                                                                  uint32_t* __restrict__ depth_order) {
   __shared__ Camera s_cam;
-  __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
+  __shared__ __align__(16) float s_sh[2][PRE_THREADS * SH_REST_FLOATS];
   load_camera(s_cam, camera);
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
-  const uint32_t block_start = blockIdx.x * PRE_THREADS;
-  const uint32_t i = block_start + threadIdx.x;
-  // The SH copy and this thread's Gaussian record load at the same time.
-  if (basis_count > 0)
-    stage_floats_async(s_sh, sh + (size_t)block_start * SH_REST_FLOATS,
-                       min((uint32_t)PRE_THREADS, count - block_start) * SH_REST_FLOATS);
+  const uint32_t blocks = (count + PRE_THREADS - 1) / PRE_THREADS;
+  const uint32_t mine = blockIdx.x < blocks ? (blocks - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  auto first_of = [&](uint32_t step) { return (blockIdx.x + step * gridDim.x) * PRE_THREADS; };
+  // Starts block `step`'s SH copy; threads past the end load the last record.
+  auto fetch = [&](uint32_t step, float (&g)[16]) {
+    const uint32_t first = first_of(step);
+    if (basis_count > 0)
+      stage_floats_async(s_sh[step & 1], sh + (size_t)first * SH_REST_FLOATS,
+                         min((uint32_t)PRE_THREADS, count - first) * SH_REST_FLOATS);
+    load_gaussian(gaussians, min(first + threadIdx.x, count - 1u), g);
+  };
   float g[16];
-  load_gaussian(gaussians, min(i, count - 1u), g);  // threads past the end load the last one and stop below
-  cp_async_wait_all();
-  __syncthreads();
-  if (i >= count) return;
-  const Projected pr = preprocess_one(s_cam, g, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count,
-                                      reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT));
-  if (tile_counts) tile_counts[i] = pr.tiles;
-  if (depth_keys) depth_keys[i] = pr.depth_bits;
-  if (depth_order) depth_order[i] = i;
+  if (mine > 0) fetch(0, g);
+  for (uint32_t step = 0; step < mine; step++) {
+    cp_async_wait_all();
+    __syncthreads();  // this block's SH is in; every thread is done with the block before last
+    float next[16];
+    if (step + 1 < mine) fetch(step + 1, next);
+    const uint32_t i = first_of(step) + threadIdx.x;
+    if (i < count) {
+      const Projected pr = preprocess_one(s_cam, g, s_sh[step & 1] + threadIdx.x * SH_REST_FLOATS, basis_count,
+                                          reinterpret_cast<float4*>(splats + (size_t)i * FLOATS_PER_SPLAT));
+      if (tile_counts) tile_counts[i] = pr.tiles;
+      if (depth_keys) depth_keys[i] = pr.depth_bits;
+      if (depth_order) depth_order[i] = i;
+    }
+    if (step + 1 < mine) {
+#pragma unroll
+      for (int k = 0; k < 16; k++) g[k] = next[k];
+    }
+  }
+}
+
+// CTAs of preprocess_kernel that fit on the device at once (its grid).
+uint32_t preprocess_grid(const dg_context* ctx, uint32_t count) {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, preprocess_kernel, PRE_THREADS, 0) != cudaSuccess) n = 1;
+    per_sm = std::max(1, n);
+  }
+  const uint32_t blocks = std::max(1u, ceil_div(count, PRE_THREADS));
+  return std::min(blocks, (uint32_t)per_sm * (uint32_t)ctx->sm_count);
 }
 
 // The same for a batch of views sharing one viewport: each CTA stages its
@@ -1125,7 +1164,7 @@ dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target) {
   dg_context* ctx = r->ctx;
   if (r->count > 0) {
     DG_LAUNCH(ctx, "preprocess",
-              preprocess_kernel<<<ceil_div(r->count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
+              preprocess_kernel<<<preprocess_grid(ctx, r->count), PRE_THREADS, 0, ctx->stream>>>(
                   typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                   typed<uint32_t>(r->scene_params), typed<float>(r->splats),
                   typed<uint32_t>(r->rasterizer->tile_offsets), typed<uint32_t>(r->rasterizer->depth_keys),

@@ -432,6 +432,8 @@ __device__ __forceinline__ void preprocess_backward_one(const Camera& cam, const
   sh_basis(dir, basis);
   const float* coef = shv;
   float raw_color[3] = {g[12], g[13], g[14]};
+  // Both SH loops are unrolled over all 15 terms (those past basis_count
+  // skipped), so basis and bgrad stay in registers.
   for (uint32_t k = 0; k < basis_count; k++)
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) raw_color[ch] = raw_color[ch] + basis[k] * coef[k * 3 + ch];
