@@ -432,8 +432,9 @@ __device__ __forceinline__ void preprocess_backward_one(const Camera& cam, const
   sh_basis(dir, basis);
   const float* coef = shv;
   float raw_color[3] = {g[12], g[13], g[14]};
-  // Both SH loops are unrolled over all 15 terms (those past basis_count
-  // skipped), so basis and bgrad stay in registers.
+  // These SH loops stay rolled: unrolled (basis and bgrad in registers) the
+  // fused backward + Adam kernel takes 112 registers, 4 CTAs per SM instead of
+  // 5, and runs slower (435 vs 408 us at 1.1M Gaussians).
   for (uint32_t k = 0; k < basis_count; k++)
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) raw_color[ch] = raw_color[ch] + basis[k] * coef[k * 3 + ch];
