@@ -160,13 +160,10 @@ __global__ void __launch_bounds__(SORT_THREADS, 3)
   const uint32_t n = count ? min(*count, capacity) : capacity;
   const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
   if (tid == 0) s_tile = atomicAdd(ticket, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  // A grid sized for the capacity has CTAs past the last tile of keys: they stop
-  // before any other work (tickets go out in order, so they are the last ones).
-  if (tile >= tiles) return;
   for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) s_whist[i] = 0;
   __syncthreads();
+  const uint32_t tile = s_tile;
+  if (tile >= tiles) return;
 
   // Load, warp-striped: warp w owns keys [w*480, w*480+480) of the tile, round j
   // reads 32 consecutive ones, so order within the tile is (warp, round, lane).
