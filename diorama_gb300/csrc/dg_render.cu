@@ -850,7 +850,6 @@ static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
   return ensure_plan(tr);
 }
 
-dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity) { return make_pairs(tr, capacity); }
 
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
                             uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out) {
@@ -1040,14 +1039,6 @@ dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const f
   DG_LAUNCH(ctx, "duplicate",
             duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, ctx->stream>>>(
                 camera, splats, order, offsets, count, per_view, view_shift, capacity, keys, values));
-  return DG_OK;
-}
-
-dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
-                             uint32_t tiles, uint2* ranges) {
-  DG_LAUNCH(ctx, "find_ranges",
-            find_ranges_kernel<1><<<stride_grid(ctx, capacity, RANGE_THREADS), RANGE_THREADS, 0, ctx->stream>>>(
-                tile_keys, pair_total, capacity, tiles, 0u, 1u, ranges));
   return DG_OK;
 }
 

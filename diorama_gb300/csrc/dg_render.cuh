@@ -65,7 +65,6 @@ dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr);
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
                             uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);
-dg_status rasterizer_grow(dg_tile_rasterizer* tr, uint32_t capacity);
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
 // Grid of a persistent blend kernel of `threads` threads per CTA over `items`
 // warp items.
@@ -98,9 +97,8 @@ dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
                                   const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t view_shift,
                                   uint32_t capacity, uint32_t* keys, uint32_t* values);
-dg_status find_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total, uint32_t capacity,
-                             uint32_t tiles, uint2* ranges);
-// The same for a batch of views whose pair keys are view << view_shift | local tile.
+// Per-tile ranges of the sorted pairs of a batch of views (dg_views.cu), whose
+// keys are view << view_shift | the view's tile index.
 dg_status find_view_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total,
                                   uint32_t capacity, uint32_t view_shift, uint32_t tiles_per_view, uint32_t tiles,
                                   uint2* ranges);
