@@ -234,11 +234,10 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
                                                                        uint32_t* __restrict__ keys,
                                                                        uint32_t* __restrict__ values) {
   __shared__ uint32_t s_excl[DUP_THREADS];
-  __shared__ uint32_t s_x0[DUP_THREADS];
-  __shared__ uint32_t s_y0[DUP_THREADS];
-  __shared__ uint32_t s_w[DUP_THREADS];
+  __shared__ uint32_t s_w[DUP_THREADS];       // the splat's tile rectangle's width
+  __shared__ float s_inv[DUP_THREADS];        // 1 / width
   __shared__ uint32_t s_index[DUP_THREADS];
-  __shared__ uint32_t s_base[DUP_THREADS];  // the splat's view, shifted into place
+  __shared__ uint32_t s_corner[DUP_THREADS];  // the key of its rectangle's first tile
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t j = blockIdx.x * DUP_THREADS + threadIdx.x;
   const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
@@ -265,11 +264,12 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   const uint32_t slot0 = offsets[first];
   uint32_t* excl = s_excl + warp * 32;
   excl[lane] = incl - n;
-  s_x0[threadIdx.x] = rect.x;
-  s_y0[threadIdx.x] = rect.y;
-  s_w[threadIdx.x] = rect.z - rect.x;
+  const uint32_t view = per_view >= count ? 0u : index / per_view;  // one view: no division
+  const uint32_t rw = rect.z - rect.x;
+  s_w[threadIdx.x] = rw;
+  s_inv[threadIdx.x] = rw ? 1.0f / (float)rw : 0.0f;
   s_index[threadIdx.x] = index;
-  s_base[threadIdx.x] = (index / per_view) << view_shift;
+  s_corner[threadIdx.x] = (view << view_shift) + rect.y * tiles.x + rect.x;
   __syncwarp();
   for (uint32_t k = lane; k < total; k += 32) {
     int lo = 0;
@@ -277,13 +277,23 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
     for (int step = 16; step > 0; step >>= 1)
       if (excl[lo + step] <= k) lo += step;
     const int src = warp * 32 + lo;
+    // The pair's row and column in the splat's rectangle: local / w and local % w
+    // by a float reciprocal, whose quotient (local < 2^22) is off by at most one,
+    // then corrected from the remainder; exact.
     const uint32_t local = k - excl[lo];
-    const uint32_t w = s_w[src];
-    const uint32_t y = s_y0[src] + local / w;
-    const uint32_t x = s_x0[src] + local % w;
+    const int32_t w = (int32_t)s_w[src];
+    int32_t q = (int32_t)((float)local * s_inv[src]);
+    int32_t r = (int32_t)local - q * w;
+    if (r < 0) {
+      q -= 1;
+      r += w;
+    } else if (r >= w) {
+      q += 1;
+      r -= w;
+    }
     const uint32_t slot = slot0 + k;
     if (slot < capacity) {
-      keys[slot] = s_base[src] + y * tiles.x + x;
+      keys[slot] = s_corner[src] + (uint32_t)q * tiles.x + (uint32_t)r;
       values[slot] = s_index[src];
     }
   }
