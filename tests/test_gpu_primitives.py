@@ -63,7 +63,7 @@ def test_prefix_sum_device_count(device):
     count.destroy()
 
 
-@pytest.mark.parametrize("size", [1, 1000, 1024, 100_003])
+@pytest.mark.parametrize("size", [1, 1000, 1024, 3840, 3841, 100_003])
 def test_radix_sort_32(device, size):
     keys = sort_keys(size)
     sort = RadixSort(device, size)
@@ -104,6 +104,43 @@ def test_radix_sort_device_count(device):
     order = stable_sort_reference(keys[:used])
     assert np.array_equal(sort.values.read(np.uint32)[:used], order)
     assert np.array_equal(sort.keys.read(np.uint32)[used:], keys[used:])
+    sort.destroy()
+    count.destroy()
+
+
+@pytest.mark.parametrize("pattern", ["equal", "descending", "top_byte_only"])
+def test_radix_sort_32_patterns(device, pattern):
+    """Stability and digit edge cases: every key equal (the identity order), keys
+    in descending order, and keys that differ only in their top byte (three
+    passes see a single digit)."""
+    size = 50_001
+    if pattern == "equal":
+        keys = np.full(size, 0xDEADBEEF, np.uint32)
+    elif pattern == "descending":
+        keys = np.arange(size, 0, -1, dtype=np.uint32) * np.uint32(977)
+    else:
+        keys = (np.random.default_rng(5).integers(0, 256, size, dtype=np.uint32) << np.uint32(24)) | np.uint32(0x123456)
+    sort = RadixSort(device, size)
+    sort.keys.write(keys)
+    sort.values.write(np.arange(size, dtype=np.uint32))
+    sort.encode()
+    order = stable_sort_reference(keys)
+    assert np.array_equal(sort.values.read(np.uint32), order)
+    assert np.array_equal(sort.keys.read(np.uint32), keys[order])
+    sort.destroy()
+
+
+def test_radix_sort_device_count_zero(device):
+    """A device-side count of 0 sorts nothing: keys and values stay as written."""
+    size = 10_000
+    keys = sort_keys(size)
+    count = device.upload(np.array([0], np.uint32))
+    sort = RadixSort(device, size, count=count)
+    sort.keys.write(keys)
+    sort.values.write(np.arange(size, dtype=np.uint32))
+    sort.encode()
+    assert np.array_equal(sort.keys.read(np.uint32), keys)
+    assert np.array_equal(sort.values.read(np.uint32), np.arange(size, dtype=np.uint32))
     sort.destroy()
     count.destroy()
 
