@@ -91,6 +91,37 @@ def test_small_views_match_single_view_renders(device, small_scene, batch):
     assert device.check() == 0
 
 
+def test_300_views_in_one_batch(device):
+    """More views than one byte numbers: the (view, depth) sort takes two passes
+    over the view's bits and the pair keys carry views up to 299 above the local
+    tile; every image still equals its own render."""
+    raw, sh = scenes.surface_scene(50_000, 22, noise=0.01)
+    train, held = scenes.ring_cameras(width=200, height=150)
+    cams = train + held
+    assert len(cams) == 300
+    r = GaussianRenderer(device)
+    r.setGaussians(activate(raw), {"rest": sh.reshape(-1), "degree": 3})
+    W, H = cams[0].viewport
+    tex = device.createTexture(W, H)
+    singles = []
+    for cam in cams:
+        for _ in range(2):  # the first frame may grow the pair buffers
+            r.encode(None, tex, cam, BG)
+            r.afterSubmit()
+        singles.append(r.pixelBuffer.read(np.float32)[: W * H * 4].copy())
+    tex.destroy()
+    r.setViewBatching(0, 0, True)
+    pixel_colors = device.createBuffer(len(cams) * W * H * 16)
+    for _ in range(2):  # the second call replays the captured batch
+        r.renderViews(cams, BG, None, pixel_colors)
+        got = pixel_colors.read(np.float32).reshape(len(cams), -1)
+        for k in range(len(cams)):
+            assert np.array_equal(got[k].view(np.uint32), singles[k].view(np.uint32)), k
+    pixel_colors.destroy()
+    assert device.check() == 0
+    r.destroy()
+
+
 def test_autotuned_views_match(device, scene):
     r, cams, colors, lasts, images = scene
     tuned = r.tuneViews(cams, BG)
