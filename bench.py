@@ -17,8 +17,9 @@ needed between steps.
 the reference itself is TypeScript + WGSL that only runs in a browser's
 WebGPU, so its CPU implementation here is the oracle (oracle/oracle.c, a C
 restatement of its WGSL, OpenMP over all host threads), on the same workload.
-For N > 1 the path has no exchange step (training does not shard; see
-the design doc): each rank trains its own replica and the value is the sum.
+For N > 1 the path has no exchange step (a training step renders one view
+against one global parameter set, so it does not shard): each rank trains its
+own replica and the value is the sum.
 """
 
 from __future__ import annotations
@@ -816,9 +817,37 @@ def run_densify_experiment(args, rank, local):
     }
 
 
+def free_port() -> int:
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def launch_replicas(n: int, argv: list[str], script: str | None = None) -> int:
+    """`bench.py --gpus N` started directly (not under torchrun): start N replica
+    processes, one per GPU, with the environment torchrun would give them (RANK,
+    LOCAL_RANK, WORLD_SIZE, MASTER_ADDR 127.0.0.1, MASTER_PORT). Rank 0's output
+    passes through; the others' is dropped. Returns the first nonzero exit code."""
+    port = free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, script or str(Path(__file__).resolve()), *argv], env=env,
+                                      stdout=None if r == 0 else subprocess.DEVNULL))
+    codes = [p.wait() for p in procs]
+    return next((c for c in codes if c != 0), 0)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_replicas(args.gpus, sys.argv[1:]))
     rank, world, local, group = dist_setup(args)
+    if world != args.gpus and rank == 0:
+        print(f"note: --gpus {args.gpus} but {world} process(es) were launched; measuring {world}", file=sys.stderr)
     if args.workload == "sort":
         result = run_sort_stress(args, rank, local) if args.impl == "ours" else None
     elif args.workload == "densify":

@@ -105,6 +105,9 @@ SIGNATURES = {
     "dg_prefix_sum_encode": (None, [_P]),
     "dg_prefix_sum_total": (_P, [_P]),
     "dg_prefix_sum_destroy": (None, [_P]),
+    "dg_prefix_sum_no_alloc": (None, [c_void_p, c_void_p, c_uint32, c_void_p]),
+    "dg_prefix_sum_no_alloc_check": (None, [c_void_p, POINTER(c_uint32)]),
+    "dg_prefix_sum_no_alloc_inject_error": (None, [c_void_p, c_uint32]),
     "dg_radix_sort_create": (None, [_P, c_uint32, c_uint32, _P, POINTER(_P)]),
     "dg_radix_sort_keys": (_P, [_P]),
     "dg_radix_sort_values": (_P, [_P]),
@@ -202,6 +205,7 @@ SIGNATURES = {
     "dg_densify_mlp_train": (None, [_P, c_void_p, c_void_p, c_uint32, c_uint32, c_uint32, c_float, c_float, c_int32,
                                     c_uint32, POINTER(c_double)]),
     "dg_densify_mlp_predict": (None, [_P, _P, c_uint32, _P]),
+    "dg_densify_mlp_gradient": (None, [_P, c_void_p, c_void_p, c_uint32, c_void_p]),
     "dg_densify_mlp_get_weights": (None, [_P, c_void_p]),
     "dg_densify_mlp_set_weights": (None, [_P, c_void_p]),
     "dg_densify_mlp_destroy": (None, [_P]),

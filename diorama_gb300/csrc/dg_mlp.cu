@@ -615,6 +615,39 @@ dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const u
   return st;
 }
 
+// The gradient of the mean cross-entropy over count samples (host arrays) at the
+// current weights and normalization, in the master layout; nothing is updated.
+dg_status dg_densify_mlp_gradient(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
+                                  float* gradient) {
+  DG_REQUIRE(m && features && labels && gradient, "NULL argument");
+  DG_REQUIRE(count > 0, "no samples");
+  dg_context* ctx = m->ctx;
+  dg_buffer *f = nullptr, *l = nullptr, *order = nullptr;
+  DG_TRY(alloc_buffer(ctx, (size_t)count * IN * 4, &f));
+  dg_status st = alloc_buffer(ctx, count, &l);
+  if (st == DG_OK) st = alloc_buffer(ctx, (size_t)count * 4, &order);
+  if (st == DG_OK) {
+    std::vector<uint32_t> identity(count);
+    std::iota(identity.begin(), identity.end(), 0u);
+    DG_CUDA(cudaMemcpyAsync(f->ptr, features, (size_t)count * IN * 4, cudaMemcpyHostToDevice, ctx->stream));
+    DG_CUDA(cudaMemcpyAsync(l->ptr, labels, count, cudaMemcpyHostToDevice, ctx->stream));
+    DG_CUDA(cudaMemcpyAsync(order->ptr, identity.data(), (size_t)count * 4, cudaMemcpyHostToDevice, ctx->stream));
+    DG_CUDA(cudaMemsetAsync(m->grads->ptr, 0, PARAMS * 4, ctx->stream));
+    DG_LAUNCH(ctx, "mlp_train",
+              mlp_train_kernel<<<ceil_div(count, ROWS), MLP_THREADS, 0, ctx->stream>>>(
+                  typed<float>(f), typed<uint8_t>(l), typed<uint32_t>(order), 0, count, make_float2(1.0f, 1.0f),
+                  typed<float>(m->norm), typed<__nv_bfloat16>(m->packed), typed<float>(m->master),
+                  typed<float>(m->grads), typed<float>(m->loss)));
+    DG_CUDA(cudaMemcpyAsync(gradient, m->grads->ptr, PARAMS * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    DG_CUDA(cudaMemsetAsync(m->grads->ptr, 0, PARAMS * 4, ctx->stream));
+    DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  free_buffer(f);
+  free_buffer(l);
+  free_buffer(order);
+  return st;
+}
+
 // survive[i] = P(the children of candidate i survive), features[count][12] and
 // survive[count] on the device.
 dg_status dg_densify_mlp_predict(dg_densify_mlp* m, dg_buffer* features, uint32_t count, dg_buffer* survive) {

@@ -13,7 +13,6 @@
 #include "dg_scan.cuh"
 
 #include <cuda/atomic>
-#include <mutex>
 #include <string>
 
 namespace dg {
@@ -192,24 +191,22 @@ constexpr size_t NO_ALLOC_BYTES = 256 + (size_t)NO_ALLOC_MAX_TILES * 8;      // 
 static __device__ __align__(256) unsigned char g_no_alloc_scratch[NO_ALLOC_BYTES];
 
 // Host code must not use g_no_alloc_scratch's name as an address: on the host it
-// is only a stand-in for the symbol. The device address is looked up once per
-// device, with that device current, and kept here.
-constexpr int NO_ALLOC_MAX_DEVICES = 64;
-static void* g_no_alloc_address[NO_ALLOC_MAX_DEVICES] = {};
-static std::mutex g_no_alloc_lock;
+// is only a stand-in for the symbol. Each call looks up the device address on
+// the current device, which must be the stream's. The lookup is cheap once the
+// library's module is loaded on that device (the first call there loads it);
+// a fresh lookup on every call stays right after cudaDeviceReset or under another
+// context, where a cached address would point at freed memory.
+constexpr uint32_t NO_ALLOC_ERROR_OFFSET = 4;  // the give-up word, after the ticket
 
-static dg_status no_alloc_scratch_address(void** out) {
-  int device = -1;
+static dg_status no_alloc_scratch_address(cudaStream_t stream, void** out) {
+  int device = -1, stream_device = -1;
   DG_CUDA(cudaGetDevice(&device));
-  DG_REQUIRE(device >= 0 && device < NO_ALLOC_MAX_DEVICES, "device index out of range for the no-alloc scan");
-  std::lock_guard<std::mutex> hold(g_no_alloc_lock);
-  if (!g_no_alloc_address[device]) {
-    void* ptr = nullptr;
-    cudaError_t err = cudaGetSymbolAddress(&ptr, g_no_alloc_scratch);
-    if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(no-alloc scan scratch)");
-    g_no_alloc_address[device] = ptr;
-  }
-  *out = g_no_alloc_address[device];
+  DG_CUDA(cudaStreamGetDevice(stream, &stream_device));
+  DG_REQUIRE(stream_device == device, "the stream belongs to another device than the current one");
+  void* ptr = nullptr;
+  cudaError_t err = cudaGetSymbolAddress(&ptr, g_no_alloc_scratch);
+  if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(no-alloc scan scratch)");
+  *out = ptr;
   return DG_OK;
 }
 
@@ -223,20 +220,58 @@ extern "C" dg_status dg_prefix_sum_no_alloc(void* stream, uint32_t* data, uint32
     return fail(DG_ERROR_INVALID_ARGUMENT, "dg_prefix_sum_no_alloc scans at most " +
                                                std::to_string(NO_ALLOC_MAX_VALUES) + " values; got " +
                                                std::to_string(count));
-  void* scratch = nullptr;
-  DG_TRY(no_alloc_scratch_address(&scratch));
   auto s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  DG_TRY(no_alloc_scratch_address(s, &scratch));
   const uint32_t tiles = std::max(1u, ceil_div(count, SCAN_TILE));
   auto* ticket = static_cast<uint32_t*>(scratch);
-  auto* error = ticket + 1;
+  auto* error = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + NO_ALLOC_ERROR_OFFSET);
   auto* status = reinterpret_cast<uint64_t*>(static_cast<char*>(scratch) + 256);
   // The previous call left its ticket and status words behind: clear what this
-  // call's tiles will read (the error word keeps any earlier give-up).
+  // call's tiles will read. The give-up word is left alone: it keeps any earlier
+  // give-up until dg_prefix_sum_no_alloc_check reads and clears it.
   DG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(uint32_t), s));
   DG_CUDA(cudaMemsetAsync(status, 0, (size_t)tiles * sizeof(uint64_t), s));
   scan_kernel<<<tiles, SCAN_THREADS, 0, s>>>(data, count, nullptr, total, status, ticket, error, nullptr,
                                                           nullptr);
   DG_CUDA(cudaGetLastError());
+  return DG_OK;
+}
+
+// Waits for the stream, then reads and clears the give-up word that the scan's
+// bounded look-back sets instead of hanging.
+extern "C" dg_status dg_prefix_sum_no_alloc_check(void* stream, uint32_t* bits) {
+  auto s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  DG_TRY(no_alloc_scratch_address(s, &scratch));
+  auto* error = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + NO_ALLOC_ERROR_OFFSET);
+  uint32_t value = 0;
+  DG_CUDA(cudaMemcpyAsync(&value, error, sizeof(value), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  if (bits) *bits = value;
+  if (value) {
+    DG_CUDA(cudaMemsetAsync(error, 0, sizeof(uint32_t), s));
+    DG_CUDA(cudaStreamSynchronize(s));
+    return fail(DG_ERROR_DEVICE_WAIT,
+                "a look-back of dg_prefix_sum_no_alloc gave up waiting; the results since the last check are wrong "
+                "(error bits " + std::to_string(value) + ")");
+  }
+  return DG_OK;
+}
+
+// Test hook: ORs bits into the give-up word, as a timed-out look-back would, so
+// that the reporting path can be tested without making a GPU wait run out.
+extern "C" dg_status dg_prefix_sum_no_alloc_inject_error(void* stream, uint32_t bits) {
+  auto s = static_cast<cudaStream_t>(stream);
+  void* scratch = nullptr;
+  DG_TRY(no_alloc_scratch_address(s, &scratch));
+  auto* error = reinterpret_cast<uint32_t*>(static_cast<char*>(scratch) + NO_ALLOC_ERROR_OFFSET);
+  uint32_t value = 0;
+  DG_CUDA(cudaMemcpyAsync(&value, error, sizeof(value), cudaMemcpyDeviceToHost, s));
+  DG_CUDA(cudaStreamSynchronize(s));
+  value |= bits;
+  DG_CUDA(cudaMemcpyAsync(error, &value, sizeof(value), cudaMemcpyHostToDevice, s));
+  DG_CUDA(cudaStreamSynchronize(s));
   return DG_OK;
 }
 

@@ -165,6 +165,16 @@ class DensifyMLP:
                   weightDecay, int(balanceClasses), seed, losses)
         return list(losses)
 
+    def gradient(self, features: np.ndarray, labels: np.ndarray) -> np.ndarray:
+        """The gradient of the mean cross-entropy over these samples at the current
+        weights (MLP_PARAMS floats, the layout of weights()); nothing is updated."""
+        f = np.ascontiguousarray(features, np.float32).reshape(-1, MLP_FEATURES)
+        y = np.ascontiguousarray(labels, np.uint8).reshape(-1)
+        assert f.shape[0] == y.size
+        out = np.zeros(MLP_PARAMS, np.float32)
+        _lib.call("dg_densify_mlp_gradient", self.handle, f.ctypes.data, y.ctypes.data, y.size, out.ctypes.data)
+        return out
+
     def predict(self, features: Buffer, count: int, survive: Buffer) -> None:
         """survive[i] = P(candidate i's children survive), both device buffers."""
         _lib.call("dg_densify_mlp_predict", self.handle, features.handle, count, survive.handle)

@@ -116,12 +116,25 @@ dg_status dg_prefix_sum_destroy(dg_prefix_sum* scan);
  * scan's look-back state lives in a ~32 KB array inside the library that every
  * GPU loading the library holds until exit. data (count u32 values, scanned in
  * place) and total (one u32) are device pointers the caller owns; stream is a
- * cudaStream_t (NULL for the legacy default stream) on the current device.
+ * cudaStream_t (NULL for the legacy default stream) that must belong to the
+ * current device (DG_ERROR_INVALID_ARGUMENT otherwise).
  * At most 16,777,216 values; larger counts return DG_ERROR_INVALID_ARGUMENT.
- * The first call on each device looks up the array's device address, so make
- * that first call before any stream capture. All calls share the one array, so
- * calls whose work overlaps on the GPU (other streams, other threads) race. */
+ * Each call looks up the array's device address on the current device; the
+ * first call on a device also loads the library's GPU code there, so make that
+ * first call before any stream capture. All calls share the one array, so calls
+ * whose work overlaps on the GPU (other streams, other threads) race.
+ * A look-back that waits too long gives up instead of hanging; the scan's
+ * output is then wrong and a give-up word in the array is set, which
+ * dg_prefix_sum_no_alloc_check reports. */
 dg_status dg_prefix_sum_no_alloc(void* stream, uint32_t* data, uint32_t count, uint32_t* total);
+/* Waits for stream, then reads and clears the give-up word of dg_prefix_sum_no_alloc
+ * on the current device: DG_ERROR_DEVICE_WAIT (bits in *bits, which may be NULL)
+ * if a scan since the last check gave up, so its results are wrong; DG_OK
+ * otherwise. Allocates nothing. No counterpart in the reference. */
+dg_status dg_prefix_sum_no_alloc_check(void* stream, uint32_t* bits);
+/* Test hook: sets bits in that give-up word, as a look-back that gave up would,
+ * so the reporting path can be tested without making a GPU wait run out. */
+dg_status dg_prefix_sum_no_alloc_inject_error(void* stream, uint32_t bits);
 
 /* ---- RadixSort (src/radixSort.ts:27-142): stable LSD sort of u32 keys (high_bits = 0)
  * or u64 keys stored as (low word, high word) sorting high_bits bits of the high word,
@@ -350,6 +363,11 @@ dg_status dg_densify_mlp_create(dg_context* ctx, uint32_t seed, dg_densify_mlp**
 dg_status dg_densify_mlp_train(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
                                uint32_t epochs, uint32_t batch, float lr, float weight_decay, int32_t balance_classes,
                                uint32_t seed, double* mean_loss);
+/* The gradient of the mean cross-entropy over count labelled samples (host
+ * arrays, as for training) at the current weights and normalization, in the
+ * DG_MLP_PARAMS layout of dg_densify_mlp_get_weights; the model is not changed. */
+dg_status dg_densify_mlp_gradient(dg_densify_mlp* m, const float* features, const uint8_t* labels, uint32_t count,
+                                  float* gradient);
 /* survive[i] = P(the children of candidate i survive); device buffers holding
  * features [count][12] and survive [count]. */
 dg_status dg_densify_mlp_predict(dg_densify_mlp* m, dg_buffer* features, uint32_t count, dg_buffer* survive);

@@ -1,7 +1,9 @@
 """Regenerates the golden vectors in tests/golden from the reference's own PyTorch
 oracles. Run here, where the reference is mounted (it is not on GPU machines):
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <the reference checkout>
+
+(or set DIORAMA_REFERENCE to the checkout instead of passing --reference).
 
 1. backward.json and loss.json: reference/backward_reference.py and
    reference/loss_reference.py are imported and their main() re-run (writing to
@@ -21,6 +23,7 @@ from __future__ import annotations
 import argparse
 import importlib.util
 import json
+import os
 import sys
 import tempfile
 import time
@@ -146,9 +149,12 @@ def make_random_16k(lr) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("DIORAMA_REFERENCE"),
+                    help="the reference project's checkout (default: $DIORAMA_REFERENCE)")
     ap.add_argument("--skip-random-16k", action="store_true")
     args = ap.parse_args()
+    if not args.reference:
+        ap.error("give the reference checkout with --reference or DIORAMA_REFERENCE")
     ref = Path(args.reference)
     fixtures = ref / "src" / "checks" / "fixtures"
     br = load_module(ref / "reference" / "backward_reference.py", "backward_reference")

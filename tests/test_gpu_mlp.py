@@ -3,8 +3,9 @@ reference densifies by its gradient threshold alone, src/shaders/densify.wgsl,
 which stays the fallback).
 
 The model's tensor-core kernels against a NumPy restatement of the same BF16
-arithmetic (inference within 1e-3; one AdamW step moves every weight with a
-clear gradient against that gradient's sign), training on a separable rule, and
+arithmetic (inference within 1e-3; the training kernel's weight and bias
+gradient values tensor by tensor; one AdamW step moves every weight with a
+clear gradient by lr against that gradient's sign), training on a separable rule, and
 the trainer: a model that is never confident reproduces the plain rule exactly,
 one that vetoes everything stops every clone and split, and the log labels
 every clone/split candidate."""
@@ -85,7 +86,55 @@ def test_predict_matches_bf16_restatement(device):
     mlp.destroy()
 
 
+def restated_gradient(p, features, labels):
+    """The mean cross-entropy's gradient in float64, rounding to BF16 where the
+    kernel does: the normalized inputs, the weights, the activations, and the
+    deltas that enter tensor-core products (dZ3 into dA2, dZ2 into dA1, and all
+    three in the weight gradients); bias gradients sum the unrounded deltas."""
+    b = lambda v: bf16(np.asarray(v, np.float32)).astype(np.float64)  # noqa: E731
+    x, z1, a1, z2, a2, z3 = forward(p, features)
+    prob = np.exp(z3 - z3.max(1, keepdims=True))
+    prob /= prob.sum(1, keepdims=True)
+    d3 = (prob - np.eye(2)[labels]) / len(labels)
+    d2 = (b(d3) @ b(p["W3"]).T) * gelu_grad(z2)
+    d1 = (b(d2) @ b(p["W2"]).T) * gelu_grad(z1)
+    return np.concatenate([(x.T @ b(d1)).ravel(), d1.sum(0), (a1.T @ b(d2)).ravel(), d2.sum(0),
+                           (a2.T @ b(d3)).ravel(), d3.sum(0)])
+
+
+def test_weight_gradients_match_float64_restatement(device):
+    """The training kernel's gradient values (not only their signs) against the
+    float64 restatement, tensor by tensor: the largest error within 1% of the
+    tensor's largest gradient, and the element-wise relative error over the
+    gradients above 5% of it small (BF16 operands, FP32 accumulation)."""
+    rng = np.random.default_rng(4)
+    mlp = DensifyMLP(device, seed=2)
+    w = random_weights(rng, 0.2)
+    mlp.setWeights(w)
+    features = rng.normal(0, 1.0, (1000, MLP_FEATURES)).astype(np.float32)
+    labels = (rng.random(1000) < 0.4).astype(np.uint8)
+    got = mlp.gradient(features, labels).astype(np.float64)
+    assert np.array_equal(mlp.weights(), w)  # nothing updated
+    want = restated_gradient(unpack(w), features, labels)
+    sizes = [("W1", 12 * 64), ("b1", 64), ("W2", 64 * 64), ("b2", 64), ("W3", 128), ("b3", 2)]
+    o = 0
+    report = {}
+    for name, size in sizes:
+        g, r = got[o:o + size], want[o:o + size]
+        o += size
+        scale = np.abs(r).max()
+        big = np.abs(r) > 0.05 * scale
+        rel = np.abs(g[big] - r[big]) / np.abs(r[big])
+        report[name] = (float(np.abs(g - r).max() / scale), float(np.median(rel)), float(rel.max()))
+        assert report[name][0] <= 1e-2 and report[name][1] <= 2e-3 and report[name][2] <= 5e-2, report
+    # The same gradient once more: the kernel clears its accumulators.
+    assert np.allclose(mlp.gradient(features, labels), got, rtol=1e-5, atol=1e-7 * np.abs(got).max())
+    mlp.destroy()
+
+
 def test_one_adamw_step_follows_the_gradient(device):
+    """Adam's first step moves each weight by lr against its gradient's sign
+    (m / (1 - beta1) = g, v / (1 - beta2) = g^2)."""
     rng = np.random.default_rng(4)
     mlp = DensifyMLP(device, seed=2)
     w = random_weights(rng, 0.2)
@@ -100,19 +149,12 @@ def test_one_adamw_step_follows_the_gradient(device):
     var = ((features.astype(np.float64) - mean) ** 2).mean(0)
     p["mean"] = mean.astype(np.float32).astype(np.float64)
     p["inv_std"] = (1 / np.sqrt(var + 1e-12)).astype(np.float32).astype(np.float64)
-    x, z1, a1, z2, a2, z3 = forward(p, features)
-    prob = np.exp(z3 - z3.max(1, keepdims=True))
-    prob /= prob.sum(1, keepdims=True)
-    d3 = prob - np.eye(2)[labels]
-    d3 /= len(labels)
-    d2 = (d3 @ p["W3"].T) * gelu_grad(z2)
-    d1 = (d2 @ p["W2"].T) * gelu_grad(z1)
-    grads = np.concatenate([(x[:, :12].T @ d1).ravel(), d1.sum(0), (a1.T @ d2).ravel(), d2.sum(0),
-                            (a2.T @ d3).ravel(), d3.sum(0)])
+    grads = restated_gradient(p, features, labels)
     step = after[:MLP_PARAMS].astype(np.float64) - w[:MLP_PARAMS]
     clear = np.abs(grads) > 0.05 * np.abs(grads).max()
     agree = np.mean(np.sign(step[clear]) == -np.sign(grads[clear]))
     assert clear.sum() > 200 and agree >= 0.98, (clear.sum(), agree)
+    assert np.allclose(np.abs(step[clear]), 1e-4, rtol=1e-2), np.abs(step[clear]).max()
     mlp.destroy()
 
 

@@ -3,10 +3,14 @@
 Some callers cannot allocate device memory (a fixed memory budget, no implicit
 synchronization allowed, or a host that owns every allocation). This entry point
 serves them: it keeps its scratch in an array inside the library. Here it is
-called through the C ABI with memory and a stream the test owns, twice in a row
-with different inputs, and its output must equal the existing PrefixSum's
-(dg_prefix_sum_*) exactly, as every integer result in these tests must. This
-file is named to be collected last.
+called through the C ABI with device memory the test owns (dg_buffer_create) on
+the legacy default stream. Its output must equal the sequential exclusive scan
+(numpy's cumsum) and the existing PrefixSum's (dg_prefix_sum_*) exactly, as every
+integer result in these tests must: two calls in a row, an empty scan, the
+largest scan it accepts, and a large call followed by a small one (leftover
+look-back words of the large call must not be read). Its give-up word is
+reported by dg_prefix_sum_no_alloc_check. This file is named to be collected
+last.
 """
 
 from __future__ import annotations
@@ -21,13 +25,16 @@ from diorama_gb300 import DioramaError, PrefixSum, _lib
 pytestmark = pytest.mark.gpu
 
 MAX_VALUES = 1 << 24
+DEFAULT_STREAM = None  # the legacy default stream of the current device
 
 
-def no_alloc():
-    fn = _lib.load().dg_prefix_sum_no_alloc
-    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
-    fn.restype = ctypes.c_int32
-    return fn
+def exclusive_scan(values: np.ndarray) -> tuple[np.ndarray, int]:
+    """The sequential scan, in u32 arithmetic (wrapping like the GPU's)."""
+    inclusive = np.cumsum(values, dtype=np.uint64)
+    out = np.zeros(values.size, np.uint64)
+    out[1:] = inclusive[:-1]
+    total = int(inclusive[-1]) if values.size else 0
+    return (out & 0xFFFFFFFF).astype(np.uint32), total & 0xFFFFFFFF
 
 
 def existing_scan(device, values: np.ndarray):
@@ -41,31 +48,74 @@ def existing_scan(device, values: np.ndarray):
     return out, total
 
 
+def no_alloc_scan(device, values: np.ndarray):
+    """Scans `values` with the no-alloc entry point in memory the test owns."""
+    data = device.createBuffer(max(16, values.size * 4))
+    if values.size:
+        data.write(values)
+    total = device.createBuffer(16)
+    total.write(np.array([0xDEADBEEF], np.uint32))
+    device.synchronize()  # the context's stream has written the inputs
+    status = _lib.fn("dg_prefix_sum_no_alloc")(DEFAULT_STREAM, data.device_pointer, values.size,
+                                                total.device_pointer)
+    assert status == _lib.DG_OK, _lib.fn("dg_last_error")()
+    bits = ctypes.c_uint32(0xFFFF)
+    status = _lib.fn("dg_prefix_sum_no_alloc_check")(DEFAULT_STREAM, ctypes.byref(bits))  # waits for the scan
+    assert status == _lib.DG_OK and bits.value == 0, _lib.fn("dg_last_error")()
+    out = data.read(np.uint32)[: values.size].copy()
+    got_total = int(total.read(np.uint32)[0])
+    data.destroy()
+    total.destroy()
+    return out, got_total
+
+
+def check(device, values: np.ndarray) -> None:
+    got, got_total = no_alloc_scan(device, values)
+    want, want_total = exclusive_scan(values)
+    assert np.array_equal(got, want)
+    assert got_total == want_total
+    if values.size:
+        prefix_sum, prefix_total = existing_scan(device, values)
+        assert np.array_equal(got, prefix_sum)
+        assert got_total == prefix_total
+
+
 def test_no_alloc_scan_matches_prefix_sum_twice(device):
-    torch = pytest.importorskip("torch")
-    fn = no_alloc()
-    stream = torch.cuda.Stream()
     rng = np.random.default_rng(11)
     for size in (300_001, 4_096 * 37 + 5):  # two calls in a row, different sizes and contents
-        values = rng.integers(0, 1 << 16, size, dtype=np.uint32)
-        data = torch.from_numpy(values.view(np.int32)).cuda()
-        total = torch.zeros(1, dtype=torch.int32, device="cuda")
-        torch.cuda.synchronize()
-        status = fn(ctypes.c_void_p(stream.cuda_stream), data.data_ptr(), size, total.data_ptr())
-        assert status == _lib.DG_OK, _lib.load().dg_last_error()
-        stream.synchronize()
-        got = data.cpu().numpy().view(np.uint32)
-        want, want_total = existing_scan(device, values)
-        assert np.array_equal(got, want)
-        assert int(total.cpu().numpy().view(np.uint32)[0]) == want_total
+        check(device, rng.integers(0, 1 << 16, size, dtype=np.uint32))
+
+
+def test_no_alloc_scan_empty_largest_then_small(device):
+    rng = np.random.default_rng(12)
+    check(device, np.zeros(0, np.uint32))
+    # Every one of the array's 4,096 look-back tiles, with sums that wrap past 2^32.
+    check(device, rng.integers(0, 1 << 12, MAX_VALUES, dtype=np.uint32))
+    check(device, rng.integers(0, 1 << 30, 9_000, dtype=np.uint32))
+    check(device, rng.integers(0, 5, 1, dtype=np.uint32))
+
+
+def test_no_alloc_scan_reports_a_give_up(device):
+    # A look-back that gives up sets the give-up word; the check reports it once.
+    lib = _lib.load()
+    assert lib.dg_prefix_sum_no_alloc_inject_error(DEFAULT_STREAM, 1) == _lib.DG_OK
+    bits = ctypes.c_uint32(0)
+    assert lib.dg_prefix_sum_no_alloc_check(DEFAULT_STREAM, ctypes.byref(bits)) == _lib.DG_ERROR_DEVICE_WAIT
+    assert bits.value == 1
+    assert b"gave up" in lib.dg_last_error()
+    assert lib.dg_prefix_sum_no_alloc_check(DEFAULT_STREAM, ctypes.byref(bits)) == _lib.DG_OK
+    assert bits.value == 0
+    # A scan after the report is correct and reports nothing.
+    check(device, np.arange(5_000, dtype=np.uint32))
 
 
 def test_no_alloc_scan_rejects_sizes_past_its_maximum(device):
-    fn = no_alloc()
+    lib = _lib.load()
     dummy = device.createBuffer(16)
-    status = fn(None, dummy.device_pointer, MAX_VALUES + 1, dummy.device_pointer)
+    status = lib.dg_prefix_sum_no_alloc(None, dummy.device_pointer, MAX_VALUES + 1, dummy.device_pointer)
     assert status == _lib.DG_ERROR_INVALID_ARGUMENT
-    assert b"at most 16777216" in _lib.load().dg_last_error()
+    assert b"at most 16777216" in lib.dg_last_error()
+    assert lib.dg_prefix_sum_no_alloc(None, None, 4, dummy.device_pointer) == _lib.DG_ERROR_INVALID_ARGUMENT
     dummy.destroy()
     with pytest.raises(DioramaError):
         _lib.call("dg_prefix_sum_encode", None)
