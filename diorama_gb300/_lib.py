@@ -175,6 +175,7 @@ SIGNATURES = {
     "dg_trainer_iteration": (c_uint32, [_P]),
     "dg_trainer_set_iteration": (None, [_P, c_uint32]),
     "dg_trainer_sh_degree": (c_uint32, [_P]),
+    "dg_trainer_adam_steps": (c_uint32, [_P]),
     "dg_trainer_count": (c_uint32, [_P]),
     "dg_trainer_renderer": (_P, [_P]),
     "dg_trainer_params": (_P, [_P]),

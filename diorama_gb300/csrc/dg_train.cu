@@ -1130,6 +1130,7 @@ dg_status dg_trainer_set_iteration(dg_trainer* t, uint32_t iteration) {
   return DG_OK;
 }
 uint32_t dg_trainer_sh_degree(const dg_trainer* t) { return t ? t->sh_degree : 0; }
+uint32_t dg_trainer_adam_steps(const dg_trainer* t) { return t ? t->adam_steps : 0; }
 uint32_t dg_trainer_count(const dg_trainer* t) { return t ? t->count : 0; }
 dg_renderer* dg_trainer_renderer(dg_trainer* t) { return t ? t->renderer : nullptr; }
 dg_buffer* dg_trainer_params(dg_trainer* t) { return t ? t->params : nullptr; }

@@ -245,6 +245,11 @@ class Trainer:
         return int(_lib.fn("dg_trainer_sh_degree")(self.handle))
 
     @property
+    def adamSteps(self) -> int:
+        """The steps that ran Adam (private in the reference; for checks)."""
+        return int(_lib.fn("dg_trainer_adam_steps")(self.handle))
+
+    @property
     def count(self) -> int:
         return int(_lib.fn("dg_trainer_count")(self.handle))
 

@@ -311,6 +311,9 @@ dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint
 uint32_t dg_trainer_iteration(const dg_trainer* t);
 dg_status dg_trainer_set_iteration(dg_trainer* t, uint32_t iteration);
 uint32_t dg_trainer_sh_degree(const dg_trainer* t);
+/* The steps that ran Adam so far, which its bias correction counts (densification
+ * steps do not; src/trainer.ts:209,217-218, private there; exposed for checks). */
+uint32_t dg_trainer_adam_steps(const dg_trainer* t);
 uint32_t dg_trainer_count(const dg_trainer* t);
 dg_renderer* dg_trainer_renderer(dg_trainer* t);
 dg_buffer* dg_trainer_params(dg_trainer* t);

@@ -16,6 +16,7 @@ from __future__ import annotations
 import math
 
 import torch
+import torch.nn.functional as F
 
 TILE = 16
 NEAR_CULL = 0.2
@@ -133,3 +134,27 @@ def render(params, view, proj, background, width, height, sh_degree):
     values = torch.cat(pieces)
     image = image.index_put((order_all,), values)
     return image
+
+
+def ssim_window(size: int = 11, sigma: float = 1.5):
+    """The normalized 11x11 Gaussian window, one per channel
+    (reference/loss_reference.py:26-29)."""
+    g = torch.tensor([math.exp(-((x - size // 2) ** 2) / (2 * sigma**2)) for x in range(size)], dtype=torch.float64)
+    g = g / g.sum()
+    return (g[:, None] @ g[None, :]).expand(3, 1, size, size).contiguous()
+
+
+def loss(render, target, lam: float = 0.2):
+    """0.8 x L1 + 0.2 x (1 - SSIM) of two (3, H, W) float64 images, SSIM with
+    zero padding and C1 = 0.01^2, C2 = 0.03^2, averaged over every pixel and
+    channel (reference/loss_reference.py:32-50)."""
+    w = ssim_window()
+    a, b = render[None], target[None]
+    blur = lambda image: F.conv2d(image, w, padding=5, groups=3)  # noqa: E731
+    mu_a, mu_b = blur(a), blur(b)
+    var_a = blur(a * a) - mu_a**2
+    var_b = blur(b * b) - mu_b**2
+    cov = blur(a * b) - mu_a * mu_b
+    c1, c2 = 0.01**2, 0.03**2
+    s = ((2 * mu_a * mu_b + c1) * (2 * cov + c2)) / ((mu_a**2 + mu_b**2 + c1) * (var_a + var_b + c2))
+    return (1 - lam) * (render - target).abs().mean() + lam * (1 - s.mean())

@@ -93,6 +93,20 @@ def group_errors(gaussian_grads: np.ndarray, sh_grads: np.ndarray, expected: dic
     return out
 
 
+def elementwise_errors(got, want, floor: float) -> tuple[float, float]:
+    """Element-wise relative errors |got - want| / |want| over the values whose
+    magnitude is above `floor` times the largest: (largest, median). This is the
+    plain "relative" form, reported beside the group-max form above, which leaves
+    the small gradients of a group unconstrained."""
+    g = np.asarray(got, np.float64).reshape(-1)
+    w = np.asarray(want, np.float64).reshape(-1)
+    big = np.abs(w) > floor * np.abs(w).max()
+    if not big.any():
+        return 0.0, 0.0
+    rel = np.abs(g[big] - w[big]) / np.abs(w[big])
+    return float(rel.max()), float(np.median(rel))
+
+
 def loss_fixture():
     d = json.loads((GOLDEN / "loss.json").read_text())
     w, h = d["size"]
