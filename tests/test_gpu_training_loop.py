@@ -83,8 +83,9 @@ def test_training_loop_matches_oracle_loop(device):
         state = gpu_state(gpu)
         if lockstep:
             gp, cp = state["params"].reshape(-1, 16)[:, mask], cpu.params.reshape(-1, 16)[:, mask]
-            assert np.abs(gp - cp).max() <= 1e-4, (step, np.abs(gp - cp).max())
-            assert np.abs(state["sh"] - cpu.sh).max() <= 1e-4, step
+            # One step from the same state: measured at most 4.8e-7 (an opacity logit).
+            assert np.abs(gp - cp).max() <= 1e-5, (step, np.abs(gp - cp).max())
+            assert np.abs(state["sh"] - cpu.sh).max() <= 1e-5, step
             cpu.stats = state["stats"].copy()
         gpu.maintain()
         cpu.maintain()
@@ -97,7 +98,7 @@ def test_training_loop_matches_oracle_loop(device):
             assert np.allclose(gp[:, mask], cp[:, mask], rtol=1e-5, atol=1e-6), step
         if step == FREE_STEPS:  # the free-running states after 45 steps
             gp, cp = state["params"].reshape(-1, 16)[:, mask], cpu.params.reshape(-1, 16)[:, mask]
-            assert np.abs(gp - cp).max() <= 1e-3 and np.median(np.abs(gp - cp)) <= 1e-5, np.abs(gp - cp).max()
+            assert np.abs(gp - cp).max() <= 1e-5, np.abs(gp - cp).max()  # measured 7e-7
     got = [(d.step, d.before, d.after, d.kept, d.cloned, d.split, d.removed) for d in gpu.densifications]
     assert got == cpu.densifications
     assert len(got) == 5 and all(d[4] + d[5] > 0 for d in got) and any(d[3] > 0 for d in got), got
@@ -105,8 +106,8 @@ def test_training_loop_matches_oracle_loop(device):
 
     g, c = np.array(losses).T
     rel = np.abs(g - c) / c
-    assert rel[:FREE_STEPS].max() <= 1e-4, rel[:FREE_STEPS].max()
-    assert rel[FREE_STEPS:].max() <= 1e-6, rel[FREE_STEPS:].max()  # the same state: the forward is bit-exact
+    assert rel[:FREE_STEPS].max() <= 1e-5, rel[:FREE_STEPS].max()  # measured 2.5e-7
+    assert rel[FREE_STEPS:].max() <= 1e-9, rel[FREE_STEPS:].max()  # the same state: the forward is bit-exact
     gpu.destroy()
     for v in views:
         v.image.destroy()
