@@ -27,6 +27,21 @@ constexpr uint32_t FLOATS_PER_SPLAT = 12;
 constexpr uint32_t SH_REST_FLOATS = 45;
 // Adam moment slots per Gaussian, one vec2 each (src/trainer.ts:17).
 constexpr uint32_t MOMENT_SLOTS = FLOATS_PER_GAUSSIAN + SH_REST_FLOATS;
+// The trainer keeps a set's moments in two planes (the same 61 vec2 slots per
+// Gaussian as the reference, MOMENT_SLOTS * 8 bytes per Gaussian in all): first
+// the 16 parameter slots of every Gaussian (128-byte records), then the 45 SH
+// slots of every Gaussian. A run of consecutive Gaussians then has its SH
+// moments in one contiguous run indexed like its SH coefficients (g * 45 + k),
+// and its parameter moments in 16-byte-aligned records, so Adam streams both with
+// 16-byte accesses and no per-slot index arithmetic. The reference interleaves
+// the 61 slots per Gaussian (488-byte records, 16-byte aligned only for every
+// other Gaussian); the checkpoint files keep that per-Gaussian order.
+__host__ __device__ __forceinline__ size_t param_moment_at(uint32_t g, uint32_t k) {
+  return (size_t)g * FLOATS_PER_GAUSSIAN + k;
+}
+__host__ __device__ __forceinline__ size_t sh_moment_at(uint32_t count, uint32_t g, uint32_t k) {
+  return (size_t)count * FLOATS_PER_GAUSSIAN + (size_t)g * SH_REST_FLOATS + k;
+}
 // Gradients per splat from the blend's backward (src/shaders/rasterizeBackward.wgsl:124-126).
 constexpr uint32_t SPLAT_GRADS = 9;
 constexpr uint32_t TILE = 16;
@@ -45,6 +60,7 @@ static_assert(sizeof(Camera) == 144, "Camera is 144 bytes like the reference's u
 // Bits of the device error word that bounded waits set instead of hanging.
 constexpr uint32_t DEVICE_ERROR_SCAN_WAIT = 1u << 0;
 constexpr uint32_t DEVICE_ERROR_SORT_WAIT = 1u << 1;
+constexpr uint32_t DEVICE_ERROR_COPY_WAIT = 1u << 2;  // a bulk copy's mbarrier
 // Iteration cap of every spin on another block's status (about a second at worst).
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 

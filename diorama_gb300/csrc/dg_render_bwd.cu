@@ -551,15 +551,13 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
   copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
 }
 
-// The fused kernel's tuning (measured at 1.1M Gaussians: 128 threads, 9 and 8
-// slots, and no minimum of resident CTAs are the fastest of the sizes tried).
-// Slots a thread loads before stepping them in the Adam passes (SH: 45 slots per
-// thread in a full CTA; parameters: 16).
-#ifndef DG_ADAM_SH_BATCH
-#define DG_ADAM_SH_BATCH 9
+// The fused kernel's tuning: the 16-byte groups of slots (four slots each) a
+// thread loads before stepping them in the Adam passes.
+#ifndef DG_ADAM_SH_QUADS
+#define DG_ADAM_SH_QUADS 3
 #endif
-#ifndef DG_ADAM_P_BATCH
-#define DG_ADAM_P_BATCH 8
+#ifndef DG_ADAM_P_QUADS
+#define DG_ADAM_P_QUADS 4
 #endif
 // A minimum of resident CTAs per SM caps the registers (without one ptxas
 // settles at 96 a thread, 5 CTAs of 128 per SM; an explicit minimum of 1 lets it
@@ -570,34 +568,62 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
 #define DG_PBWD_BOUNDS __launch_bounds__(PBWD_THREADS)
 #endif
 
+__device__ __forceinline__ float4 f4_load(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void f4_store(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
 // The training step's preprocess backward with Adam applied at once
-// (src/shaders/preprocessBackward.wgsl:28-181, then src/shaders/adam.wgsl:80-107):
-// the CTA computes its 128 Gaussians' gradients into shared memory (the SH
-// coefficients staged there turn into their gradients), then steps Adam over the
-// CTA's slots, one thread per slot, reading and writing the Gaussians' raw
-// parameters, SH coefficients, moment records and activated values as contiguous
-// runs: the 180 + 64 bytes of gradients per Gaussian never go to memory and back.
-// Each thread also adds its Gaussian's densification statistics
-// (src/shaders/adam.wgsl:126-134).
-// gaussian_grads and sh_grads (may be NULL) also receive the gradients.
+// (src/shaders/preprocessBackward.wgsl:28-181, then src/shaders/adam.wgsl:80-107).
+// A CTA takes 128 consecutive Gaussians:
+// 1. one bulk copy (TMA) brings their SH coefficients, a contiguous 23 KB, into
+//    shared memory, completed on an mbarrier;
+// 2. each thread computes one Gaussian's gradients into shared memory (the SH
+//    coefficients staged there turn into their gradients; the 16 parameter
+//    gradients go to a row of pitch 17) and adds its densification statistics
+//    (src/shaders/adam.wgsl:126-134);
+// 3. Adam steps the CTA's SH slots: their coefficients, SH moments (the second
+//    plane of the moment buffer) and gradients share one index, so each thread
+//    takes 16-byte groups of four slots;
+// 4. Adam steps the raw parameter slots a quarter record (four slots) at a time:
+//    raw values, parameter moments (the first plane) and activated values move
+//    as 16-byte groups. Slots 7 and 15 (pads: a densified Gaussian's kind and
+//    step) keep their raw value and moments; their activated value is 0, as the
+//    reference leaves it (src/shaders/adam.wgsl:60-71 does not write them).
+// The 244 bytes of gradients per Gaussian never go to memory and back;
+// gaussian_grads and sh_grads (may be NULL) also receive them. The host checks
+// that every buffer starts 16-byte aligned. A copy that does not complete within
+// the wait limit sets DEVICE_ERROR_COPY_WAIT and the CTA returns.
 __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
     const Camera* __restrict__ camera, float* __restrict__ gaussians, float* __restrict__ sh, uint32_t count,
     const uint32_t* __restrict__ scene_params, const float* __restrict__ splats, const float* __restrict__ splat_grads,
     const AdamParams* __restrict__ adam, float* __restrict__ params, float2* __restrict__ moments,
     float4* __restrict__ stats, float2* __restrict__ aux, float* __restrict__ gaussian_grads,
-    float* __restrict__ sh_grads) {
+    float* __restrict__ sh_grads, uint32_t* __restrict__ error) {
   constexpr uint32_t GP = FLOATS_PER_GAUSSIAN + 1;  // a row pitch prime to 32
   __shared__ Camera s_cam;
   __shared__ __align__(16) float s_sh[PBWD_THREADS * SH_REST_FLOATS];  // coefficients, then their gradients
   __shared__ float s_pg[PBWD_THREADS * GP];                            // parameter gradients
   __shared__ AdamParams s_ap;
-  load_camera(s_cam, camera);
-  if (threadIdx.x == 0) s_ap = *adam;
+  __shared__ __align__(8) uint64_t s_bar;
   const uint32_t block_start = blockIdx.x * PBWD_THREADS;
   const uint32_t here = min(PBWD_THREADS, count - block_start);
-  stage_floats_async(s_sh, sh + (size_t)block_start * SH_REST_FLOATS, here * SH_REST_FLOATS);
-  cp_async_wait_all();
-  __syncthreads();
+  const uint32_t sh_total = here * SH_REST_FLOATS;
+  float* sh_block = sh + (size_t)block_start * SH_REST_FLOATS;
+  const uint32_t quads = sh_total / 4;  // the 16-byte groups (all of a full CTA's 5,760 floats)
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar, 1);
+    mbar_arrive_expect_tx(&s_bar, quads * 16);
+    bulk_copy_to_shared(s_sh, sh_block, quads * 16, &s_bar);
+    s_ap = *adam;
+  }
+  __syncthreads();  // the barrier is initialized before anyone waits on it
+  load_camera(s_cam, camera);
+  for (uint32_t e = quads * 4 + threadIdx.x; e < sh_total; e += PBWD_THREADS) s_sh[e] = sh_block[e];
+  const bool copied = mbar_wait_bounded(&s_bar, 0);
+  if (__syncthreads_or(!copied)) {
+    if (threadIdx.x == 0) atomicOr(error, DEVICE_ERROR_COPY_WAIT);
+    mbar_wait_bounded(&s_bar, 0);  // the copy may still be writing this CTA's shared memory
+    return;
+  }
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
   const uint32_t i = block_start + threadIdx.x;
@@ -612,66 +638,97 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
     accumulate_stats_one(s_ap.viewport, splats, splat_grads, stats, aux, i);
   }
   __syncthreads();
-  if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, here * SH_REST_FLOATS);
+  if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, sh_total);
   const AdamParams& ap = s_ap;
-  // The SH slots (moment slots 16-60 of each record): each thread loads a batch of
-  // slots before stepping them, so that enough reads are in flight to cover DRAM
-  // latency at this kernel's occupancy.
-  constexpr uint32_t SH_BATCH = DG_ADAM_SH_BATCH;
-  float* sh_block = sh + (size_t)block_start * SH_REST_FLOATS;
-  float2* sh_moments = moments + (size_t)block_start * MOMENT_SLOTS + FLOATS_PER_GAUSSIAN;
-  const uint32_t sh_total = here * SH_REST_FLOATS;
-  for (uint32_t base = threadIdx.x; base < sh_total; base += PBWD_THREADS * SH_BATCH) {
-    float2 m[SH_BATCH];
-    float v[SH_BATCH];
+  const float inv_bc1 = ap.inv_bias_correction1, inv_sqrt_bc2 = ap.inv_sqrt_bias_correction2;
+
+  // 3. The SH slots, four at a time; a thread loads a batch of groups before
+  // stepping them, so that enough reads are in flight.
+  {
+    constexpr uint32_t B = DG_ADAM_SH_QUADS;
+    float4* m_block = reinterpret_cast<float4*>(moments + sh_moment_at(count, block_start, 0));
+    const float lr = ap.sh_lr;
+    for (uint32_t base = threadIdx.x; base < quads; base += PBWD_THREADS * B) {
+      float4 v[B], m0[B], m1[B];
 #pragma unroll
-    for (uint32_t u = 0; u < SH_BATCH; u++) {
-      const uint32_t e = base + u * PBWD_THREADS;
-      if (e < sh_total) {
-        const uint32_t g = e / SH_REST_FLOATS;
-        m[u] = sh_moments[(size_t)g * MOMENT_SLOTS + (e - g * SH_REST_FLOATS)];
-        v[u] = sh_block[e];
+      for (uint32_t u = 0; u < B; u++) {
+        const uint32_t q = base + u * PBWD_THREADS;
+        if (q < quads) {
+          v[u] = f4_load(sh_block + 4 * q);
+          m0[u] = m_block[2 * q];
+          m1[u] = m_block[2 * q + 1];
+        }
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < B; u++) {
+        const uint32_t q = base + u * PBWD_THREADS;
+        if (q < quads) {
+          const float4 g = f4_load(s_sh + 4 * q);
+          float2 a = make_float2(m0[u].x, m0[u].y), b = make_float2(m0[u].z, m0[u].w);
+          float2 c = make_float2(m1[u].x, m1[u].y), d = make_float2(m1[u].z, m1[u].w);
+          float4 out;
+          out.x = adam_step_fast(v[u].x, g.x, a, lr, inv_bc1, inv_sqrt_bc2);
+          out.y = adam_step_fast(v[u].y, g.y, b, lr, inv_bc1, inv_sqrt_bc2);
+          out.z = adam_step_fast(v[u].z, g.z, c, lr, inv_bc1, inv_sqrt_bc2);
+          out.w = adam_step_fast(v[u].w, g.w, d, lr, inv_bc1, inv_sqrt_bc2);
+          f4_store(sh_block + 4 * q, out);
+          m_block[2 * q] = make_float4(a.x, a.y, b.x, b.y);
+          m_block[2 * q + 1] = make_float4(c.x, c.y, d.x, d.y);
+        }
       }
     }
-#pragma unroll
-    for (uint32_t u = 0; u < SH_BATCH; u++) {
-      const uint32_t e = base + u * PBWD_THREADS;
-      if (e < sh_total) {
-        const uint32_t g = e / SH_REST_FLOATS;
-        sh_block[e] = adam_step_fast(v[u], s_sh[e], m[u], ap.sh_lr, ap.inv_bias_correction1,
-                                     ap.inv_sqrt_bias_correction2);
-        sh_moments[(size_t)g * MOMENT_SLOTS + (e - g * SH_REST_FLOATS)] = m[u];
-      }
+    // The last floats of a partial CTA, one slot at a time.
+    float2* m_slots = moments + sh_moment_at(count, block_start, 0);
+    for (uint32_t e = quads * 4 + threadIdx.x; e < sh_total; e += PBWD_THREADS) {
+      float2 m = m_slots[e];
+      sh_block[e] = adam_step_fast(sh_block[e], s_sh[e], m, lr, inv_bc1, inv_sqrt_bc2);
+      m_slots[e] = m;
     }
   }
-  // The raw parameter slots (0-15 but 7 and 15) and their activated values, all
-  // of a thread's slots loaded at once (16 per thread in a full CTA).
-  constexpr uint32_t P_BATCH = DG_ADAM_P_BATCH;
-  float* p_block = params + (size_t)block_start * FLOATS_PER_GAUSSIAN;
-  float* a_block = gaussians + (size_t)block_start * FLOATS_PER_GAUSSIAN;
-  float2* p_moments = moments + (size_t)block_start * MOMENT_SLOTS;
-  const uint32_t p_total = here * FLOATS_PER_GAUSSIAN;
-  for (uint32_t base = threadIdx.x; base < p_total; base += PBWD_THREADS * P_BATCH) {
-    float2 m[P_BATCH];
-    float v[P_BATCH];
+
+  // 4. The raw parameter slots, a quarter record at a time (PBWD_THREADS is a
+  // multiple of 4, so a thread always takes the same quarter of its records).
+  {
+    constexpr uint32_t B = DG_ADAM_P_QUADS;
+    float* p_block = params + (size_t)block_start * FLOATS_PER_GAUSSIAN;
+    float* a_block = gaussians + (size_t)block_start * FLOATS_PER_GAUSSIAN;
+    float4* m_block = reinterpret_cast<float4*>(moments + param_moment_at(block_start, 0));
+    const uint32_t p_quads = here * 4;
+    const uint32_t k0 = 4 * (threadIdx.x & 3u);
+    for (uint32_t base = threadIdx.x; base < p_quads; base += PBWD_THREADS * B) {
+      float4 x[B], m0[B], m1[B];
 #pragma unroll
-    for (uint32_t u = 0; u < P_BATCH; u++) {
-      const uint32_t e = base + u * PBWD_THREADS;
-      const uint32_t k = e & 15u;  // the same for every u: PBWD_THREADS is a multiple of 16
-      if (e < p_total && k != 7 && k != 15) {
-        m[u] = p_moments[(size_t)(e >> 4) * MOMENT_SLOTS + k];
-        v[u] = p_block[e];
+      for (uint32_t u = 0; u < B; u++) {
+        const uint32_t q = base + u * PBWD_THREADS;
+        if (q < p_quads) {
+          x[u] = f4_load(p_block + 4 * q);
+          m0[u] = m_block[2 * q];
+          m1[u] = m_block[2 * q + 1];
+        }
       }
-    }
 #pragma unroll
-    for (uint32_t u = 0; u < P_BATCH; u++) {
-      const uint32_t e = base + u * PBWD_THREADS;
-      const uint32_t g = e >> 4, k = e & 15u;
-      if (e < p_total && k != 7 && k != 15) {
-        float act;
-        p_block[e] = adam_param_slot(ap, k, v[u], s_pg[g * GP + k], m[u], act);
-        p_moments[(size_t)g * MOMENT_SLOTS + k] = m[u];
-        a_block[e] = act;
+      for (uint32_t u = 0; u < B; u++) {
+        const uint32_t q = base + u * PBWD_THREADS;
+        if (q < p_quads) {
+          const float* grad = s_pg + (q >> 2) * GP + k0;
+          float xs[4] = {x[u].x, x[u].y, x[u].z, x[u].w};
+          float2 ms[4] = {make_float2(m0[u].x, m0[u].y), make_float2(m0[u].z, m0[u].w),
+                          make_float2(m1[u].x, m1[u].y), make_float2(m1[u].z, m1[u].w)};
+          float act[4];
+#pragma unroll
+          for (uint32_t j = 0; j < 4; j++) {
+            const uint32_t k = k0 + j;
+            if (j == 3 && (k == 7 || k == 15)) {
+              act[j] = 0.0f;  // a pad: raw value and moments stay as they are
+            } else {
+              xs[j] = adam_param_slot(ap, k, xs[j], grad[j], ms[j], act[j]);
+            }
+          }
+          f4_store(p_block + 4 * q, make_float4(xs[0], xs[1], xs[2], xs[3]));
+          m_block[2 * q] = make_float4(ms[0].x, ms[0].y, ms[1].x, ms[1].y);
+          m_block[2 * q + 1] = make_float4(ms[2].x, ms[2].y, ms[3].x, ms[3].y);
+          f4_store(a_block + 4 * q, make_float4(act[0], act[1], act[2], act[3]));
+        }
       }
     }
   }
@@ -698,12 +755,16 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
 
 dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam, float* params, float2* moments,
                                          float4* stats, float2* aux, bool keep_gradients) {
+  // Every stream of the kernel moves 16-byte groups from the start of each buffer.
+  const void* starts[] = {params, moments, ptr_of(r->gaussians), ptr_of(r->sh)};
+  for (const void* p : starts)
+    DG_REQUIRE((reinterpret_cast<uintptr_t>(p) & 15) == 0, "the training buffers must start 16-byte aligned");
   DG_LAUNCH(r->ctx, "preprocess_backward_adam",
             preprocess_backward_adam_kernel<<<ceil_div(r->count, PBWD_THREADS), PBWD_THREADS, 0, r->ctx->stream>>>(
                 typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                 typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats), adam, params,
                 moments, stats, aux, keep_gradients ? typed<float>(r->grad_gaussians) : nullptr,
-                keep_gradients ? typed<float>(r->grad_sh) : nullptr));
+                keep_gradients ? typed<float>(r->grad_sh) : nullptr, r->ctx->device_error));
   return DG_OK;
 }
 

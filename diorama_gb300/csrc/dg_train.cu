@@ -48,7 +48,7 @@ __global__ void reset_opacity_kernel(float* __restrict__ params, float2* __restr
   const size_t at = (size_t)i * FLOATS_PER_GAUSSIAN + 3;
   const float v = fminf(params[at], RESET_LOGIT);
   params[at] = v;
-  moments[(size_t)i * MOMENT_SLOTS + RESET_SLOT] = make_float2(0.f, 0.f);
+  moments[param_moment_at(i, RESET_SLOT)] = make_float2(0.f, 0.f);
   gaussians[at] = sigmoidf_(v);
 }
 
@@ -124,9 +124,14 @@ __device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const
                                                   uint32_t first_id, float* __restrict__ new_params,
                                                   float* __restrict__ new_sh, float2* __restrict__ new_moments,
                                                   uint32_t* __restrict__ new_ids, float2* __restrict__ new_aux,
-                                                  float* __restrict__ new_gaussians, uint32_t i, uint32_t k,
-                                                  uint32_t a, uint32_t o) {
-  const uint32_t e = i * MOMENT_SLOTS + k;
+                                                  float* __restrict__ new_gaussians, uint32_t count,
+                                                  uint32_t new_count, uint32_t i, uint32_t k, uint32_t a,
+                                                  uint32_t o) {
+  // Moment slot k of Gaussian g in a set of n (the two planes of param_moment_at / sh_moment_at).
+  auto slot = [](uint32_t n, uint32_t g, uint32_t k) {
+    return k < FLOATS_PER_GAUSSIAN ? param_moment_at(g, k) : sh_moment_at(n, g, k - FLOATS_PER_GAUSSIAN);
+  };
+  const size_t e = slot(count, i, k);
   const uint32_t copies = a == 1 ? 1u : 2u;
   if (k == 0) {
     for (uint32_t c = 0; c < copies; c++) {
@@ -145,7 +150,7 @@ __device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const
   for (uint32_t c = 0; c < copies; c++) {
     const uint32_t dst = o + c;
     const bool keep = (a == 1 || a == 2) && c == 0;
-    new_moments[(size_t)dst * MOMENT_SLOTS + k] = keep ? m : zero;
+    new_moments[slot(new_count, dst, k)] = keep ? m : zero;
     if (k < FLOATS_PER_GAUSSIAN) {
       float v = value;
       if (a == 2 && c == 1) {
@@ -181,7 +186,8 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
                                                            const uint32_t* __restrict__ ids,
                                                            const float2* __restrict__ aux,
                                                            const uint32_t* __restrict__ outputs, uint32_t count,
-                                                           uint32_t first_id, float* __restrict__ new_params,
+                                                           uint32_t new_count, uint32_t first_id,
+                                                           float* __restrict__ new_params,
                                                            float* __restrict__ new_sh,
                                                            float2* __restrict__ new_moments,
                                                            uint32_t* __restrict__ new_ids,
@@ -195,10 +201,10 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
     if (a == 0) continue;
     const uint32_t o = outputs[i];
     densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids, new_aux,
-                      new_gaussians, i, lane, a, o);
+                      new_gaussians, count, new_count, i, lane, a, o);
     if (lane + 32u < MOMENT_SLOTS)
       densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids,
-                        new_aux, new_gaussians, i, lane + 32u, a, o);
+                        new_aux, new_gaussians, count, new_count, i, lane + 32u, a, o);
   }
 }
 
@@ -870,7 +876,7 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
                                   ctx->stream>>>(
                 dp, typed<float>(t->params), typed<uint8_t>(actions), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),
-                count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
+                count, new_count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
                 typed<uint32_t>(ids), typed<float2>(aux), typed<float>(gaussians)));
   DG_LAUNCH(ctx, "densify_place",
             densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
@@ -1262,7 +1268,10 @@ dg_status dg_trainer_save_checkpoint(dg_trainer* t, const char* path) {
       size_t at = 62;
       row[at++] = params[i * FLOATS_PER_GAUSSIAN + 7];
       row[at++] = params[i * FLOATS_PER_GAUSSIAN + 15];
-      std::memcpy(row + at, moments.data() + i * MOMENT_SLOTS * 2, MOMENT_SLOTS * 8);
+      // The moments in the reference's per-Gaussian order: 16 parameter slots, then 45 SH slots.
+      std::memcpy(row + at, moments.data() + param_moment_at((uint32_t)i, 0) * 2, FLOATS_PER_GAUSSIAN * 8);
+      std::memcpy(row + at + FLOATS_PER_GAUSSIAN * 2, moments.data() + sh_moment_at(n, (uint32_t)i, 0) * 2,
+                  SH_REST_FLOATS * 8);
       at += MOMENT_SLOTS * 2;
       std::memcpy(row + at, stats.data() + i * 4, 16);
       std::memcpy(row + at + 4, aux.data() + i * 2, 8);
@@ -1362,7 +1371,12 @@ dg_status dg_trainer_resume(dg_context* ctx, const char* path, const dg_training
     for (uint32_t c = 0; c < per_channel; c++)
       for (uint32_t channel = 0; channel < 3; channel++)
         sh[i * SH_REST_FLOATS + c * 3 + channel] = real(0, i, rc[channel * per_channel + c]);
-    for (uint32_t k = 0; k < MOMENT_SLOTS * 2; k++) moments[i * MOMENT_SLOTS * 2 + k] = real(0, i, mc[k]);
+    for (uint32_t k = 0; k < MOMENT_SLOTS; k++) {  // the file's per-Gaussian order into the two planes
+      const size_t at = k < FLOATS_PER_GAUSSIAN ? param_moment_at((uint32_t)i, k)
+                                                : sh_moment_at(n, (uint32_t)i, k - FLOATS_PER_GAUSSIAN);
+      moments[at * 2] = real(0, i, mc[2 * k]);
+      moments[at * 2 + 1] = real(0, i, mc[2 * k + 1]);
+    }
     for (int k = 0; k < 4; k++) stats[i * 4 + k] = real(0, i, sc[k]);
     for (int k = 0; k < 2; k++) aux[i * 2 + k] = real(0, i, sc[4 + k]);
     ids[i] = word(1, i, idc);

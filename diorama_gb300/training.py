@@ -129,6 +129,22 @@ def activate(params) -> np.ndarray:
     return out.astype(np.float32).reshape(-1)
 
 
+def moments_to_reference(planes, count: int) -> np.ndarray:
+    """The trainer's moment buffer (two planes: count x 16 parameter slots, then
+    count x 45 SH slots, each an (m, v) pair) in the reference's layout: 61 slots
+    per Gaussian, parameters first (src/trainer.ts:17), as count * 122 floats."""
+    p = np.asarray(planes, np.float32).reshape(-1)[: count * MOMENT_SLOTS * 2]
+    params = p[: count * FLOATS_PER_GAUSSIAN * 2].reshape(count, FLOATS_PER_GAUSSIAN * 2)
+    sh = p[count * FLOATS_PER_GAUSSIAN * 2:].reshape(count, SH_REST_FLOATS * 2)
+    return np.ascontiguousarray(np.concatenate([params, sh], axis=1)).reshape(-1)
+
+
+def moments_from_reference(reference, count: int) -> np.ndarray:
+    """The inverse of moments_to_reference."""
+    r = np.asarray(reference, np.float32).reshape(count, MOMENT_SLOTS * 2)
+    return np.concatenate([r[:, : FLOATS_PER_GAUSSIAN * 2].reshape(-1), r[:, FLOATS_PER_GAUSSIAN * 2:].reshape(-1)])
+
+
 def _views_c(views) -> ctypes.Array:
     arr = (_lib.TrainingViewC * len(views))()
     for k, v in enumerate(views):
@@ -257,6 +273,14 @@ class Trainer:
     def buffers(self) -> dict:
         b = lambda name: borrowed(self.device, _lib.fn(name)(self.handle))  # noqa: E731
         return {"params": b("dg_trainer_params"), "moments": b("dg_trainer_moments"), "stats": b("dg_trainer_stats")}
+
+    def readMoments(self) -> np.ndarray:
+        """Adam's moments in the reference's layout (count x 61 (m, v) pairs)."""
+        return moments_to_reference(self.buffers["moments"].read(np.float32), self.count)
+
+    def writeMoments(self, reference) -> None:
+        """Sets Adam's moments from the reference's layout (count x 61 (m, v) pairs)."""
+        self.buffers["moments"].write(moments_from_reference(reference, self.count))
 
     @property
     def densifications(self) -> list[Densification]:

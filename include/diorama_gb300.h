@@ -317,6 +317,13 @@ uint32_t dg_trainer_adam_steps(const dg_trainer* t);
 uint32_t dg_trainer_count(const dg_trainer* t);
 dg_renderer* dg_trainer_renderer(dg_trainer* t);
 dg_buffer* dg_trainer_params(dg_trainer* t);
+/* buffers.moments: Adam's (m, v) per slot, the reference's 61 slots per Gaussian
+ * (src/trainer.ts:17; MOMENT_SLOTS * 8 bytes per Gaussian) held in two planes:
+ * the 16 parameter slots of every Gaussian (count x 16 (m, v), 128-byte records),
+ * then the 45 SH slots of every Gaussian (count x 45 (m, v)). The reference
+ * interleaves the 61 slots per Gaussian; the planes let Adam move 16-byte groups
+ * (a run of Gaussians has its SH moments contiguous, indexed like its SH
+ * coefficients). Checkpoint files keep the reference's per-Gaussian order. */
 dg_buffer* dg_trainer_moments(dg_trainer* t);
 dg_buffer* dg_trainer_stats(dg_trainer* t);
 uint32_t dg_trainer_densification_count(const dg_trainer* t);

@@ -207,7 +207,7 @@ def test_learned_densify_fallback_and_veto(device):
     warm = _densifying_run(device, views, params)
     raw = warm.exportRaw()
     stats = warm.buffers["stats"].read(np.float32)
-    moments = warm.buffers["moments"].read(np.float32)
+    moments = warm.readMoments()
     n = raw.params.size // 16
     rng = np.random.default_rng(9)
     stats = stats.reshape(-1, 4)
@@ -219,7 +219,7 @@ def test_learned_densify_fallback_and_veto(device):
     def densify_once(mlp=None):
         t = Trainer(device, RawGaussians(raw.params.copy(), raw.sh.copy()), views,
                     replace(DEFAULT_SETTINGS, extent=3.85, densifyGradThreshold=1e-4))
-        t.buffers["moments"].write(moments)
+        t.writeMoments(moments)
         t.buffers["stats"].write(stats)
         if mlp is not None:
             t.setDensifyMLP(mlp, 0.6)

@@ -68,7 +68,7 @@ def test_adam_step_matches_oracle(device):
     t = Trainer(device, RawGaussians(params, sh), views, settings)
     moments = rng.uniform(-1, 1, n * 61 * 2).astype(np.float32)
     moments[1::2] = np.abs(moments[1::2])
-    t.buffers["moments"].write(moments)
+    t.writeMoments(moments)
     t.setKeepGradients(True)
     t.optimize()
     grads = t.renderer.gradients
@@ -84,7 +84,7 @@ def test_adam_step_matches_oracle(device):
     mask[[7, 15]] = False
     assert np.allclose(got_p.reshape(-1, 16)[:, mask], want_p.reshape(-1, 16)[:, mask], rtol=1e-6, atol=1e-7)
     assert np.allclose(t.renderer.shBuffer.read(np.float32), want_sh, rtol=1e-6, atol=1e-7)
-    got_m = t.buffers["moments"].read(np.float32)
+    got_m = t.readMoments()
     assert np.allclose(got_m, want_m, rtol=1e-5, atol=1e-9)
     slots = got_m.reshape(n, 61, 2)
     assert np.array_equal(slots[:, [7, 15]], moments.reshape(n, 61, 2)[:, [7, 15]])  # padding slots untouched
@@ -133,7 +133,7 @@ def test_densify_and_reset(device, prune_large):
     cam = CameraData(IDENTITY, IDENTITY, (16, 16))
     t = Trainer(device, RawGaussians(params.copy(), sh), [TrainingView("unused", cam, image)],
                 replace(DEFAULT_SETTINGS, extent=1.0))
-    t.buffers["moments"].write(moments)
+    t.writeMoments(moments)
     t.buffers["stats"].write(stats)
     t.iteration = 700
     t.densify(prune_large)
@@ -146,7 +146,7 @@ def test_densify_and_reset(device, prune_large):
     got_p = t.buffers["params"].read(np.float32)
     assert np.allclose(got_p, want_p, rtol=1e-5, atol=1e-6)
     assert np.array_equal(t.renderer.shBuffer.read(np.float32), want_sh)
-    got_m = t.buffers["moments"].read(np.float32)
+    got_m = t.readMoments()
     assert np.array_equal(got_m, want_m)
     assert not t.buffers["stats"].read(np.float32).any()
     act = t.renderer.gaussianBuffer.read(np.float32).reshape(-1, 16)
@@ -161,7 +161,7 @@ def test_densify_and_reset(device, prune_large):
     # Opacity reset: every opacity capped at 0.01, and only its Adam slot cleared.
     t.resetOpacity()
     p2 = t.buffers["params"].read(np.float32).reshape(-1, 16)
-    m2 = t.buffers["moments"].read(np.float32).reshape(-1, 122)
+    m2 = t.readMoments().reshape(-1, 122)
     capped = np.float32(-4.59511985013459)
     assert np.array_equal(p2[:, 3], np.minimum(got_p.reshape(-1, 16)[:, 3], capped))
     assert not m2[:, 6:8].any()

@@ -38,7 +38,7 @@ def gpu_state(gpu):
     n = gpu.count
     b = gpu.buffers
     return dict(params=b["params"].read(np.float32)[: n * 16].copy(),
-                moments=b["moments"].read(np.float32)[: n * 122].copy(),
+                moments=gpu.readMoments(),
                 stats=b["stats"].read(np.float32)[: n * 4].copy(),
                 sh=gpu.renderer.shBuffer.read(np.float32)[: n * 45].copy(),
                 gaussians=gpu.renderer.gaussianBuffer.read(np.float32)[: n * 16].copy())
