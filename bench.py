@@ -58,11 +58,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
-    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn"],
+    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn", "profile"],
                     help="train: the headline training step; sort: the sort/scan/ranges stress "
                          "(1.1M random Gaussians at 1960x1090, the reference's 6-pass sort); densify: "
                          "plain vs learned densification on the planes-and-boxes scene (minutes); knn: the "
-                         "starting Gaussians' nearest-neighbour distances of a point cloud")
+                         "starting Gaussians' nearest-neighbour distances of a point cloud; profile: one training "
+                         "step bracketed for a profiler started with collection off")
     ap.add_argument("--knn-points", type=int, default=1_100_000, help="knn workload: points in the cloud")
     ap.add_argument("--train-steps", type=int, default=30_000, help="densify workload: steps per training run")
     ap.add_argument("--plain-runs", type=int, default=3, help="densify workload: seeded plain runs that log labels")
@@ -623,6 +624,54 @@ def run_sort_stress(args, rank, local):
     return result
 
 
+def run_profile_step(args, rank, local):
+    """One training step of the headline workload (direct launches), bracketed for a
+    profiler started with collection off (`ncu --profile-from-start off`), after
+    --warmup steps. Prints the step's work: the blend's evaluations (the forward's
+    pixel_last summed over the frame's pixels), pairs and Gaussians, with the
+    step's kernel times from CUDA events, so that a profiler's per-kernel counters
+    can be divided by the work of the same launch."""
+    if rank != 0:
+        return None
+    from diorama_gb300 import DEFAULT_SETTINGS, Device, GaussianRenderer, RawGaussians, Trainer, TrainingView, activate
+
+    raw, sh, truth_raw, truth_sh, cams = build_scene(args)
+    device = Device(local)
+    W, H = cams[0].viewport
+    photographer = GaussianRenderer(device)
+    photographer.setGaussians(activate(truth_raw), {"rest": truth_sh.reshape(-1), "degree": 3})
+    views = []
+    for k, cam in enumerate(cams):
+        tex = device.createTexture(W, H)
+        photographer.encode(None, tex, cam, (0, 0, 0))
+        views.append(TrainingView(f"view {k}", cam, tex))
+    device.synchronize()
+    photographer.destroy()
+    settings = replace(DEFAULT_SETTINGS, extent=4.0, shDegreeInterval=1, densifyUntil=0)
+    trainer = Trainer(device, RawGaussians(raw.reshape(-1), sh.reshape(-1)), views, settings)
+    for _ in range(args.warmup):
+        trainer.step()
+    trainer.renderer.afterSubmit()
+    view = trainer.nextView()
+    device.setKernelTiming(True)
+    device.kernelTimingReport()
+    device.profile(True)
+    trainer.step()
+    device.profile(False)
+    report = device.kernelTimingReport()
+    device.setKernelTiming(False)
+    last = trainer.renderer.pixelLastBuffer.read(np.uint32)[: W * H]
+    result = {"workload": "one training step for a profiler", "gaussians": trainer.count, "viewport": [W, H],
+              "view": view, "warmup_steps": args.warmup, "pairs": trainer.renderer.tiles.lastPairCount,
+              "blend_evaluations": int(last.astype(np.int64).sum()),
+              "kernels_us": {k: round(1000 * t / c, 2) for k, (c, t) in report.items()}}
+    trainer.destroy()
+    for v in views:
+        v.image.destroy()
+    device.destroy()
+    return result
+
+
 def run_knn(args, rank, local):
     """The starting Gaussians' neighbour distances (src/loadDataset.ts:124-149) of
     a structure-from-motion-like cloud (clusters, a plane, 1% far outliers,
@@ -854,6 +903,8 @@ def main():
         result = run_densify_experiment(args, rank, local) if args.impl == "ours" else None
     elif args.workload == "knn":
         result = run_knn(args, rank, local) if args.impl == "ours" else None
+    elif args.workload == "profile":
+        result = run_profile_step(args, rank, local) if args.impl == "ours" else None
     elif args.impl == "reference":
         result = run_reference(args, rank, world, group)
     else:

@@ -82,6 +82,7 @@ SIGNATURES = {
     "dg_context_check": (None, [_P, POINTER(c_uint32)]),
     "dg_context_launch_count": (None, [_P, POINTER(c_uint64)]),
     "dg_context_set_kernel_timing": (None, [_P, c_int32]),
+    "dg_context_profile": (None, [_P, c_int32]),
     "dg_context_kernel_timing_report": (None, [_P, ctypes.c_char_p, c_uint64]),
     "dg_event_create": (None, [_P, POINTER(_P)]),
     "dg_event_record": (None, [_P]),

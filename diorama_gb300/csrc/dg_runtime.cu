@@ -3,6 +3,8 @@
 #include "dg_common.cuh"
 #include "dg_scan.cuh"
 
+#include <cuda_profiler_api.h>
+
 #include <algorithm>
 #include <cstdio>
 
@@ -203,6 +205,13 @@ dg_status dg_context_check(dg_context* ctx, uint32_t* bits) {
 dg_status dg_context_launch_count(dg_context* ctx, uint64_t* out) {
   DG_REQUIRE(ctx && out, "NULL argument");
   *out = ctx->launches;
+  return DG_OK;
+}
+
+dg_status dg_context_profile(dg_context* ctx, int32_t enabled) {
+  DG_REQUIRE(ctx, "NULL argument");
+  DG_CUDA(cudaStreamSynchronize(ctx->stream));
+  DG_CUDA(enabled ? cudaProfilerStart() : cudaProfilerStop());
   return DG_OK;
 }
 

@@ -116,69 +116,93 @@ __device__ __forceinline__ uint32_t pcg(uint32_t v) {
 
 __device__ __forceinline__ float unit_of(uint32_t h) { return ((float)(h >> 8u) + 0.5f) / 16777216.0f; }
 
-// Slot k of Gaussian i, whose action is a (1 keep, 2 clone, 3 split) and whose
-// first output is o.
-__device__ __forceinline__ void densify_copy_slot(const DensifyParams& dp, const float* __restrict__ params,
-                                                  const float* __restrict__ sh, const float2* __restrict__ moments,
-                                                  const uint32_t* __restrict__ ids, const float2* __restrict__ aux,
-                                                  uint32_t first_id, float* __restrict__ new_params,
-                                                  float* __restrict__ new_sh, float2* __restrict__ new_moments,
-                                                  uint32_t* __restrict__ new_ids, float2* __restrict__ new_aux,
-                                                  float* __restrict__ new_gaussians, uint32_t count,
-                                                  uint32_t new_count, uint32_t i, uint32_t k, uint32_t a,
-                                                  uint32_t o) {
-  // Moment slot k of Gaussian g in a set of n (the two planes of param_moment_at / sh_moment_at).
-  auto slot = [](uint32_t n, uint32_t g, uint32_t k) {
-    return k < FLOATS_PER_GAUSSIAN ? param_moment_at(g, k) : sh_moment_at(n, g, k - FLOATS_PER_GAUSSIAN);
-  };
-  const size_t e = slot(count, i, k);
-  const uint32_t copies = a == 1 ? 1u : 2u;
-  if (k == 0) {
-    for (uint32_t c = 0; c < copies; c++) {
-      const bool keep = (a == 1 || a == 2) && c == 0;
-      new_ids[o + c] = keep ? ids[i] : first_id + o + c;
-      new_aux[o + c] = make_float2(0.0f, keep ? aux[i].y : 0.0f);
+// Moment slot k (0-60) of Gaussian g in a set of n, in the two planes of
+// param_moment_at / sh_moment_at.
+__device__ __forceinline__ size_t moment_slot(uint32_t n, uint32_t g, uint32_t k) {
+  return k < FLOATS_PER_GAUSSIAN ? param_moment_at(g, k) : sh_moment_at(n, g, k - FLOATS_PER_GAUSSIAN);
+}
+
+// What one lane reads of one Gaussian: the moments and values of its two slots
+// (lane and lane + 32), and on lane 0 the identity and the steps seen.
+struct SlotPair {
+  float2 m[2];
+  float v[2];
+  uint32_t id;
+  float seen;
+};
+
+__device__ __forceinline__ void densify_load(const float* __restrict__ params, const float* __restrict__ sh,
+                                             const float2* __restrict__ moments, const uint32_t* __restrict__ ids,
+                                             const float2* __restrict__ aux, uint32_t count, uint32_t i,
+                                             uint32_t lane, SlotPair& s) {
+#pragma unroll
+  for (uint32_t h = 0; h < 2; h++) {
+    const uint32_t k = lane + 32u * h;
+    if (k < MOMENT_SLOTS) {
+      s.m[h] = moments[moment_slot(count, i, k)];
+      s.v[h] = k < FLOATS_PER_GAUSSIAN ? params[(size_t)i * FLOATS_PER_GAUSSIAN + k]
+                                       : sh[(size_t)i * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)];
     }
   }
-  const float2 m = moments[e];
+  if (lane == 0) {
+    s.id = ids[i];
+    s.seen = aux[i].y;
+  }
+}
+
+// Writes the outputs of Gaussian i, whose action is a (1 keep, 2 clone, 3 split)
+// and whose first output is o (src/shaders/densify.wgsl:148-180): a kept Gaussian
+// and a clone's original keep their moments, identity and steps seen; new ones
+// get zero moments, identity first_id + their output index and zero statistics;
+// a clone's copy and split children are stamped with their kind and the step
+// (slots 7 and 15), split children shrink by 1.6 (densify_place_kernel then sets
+// their positions). The activated values follow (src/shaders/adam.wgsl:74-77).
+__device__ __forceinline__ void densify_store(const DensifyParams& dp, uint32_t first_id, uint32_t new_count,
+                                              uint32_t a, uint32_t o, uint32_t lane, const SlotPair& s,
+                                              float* __restrict__ new_params, float* __restrict__ new_sh,
+                                              float2* __restrict__ new_moments, uint32_t* __restrict__ new_ids,
+                                              float2* __restrict__ new_aux, float* __restrict__ new_gaussians) {
+  const uint32_t copies = a == 1 ? 1u : 2u;
   const float2 zero = make_float2(0.f, 0.f);
-  float value = 0.0f;
-  if (k < FLOATS_PER_GAUSSIAN)
-    value = params[(size_t)i * FLOATS_PER_GAUSSIAN + k];
-  else
-    value = sh[(size_t)i * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)];
   for (uint32_t c = 0; c < copies; c++) {
     const uint32_t dst = o + c;
     const bool keep = (a == 1 || a == 2) && c == 0;
-    new_moments[slot(new_count, dst, k)] = keep ? m : zero;
-    if (k < FLOATS_PER_GAUSSIAN) {
-      float v = value;
-      if (a == 2 && c == 1) {
-        if (k == 7) v = 1.0f;
-        if (k == 15) v = (float)dp.seed;
+    if (lane == 0) {
+      new_ids[dst] = keep ? s.id : first_id + dst;
+      new_aux[dst] = make_float2(0.0f, keep ? s.seen : 0.0f);
+    }
+#pragma unroll
+    for (uint32_t h = 0; h < 2; h++) {
+      const uint32_t k = lane + 32u * h;
+      if (k >= MOMENT_SLOTS) continue;
+      new_moments[moment_slot(new_count, dst, k)] = keep ? s.m[h] : zero;
+      if (k < FLOATS_PER_GAUSSIAN) {
+        float v = s.v[h];
+        if (a == 2 && c == 1) {
+          if (k == 7) v = 1.0f;
+          if (k == 15) v = (float)dp.seed;
+        }
+        if (a == 3) {
+          if (k >= 4 && k <= 6) v = s.v[h] - LOG_SPLIT_SHRINK;
+          if (k == 7) v = 2.0f;
+          if (k == 15) v = (float)dp.seed;
+        }
+        new_params[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = v;
+        if (k != 7 && k != 15) new_gaussians[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = activated(k, v);
+      } else {
+        new_sh[(size_t)dst * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)] = s.v[h];
       }
-      if (a == 3) {
-        if (k >= 4 && k <= 6) v = value - LOG_SPLIT_SHRINK;
-        if (k == 7) v = 2.0f;
-        if (k == 15) v = (float)dp.seed;
-      }
-      new_params[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = v;
-      // The activated copy (src/shaders/adam.wgsl:74-77; a split child's position
-      // is replaced by densify_place_kernel, in both).
-      if (k != 7 && k != 15) new_gaussians[(size_t)dst * FLOATS_PER_GAUSSIAN + k] = activated(k, v);
-    } else {
-      new_sh[(size_t)dst * SH_REST_FLOATS + (k - FLOATS_PER_GAUSSIAN)] = value;
     }
   }
 }
 
-// src/shaders/densify.wgsl:148-180, split in two for coalescing. This kernel takes
-// one Gaussian per warp, a moment slot per lane, and copies the Adam moments (kept for a
-// kept Gaussian and a clone's original, zero for new ones), the raw parameters
-// and the SH coefficients; densify_place_kernel then places split children.
-// The identity of each output Gaussian and its learned-densification statistics
-// travel along (slot 0's thread): a kept Gaussian and a clone's original keep
-// theirs, a new Gaussian gets identity first_id + its output index and zeros.
+// src/shaders/densify.wgsl:148-180, split in two for coalescing. Each warp takes
+// 32 consecutive Gaussians at a time: lane l reads the action and output offset
+// of Gaussian l in one coalesced pass, then the warp copies the live ones two at
+// a time, a moment slot per lane (lanes l and l + 32 of the 61; each slot's
+// moment, raw value or SH coefficient is a contiguous run across the lanes), with
+// both Gaussians' reads issued before their writes. densify_place_kernel then
+// places split children.
 __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
                                                            const uint8_t* __restrict__ actions,
                                                            const float* __restrict__ sh,
@@ -193,18 +217,30 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
                                                            uint32_t* __restrict__ new_ids,
                                                            float2* __restrict__ new_aux,
                                                            float* __restrict__ new_gaussians) {
-  // A warp per Gaussian, grid-stride: the action and output offset are read once
-  // per Gaussian, and the 61 slots (lanes l and l + 32) are contiguous runs.
-  const uint32_t lane = threadIdx.x & 31u, warps = gridDim.x * (256u / 32u);
-  for (uint32_t i = blockIdx.x * (256u / 32u) + (threadIdx.x >> 5); i < count; i += warps) {
-    const uint32_t a = actions[i];
-    if (a == 0) continue;
-    const uint32_t o = outputs[i];
-    densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids, new_aux,
-                      new_gaussians, count, new_count, i, lane, a, o);
-    if (lane + 32u < MOMENT_SLOTS)
-      densify_copy_slot(dp, params, sh, moments, ids, aux, first_id, new_params, new_sh, new_moments, new_ids,
-                        new_aux, new_gaussians, count, new_count, i, lane + 32u, a, o);
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t first = warp * 32u; first < count; first += warps * 32u) {
+    const uint32_t mine = first + lane;
+    const uint32_t my_action = mine < count ? actions[mine] : 0u;
+    const uint32_t my_output = my_action ? outputs[mine] : 0u;
+    uint32_t live = __ballot_sync(0xffffffffu, my_action != 0);
+    while (live) {
+      const uint32_t j0 = __ffs(live) - 1;
+      live &= live - 1;
+      const bool two = live != 0;  // the same on every lane
+      const uint32_t j1 = two ? __ffs(live) - 1 : j0;
+      if (two) live &= live - 1;
+      const uint32_t a0 = __shfl_sync(0xffffffffu, my_action, j0), o0 = __shfl_sync(0xffffffffu, my_output, j0);
+      const uint32_t a1 = __shfl_sync(0xffffffffu, my_action, j1), o1 = __shfl_sync(0xffffffffu, my_output, j1);
+      SlotPair s0, s1;
+      densify_load(params, sh, moments, ids, aux, count, first + j0, lane, s0);
+      if (two) densify_load(params, sh, moments, ids, aux, count, first + j1, lane, s1);
+      densify_store(dp, first_id, new_count, a0, o0, lane, s0, new_params, new_sh, new_moments, new_ids, new_aux,
+                    new_gaussians);
+      if (two)
+        densify_store(dp, first_id, new_count, a1, o1, lane, s1, new_params, new_sh, new_moments, new_ids, new_aux,
+                      new_gaussians);
+    }
   }
 }
 
@@ -872,7 +908,7 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   }
   dg_renderer* r = t->renderer;
   DG_LAUNCH(ctx, "densify_copy",
-            densify_copy_kernel<<<std::max(1u, std::min(ceil_div(count, 8), (uint32_t)ctx->sm_count * 8u)), 256, 0,
+            densify_copy_kernel<<<std::max(1u, std::min(ceil_div(count, 256), (uint32_t)ctx->sm_count * 8u)), 256, 0,
                                   ctx->stream>>>(
                 dp, typed<float>(t->params), typed<uint8_t>(actions), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),

@@ -217,6 +217,10 @@ class Device:
         _lib.call("dg_context_launch_count", self.handle, ctypes.byref(out))
         return out.value
 
+    def profile(self, enabled: bool) -> None:
+        """Starts or stops a profiler's collection (for profilers started with it off)."""
+        _lib.call("dg_context_profile", self.handle, int(enabled))
+
     def setKernelTiming(self, enabled: bool) -> None:
         _lib.call("dg_context_set_kernel_timing", self.handle, int(enabled))
 

@@ -71,6 +71,10 @@ dg_status dg_context_launch_count(dg_context* ctx, uint64_t* out);
  * clears) is one line per kernel name: "name launches total_ms". No reference
  * counterpart (the reference only times whole frames, src/checks/tiles.ts:188-218). */
 dg_status dg_context_set_kernel_timing(dg_context* ctx, int32_t enabled);
+/* Marks the work a profiler started with its collection off records: waits for
+ * the context's stream, then starts (enabled = 1) or stops (0) the collection
+ * (cudaProfilerStart / cudaProfilerStop). No reference counterpart. */
+dg_status dg_context_profile(dg_context* ctx, int32_t enabled);
 dg_status dg_context_kernel_timing_report(dg_context* ctx, char* text, uint64_t capacity);
 
 /* ---- events on the context's stream, for timing work enqueued through it
