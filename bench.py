@@ -180,11 +180,12 @@ def build_scene(args):
     return raw, sh, truth_raw, truth_sh, train_cams[: args.views]
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one
-# `ncu --set full --clock-control none` capture of each kernel at 1.1M Gaussians
-# (`python bench.py --steps 2 --warmup 3 --views 8 --no-cpu-baseline --no-graph
-# --no-held-out`, one launch, `-k regex:<kernel> -s 3 -c 1`).
-NCU_TRAFFIC = {"preprocess_backward_adam": 1_950_470_608, "preprocess": 313_713_664}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of each
+# kernel at 1.1M Gaussians, from one ncu capture of the profiled training step:
+# `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+# --clock-control none --profile-from-start off -k regex:<kernel> -c 1
+# python bench.py --workload profile --views 8 --warmup 3`.
+NCU_TRAFFIC = {"preprocess_backward_adam": 1_838_054_656, "preprocess": 313_713_664}
 
 
 # Algorithmic bytes per unit: what each kernel must move at minimum.

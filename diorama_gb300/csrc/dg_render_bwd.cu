@@ -612,7 +612,8 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
   if (threadIdx.x == 0) {
     mbar_init(&s_bar, 1);
     mbar_arrive_expect_tx(&s_bar, quads * 16);
-    bulk_copy_to_shared(s_sh, sh_block, quads * 16, &s_bar);
+    // Kept in L2 for the Adam pass, which reads the coefficients again.
+    bulk_copy_to_shared(s_sh, sh_block, quads * 16, &s_bar, l2_policy_evict_last());
     s_ap = *adam;
   }
   __syncthreads();  // the barrier is initialized before anyone waits on it
@@ -641,6 +642,9 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
   if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, sh_total);
   const AdamParams& ap = s_ap;
   const float inv_bc1 = ap.inv_bias_correction1, inv_sqrt_bc2 = ap.inv_sqrt_bias_correction2;
+  // The streams below are read and written once: evict them first, so the
+  // coefficients staged with evict-last stay in L2 until step 3 reads them again.
+  const uint64_t stream = l2_policy_evict_first();
 
   // 3. The SH slots, four at a time; a thread loads a batch of groups before
   // stepping them, so that enough reads are in flight.
@@ -654,9 +658,9 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
       for (uint32_t u = 0; u < B; u++) {
         const uint32_t q = base + u * PBWD_THREADS;
         if (q < quads) {
-          v[u] = f4_load(sh_block + 4 * q);
-          m0[u] = m_block[2 * q];
-          m1[u] = m_block[2 * q + 1];
+          v[u] = ld_hinted(sh_block + 4 * q, stream);
+          m0[u] = ld_hinted(m_block + 2 * q, stream);
+          m1[u] = ld_hinted(m_block + 2 * q + 1, stream);
         }
       }
 #pragma unroll
@@ -671,9 +675,9 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
           out.y = adam_step_fast(v[u].y, g.y, b, lr, inv_bc1, inv_sqrt_bc2);
           out.z = adam_step_fast(v[u].z, g.z, c, lr, inv_bc1, inv_sqrt_bc2);
           out.w = adam_step_fast(v[u].w, g.w, d, lr, inv_bc1, inv_sqrt_bc2);
-          f4_store(sh_block + 4 * q, out);
-          m_block[2 * q] = make_float4(a.x, a.y, b.x, b.y);
-          m_block[2 * q + 1] = make_float4(c.x, c.y, d.x, d.y);
+          st_hinted(sh_block + 4 * q, out, stream);
+          st_hinted(m_block + 2 * q, make_float4(a.x, a.y, b.x, b.y), stream);
+          st_hinted(m_block + 2 * q + 1, make_float4(c.x, c.y, d.x, d.y), stream);
         }
       }
     }
@@ -701,9 +705,9 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
       for (uint32_t u = 0; u < B; u++) {
         const uint32_t q = base + u * PBWD_THREADS;
         if (q < p_quads) {
-          x[u] = f4_load(p_block + 4 * q);
-          m0[u] = m_block[2 * q];
-          m1[u] = m_block[2 * q + 1];
+          x[u] = ld_hinted(p_block + 4 * q, stream);
+          m0[u] = ld_hinted(m_block + 2 * q, stream);
+          m1[u] = ld_hinted(m_block + 2 * q + 1, stream);
         }
       }
 #pragma unroll
@@ -724,10 +728,10 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
               xs[j] = adam_param_slot(ap, k, xs[j], grad[j], ms[j], act[j]);
             }
           }
-          f4_store(p_block + 4 * q, make_float4(xs[0], xs[1], xs[2], xs[3]));
-          m_block[2 * q] = make_float4(ms[0].x, ms[0].y, ms[1].x, ms[1].y);
-          m_block[2 * q + 1] = make_float4(ms[2].x, ms[2].y, ms[3].x, ms[3].y);
-          f4_store(a_block + 4 * q, make_float4(act[0], act[1], act[2], act[3]));
+          st_hinted(p_block + 4 * q, make_float4(xs[0], xs[1], xs[2], xs[3]), stream);
+          st_hinted(m_block + 2 * q, make_float4(ms[0].x, ms[0].y, ms[1].x, ms[1].y), stream);
+          st_hinted(m_block + 2 * q + 1, make_float4(ms[2].x, ms[2].y, ms[3].x, ms[3].y), stream);
+          st_hinted(a_block + 4 * q, make_float4(act[0], act[1], act[2], act[3]), stream);
         }
       }
     }
