@@ -54,3 +54,18 @@ def test_null_arguments_fail_with_a_status():
     assert b"NULL" in lib.dg_last_error()
     out = ctypes.c_void_p()
     assert lib.dg_renderer_create(None, 0, ctypes.byref(out)) == _lib.DG_ERROR_INVALID_ARGUMENT
+
+
+def test_node_addon_calls_only_declared_entry_points():
+    """The Node-API addon (diorama_gb300/node/diorama.cc; not compiled here: node
+    is absent) wraps only functions the header declares, and the TypeScript shims
+    call only functions the addon registers."""
+    root = HEADER.parent.parent / "diorama_gb300" / "node"
+    addon = (root / "diorama.cc").read_text()
+    called = set(re.findall(r"\b(dg_[a-z0-9_]+)\s*\(", addon))
+    assert called and called <= set(declared_functions()), called - set(declared_functions())
+    registered = set(re.findall(r'\{"([a-zA-Z]+)", nullptr,', addon))
+    used = set()
+    for ts in (root / "ts").glob("*.ts"):
+        used |= set(re.findall(r"native\.([a-zA-Z]+)\(", ts.read_text()))
+    assert used and used <= registered, used - registered
