@@ -873,9 +873,11 @@ dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splat
   if (st == DG_OK) st = alloc_buffer(ctx, scan_scratch_bytes(std::max(count, 1u)), &tr->scan_scratch);
   if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->raster_params);
   if (st == DG_OK) st = alloc_buffer(ctx, 16, &tr->work);
-  if (st == DG_OK && cudaMallocHost(&tr->pinned_total, 4) != cudaSuccess) st = fail(DG_ERROR_OUT_OF_MEMORY, "pinned");
-  if (st == DG_OK && cudaEventCreateWithFlags(&tr->readback_event, cudaEventDisableTiming) != cudaSuccess)
-    st = fail(DG_ERROR_CUDA, "event");
+  if (st == DG_OK && cudaMallocHost(&tr->pinned_totals, 4 * dg_tile_rasterizer::READBACKS) != cudaSuccess)
+    st = fail(DG_ERROR_OUT_OF_MEMORY, "pinned");
+  for (uint32_t k = 0; k < dg_tile_rasterizer::READBACKS && st == DG_OK; k++)
+    if (cudaEventCreateWithFlags(&tr->readback_events[k], cudaEventDisableTiming) != cudaSuccess)
+      st = fail(DG_ERROR_CUDA, "event");
   uint32_t capacity = initial_pair_capacity ? initial_pair_capacity : std::max(1u << 16, count * 8u);
   if (st == DG_OK) st = make_pairs(tr, capacity);
   tr->depth_first = depth_first;
@@ -1098,11 +1100,40 @@ dg_buffer* rasterizer_sorted_keys(dg_tile_rasterizer* tr) {
   return tr->keys64;
 }
 
+// Consumes the queued readbacks whose copies are done (all of them with `wait`),
+// oldest first, growing the pair buffers when a frame needed more pairs than
+// they hold: the reference's afterSubmit (src/tileRasterizer.ts:229-244), whose
+// promise resolves for every frame.
+static dg_status consume_readbacks(dg_tile_rasterizer* tr, bool wait) {
+  constexpr uint32_t R = dg_tile_rasterizer::READBACKS;
+  while (tr->readback_tail != tr->readback_head) {
+    cudaEvent_t e = tr->readback_events[tr->readback_tail % R];
+    if (!wait && cudaEventQuery(e) == cudaErrorNotReady) break;
+    DG_CUDA(cudaEventSynchronize(e));
+    tr->last_pair_count = tr->pinned_totals[tr->readback_tail % R];
+    tr->readback_tail++;
+    DG_TRY(rasterizer_reserve_pairs(tr, tr->last_pair_count));
+  }
+  return DG_OK;
+}
+
+dg_status rasterizer_reserve_pairs(dg_tile_rasterizer* tr, uint64_t pairs) {
+  if (pairs <= tr->pair_capacity) return DG_OK;
+  const double want = std::ceil(std::log2((double)pairs * 1.25));
+  DG_REQUIRE(want < 30, "the frame needs more pairs than the sort can hold");
+  return make_pairs(tr, 1u << (uint32_t)want);
+}
+
 dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr) {
-  if (tr->readback_state != 0) return DG_OK;
-  DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, tr->ctx->stream));
-  DG_CUDA(cudaEventRecord(tr->readback_event, tr->ctx->stream));
-  tr->readback_state = 1;
+  constexpr uint32_t R = dg_tile_rasterizer::READBACKS;
+  if (tr->readback_head - tr->readback_tail == R) {  // full: the oldest first
+    DG_CUDA(cudaEventSynchronize(tr->readback_events[tr->readback_tail % R]));
+    DG_TRY(consume_readbacks(tr, false));
+  }
+  const uint32_t slot = tr->readback_head % R;
+  DG_CUDA(cudaMemcpyAsync(tr->pinned_totals + slot, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, tr->ctx->stream));
+  DG_CUDA(cudaEventRecord(tr->readback_events[slot], tr->ctx->stream));
+  tr->readback_head++;
   return DG_OK;
 }
 
@@ -1226,17 +1257,7 @@ dg_status dg_tile_rasterizer_encode_backward(dg_tile_rasterizer* tr, const float
 
 dg_status dg_tile_rasterizer_after_submit(dg_tile_rasterizer* tr, int32_t wait) {
   DG_REQUIRE(tr, "NULL argument");
-  if (tr->readback_state != 1) return DG_OK;
-  if (!wait && cudaEventQuery(tr->readback_event) == cudaErrorNotReady) return DG_OK;
-  DG_CUDA(cudaEventSynchronize(tr->readback_event));
-  tr->last_pair_count = *tr->pinned_total;
-  tr->readback_state = 0;
-  if (tr->last_pair_count > tr->pair_capacity) {
-    double want = std::ceil(std::log2((double)tr->last_pair_count * 1.25));
-    DG_REQUIRE(want < 30, "the frame needs more pairs than the sort can hold");
-    DG_TRY(make_pairs(tr, 1u << (uint32_t)want));
-  }
-  return DG_OK;
+  return consume_readbacks(tr, wait != 0);
 }
 
 uint32_t dg_tile_rasterizer_last_pair_count(const dg_tile_rasterizer* tr) { return tr ? tr->last_pair_count : 0; }
@@ -1257,11 +1278,12 @@ dg_status dg_tile_rasterizer_destroy(dg_tile_rasterizer* tr) {
                        tr->counts_sorted, tr->keys64, tr->work, tr->work_plan, tr->chunks, tr->checkpoints,
                        tr->blend_mask})
     free_buffer(b);
-  if (tr->readback_event) {
-    cudaEventSynchronize(tr->readback_event);
-    cudaEventDestroy(tr->readback_event);
-  }
-  if (tr->pinned_total) cudaFreeHost(tr->pinned_total);
+  for (cudaEvent_t e : tr->readback_events)
+    if (e) {
+      cudaEventSynchronize(e);
+      cudaEventDestroy(e);
+    }
+  if (tr->pinned_totals) cudaFreeHost(tr->pinned_totals);
   delete tr;
   return DG_OK;
 }

@@ -26,10 +26,13 @@ struct dg_tile_rasterizer {
   dg_buffer* pixel_color;
   dg_buffer* pixel_last;
   uint32_t pixel_count;
-  // Pair-count readback (src/tileRasterizer.ts:187-191, 229-244)
-  uint32_t* pinned_total;
-  cudaEvent_t readback_event;
-  int readback_state;  // 0 idle, 1 queued
+  // Pair-count readbacks (src/tileRasterizer.ts:187-191, 229-244): a ring of
+  // READBACKS pinned words, each with the event its copy completes, queued one
+  // per frame and consumed in order, [readback_tail, readback_head).
+  static constexpr uint32_t READBACKS = 4;
+  uint32_t* pinned_totals;
+  cudaEvent_t readback_events[READBACKS];
+  uint32_t readback_head, readback_tail;
   uint32_t last_pair_count;
   uint32_t tiles_x, tiles_y;
   float viewport[2];
@@ -61,7 +64,11 @@ dg_status rasterizer_prepare(dg_tile_rasterizer* tr, const float viewport[2], co
 // The frame's kernels. counts_ready: tile_offsets already hold the per-splat
 // tile counts (the renderer's preprocess writes them), so count_tiles is skipped.
 dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool counts_ready);
+// Queues this frame's pair-count readback (waiting for the oldest queued one first
+// if the ring is full). Not while a graph is being captured.
 dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr);
+// Grows the pair buffers to 2^ceil(log2(1.25 * pairs)) if pairs exceed them.
+dg_status rasterizer_reserve_pairs(dg_tile_rasterizer* tr, uint64_t pairs);
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
                             uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);

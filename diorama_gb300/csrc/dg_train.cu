@@ -536,9 +536,6 @@ static dg_status launch_step(dg_trainer* t, bool with_adam) {
                                            typed<float2>(t->aux), t->keep_gradients));
   else
     DG_TRY(launch_stats(t));
-  // The frame's pair count, for afterSubmit (src/tileRasterizer.ts:187-191).
-  dg_tile_rasterizer* tr = r->rasterizer;
-  DG_CUDA(cudaMemcpyAsync(tr->pinned_total, tr->scan_total->ptr, 4, cudaMemcpyDeviceToHost, t->ctx->stream));
   return DG_OK;
 }
 
@@ -745,9 +742,11 @@ dg_status dg_trainer_optimize(dg_trainer* t) {
   } else {
     DG_TRY(launch_step(t, !densify_now));
   }
+  // The frame's pair count, for afterSubmit (src/tileRasterizer.ts:187-191): queued
+  // after the step (outside any captured graph), consumed once it has arrived; a
+  // frame that needed more pairs than the buffers hold grows them for the next.
   dg_tile_rasterizer* tr = r->rasterizer;
-  DG_CUDA(cudaEventRecord(tr->readback_event, t->ctx->stream));
-  tr->readback_state = 1;
+  DG_TRY(rasterizer_queue_readback(tr));
   DG_TRY(dg_tile_rasterizer_after_submit(tr, 0));
   t->due_densify = densify_now;
   t->due_reset = densifying && it % s.opacity_reset_interval == 0;
@@ -918,9 +917,17 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
             densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
                 dp, typed<float>(t->params), typed<uint8_t>(actions), typed<uint32_t>(outputs), count,
                 typed<float>(params), typed<float>(gaussians)));
+  // The last frame's pair count (every queued readback has arrived: the counts
+  // above were read back), scaled to the new count with 10% to spare, sizes the
+  // new set's pair buffers, so the frames after a densification do not overflow
+  // them while their own readbacks are in flight (the reference grows them a
+  // frame or two later, after such a frame, src/tileRasterizer.ts:229-244).
+  st = dg_tile_rasterizer_after_submit(r->rasterizer, 1);
+  const double last_pairs = r->rasterizer ? (double)r->rasterizer->last_pair_count : 0.0;
   // Hand the new set to the renderer; the old buffers go once the work above is done.
   drop_graph(t);
-  st = dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree);
+  if (st == DG_OK) st = dg_renderer_adopt_gaussians(r, new_count, gaussians, sh, t->sh_degree);
+  if (st == DG_OK) st = rasterizer_reserve_pairs(r->rasterizer, (uint64_t)(last_pairs * new_count / count * 1.1));
   if (st == DG_OK) st = renderer_ensure_gradients(r);
   if (t->log_enabled && st == DG_OK) {
     DG_CUDA(cudaStreamSynchronize(ctx->stream));

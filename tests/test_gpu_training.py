@@ -343,3 +343,36 @@ def test_host_photos_match_device_images(device):
         p.free()
     for v in views:
         v.image.destroy()
+
+
+def test_pair_buffers_grow_while_training_runs_ahead(device):
+    """A training loop that never waits for the GPU still grows the pair buffers
+    once a frame needs more pairs than they hold (the reference's afterSubmit
+    resolves for every frame, src/tileRasterizer.ts:229-244): every step queues its
+    pair-count readback, and later steps consume the ones that have arrived.
+    100 large Gaussians at 512x512 need ~10^5 pairs against the initial 2^16."""
+    rng = np.random.default_rng(3)
+    n = 100
+    params = np.zeros((n, 16), np.float32)
+    params[:, 0:3] = rng.uniform(-0.6, 0.6, (n, 3))
+    params[:, 3] = 1.0
+    params[:, 4:7] = np.log(0.6)
+    params[:, 8] = 1.0
+    params[:, 12:15] = rng.uniform(-1, 1, (n, 3))
+    cams = [CameraData(lookAt([3 * math.sin(a), 0.5, 3 * math.cos(a)], [0, 0, 0], [0, 1, 0]),
+                       perspective(math.pi / 3, 1, 0.1, 100), (512, 512)) for a in (0.0, 2.0)]
+    photos = [device.createTexture(512, 512) for _ in cams]
+    views = [TrainingView(f"view {k}", c, p) for k, (c, p) in enumerate(zip(cams, photos))]
+    t = Trainer(device, RawGaussians(params.reshape(-1), np.zeros(n * 45, np.float32)), views,
+                replace(DEFAULT_SETTINGS, extent=3.0, densifyUntil=0))
+    t.setGraph(True)
+    for _ in range(12):
+        t.step()
+    tiles = t.renderer.tiles
+    grown = tiles.pairCapacity  # before any wait: grown by the loop itself
+    t.renderer.afterSubmit()
+    assert tiles.lastPairCount > 1 << 16, tiles.lastPairCount
+    assert grown >= tiles.lastPairCount, (grown, tiles.lastPairCount)
+    t.destroy()
+    for p in photos:
+        p.destroy()
