@@ -65,8 +65,14 @@ def parse():
                          "starting Gaussians' nearest-neighbour distances of a point cloud; profile: one training "
                          "step bracketed for a profiler started with collection off")
     ap.add_argument("--knn-points", type=int, default=1_100_000, help="knn workload: points in the cloud")
-    ap.add_argument("--train-steps", type=int, default=30_000, help="densify workload: steps per training run")
-    ap.add_argument("--plain-runs", type=int, default=3, help="densify workload: seeded plain runs that log labels")
+    ap.add_argument("--densify-steps", type=int, default=15_000,
+                    help="learned-vs-plain comparison: steps per training run (the reference's 30,000-step "
+                         "schedule scaled to this)")
+    ap.add_argument("--densify-threshold", type=float, default=1.5e-5,
+                    help="learned-vs-plain comparison: the densification gradient threshold")
+    ap.add_argument("--densify-seeds", type=int, default=3, help="learned-vs-plain comparison: starting sets")
+    ap.add_argument("--no-densify-comparison", action="store_true",
+                    help="train workload: leave out the learned-vs-plain comparison (minutes)")
     ap.add_argument("--unbalanced", action="store_true",
                     help="densify workload: plain cross-entropy (by default both labels weigh the same: ~98%% of "
                          "children survive, and unweighted the model only learns that)")
@@ -112,7 +118,8 @@ def config(args, world):
         "viewport": [980, 545],
         "training_views": args.views,
         "sh_degree": 3,
-        "densify": "off in the timed steps (steady state past step 15,000)",
+        "densify": "off in the timed steps (steady state past step 15,000); the learned-vs-plain comparison "
+                   "(densify_comparison) trains its own runs after the timed steps",
         "l2": "working set ~3 GB > 129 MB L2; no flush needed",
         "parallelism": f"replicas x{world}",
     }
@@ -381,6 +388,10 @@ def run_ours(args, rank, world, local, group):
         v.image.destroy()
     for p in pinned:
         p.free()
+    # The benchmark spec's second measure: learned against plain densification at the
+    # ~1.1M-Gaussian scale (rank 0 of a replica run; minutes).
+    if rank == 0 and not args.no_densify_comparison:
+        result["densify_comparison"] = densify_comparison(device, args)
     device.destroy()
     return result
 
@@ -738,22 +749,56 @@ def run_knn(args, rank, local):
     return result
 
 
-def run_densify_experiment(args, rank, local):
-    """The planes-and-boxes scene (500k ground-truth Gaussians,
-    263 training and 37 held-out 980x545 views), trained from 100k noisy surface
-    samples. Seeded plain runs log each clone/split candidate's features and
-    whether its children survive pruning 1,000 steps later; the model (MLP 12 ->
-    64 -> 64 -> 2, BF16, AdamW lr 1e-3, 5 epochs) learns from those labels; then a
-    plain and a learned run from the same start are compared on held-out PSNR and
-    SSIM, Gaussian count, training wall time and time to reach the plain run's
-    final held-out PSNR minus 0.1 dB (first reached, and for good: the opacity
-    resets every 3,000 steps pull the PSNR down until densification ends)."""
-    if rank != 0:
-        return None
-    from diorama_gb300 import (DEFAULT_SETTINGS, DensifyMLP, Device, GaussianRenderer, RawGaussians, Trainer,
-                               TrainingView, activate, scenes)
+def densify_schedule(steps: int, threshold: float):
+    """The reference's schedule (src/trainer.ts:65-82, densification from step 500
+    to 15,000 every 100 steps, opacity reset every 3,000, SH degree +1 every
+    1,000, position learning rate decaying over 30,000 steps) scaled to `steps`,
+    on the planes-and-boxes scene's extent 4 with config 1's opacity lr 5e-2 and
+    the given gradient threshold. Returns the settings and the label horizon (1,000
+    steps, scaled)."""
+    from diorama_gb300 import DEFAULT_SETTINGS
 
-    device = Device(local)
+    f = steps / 30_000
+    settings = replace(DEFAULT_SETTINGS, extent=4.0, opacityLr=0.05, densifyGradThreshold=threshold,
+                       positionLrSteps=steps, shDegreeInterval=max(1, round(1000 * f)),
+                       densifyFrom=round(500 * f), densifyUntil=round(15_000 * f),
+                       densifyInterval=max(1, round(100 * f)), opacityResetInterval=max(1, round(3000 * f)))
+    return settings, max(1, round(1000 * f))
+
+
+def time_to_target(curve: list, target: float):
+    """Training seconds at the first evaluation from which the held-out PSNR stays
+    at or above the target (the opacity resets pull it down while densifying)."""
+    at = None
+    for step, seconds, psnr, _count in curve:
+        if psnr < target:
+            at = None
+        elif at is None:
+            at = seconds
+    return at
+
+
+def densify_comparison(device, args) -> dict:
+    """Learned against plain densification (configs 1 and 4) on the
+    planes-and-boxes scene: 500k ground-truth Gaussians on 40 planes and boxes,
+    263 training and 37 held-out 980x545 views, training from 100k noisy surface
+    samples on the reference's schedule scaled to --densify-steps, with
+    densification threshold --densify-threshold (1.5e-5 by default: the plain
+    path grows to ~1.2M Gaussians).
+
+    For each of --densify-seeds starting sets: a plain run that logs every
+    clone/split candidate's 12 features and whether any of its children is still
+    alive a (scaled) 1,000 steps later; then a model (MLP 12 -> 64 -> 64 -> 2,
+    BF16 tensor-core kernels, AdamW lr 1e-3, 5 epochs, both labels weighted
+    equally) trained on the OTHER seeds' labels, and a learned run from the same
+    start, in which the model decides the plain rule's candidates where it is
+    confident (max(p, 1 - p) >= 0.6) and the threshold rule decides the rest.
+    Per seed: held-out PSNR and SSIM, final Gaussians, training wall time
+    (evaluations excluded) and the time to reach, for good, the plain run's final
+    PSNR minus 0.1 dB; across seeds, their means and ranges."""
+    from diorama_gb300 import DensifyMLP, GaussianRenderer, RawGaussians, Trainer, TrainingView, activate, scenes
+
+    steps, threshold, seeds = args.densify_steps, args.densify_threshold, list(range(1, args.densify_seeds + 1))
     truth_raw, truth_sh = scenes.surface_scene(GROUND_TRUTH, TRUTH_SEED)
     train_cams, held_cams = scenes.ring_cameras()
     W, H = train_cams[0].viewport
@@ -771,20 +816,18 @@ def run_densify_experiment(args, rank, local):
     train_views, held_views = photos(train_cams, "train"), photos(held_cams, "held-out")
     device.synchronize()
     photographer.destroy()
-    settings = replace(DEFAULT_SETTINGS, extent=4.0, opacityLr=0.05)
-    steps = args.train_steps
-    every = max(100, steps // 30)
+    settings, horizon = densify_schedule(steps, threshold)
+    every = max(1, steps // 20)
 
     def run(seed, mlp=None, log=False):
         raw, sh = scenes.surface_scene(100_000, seed, noise=0.01)
         t = Trainer(device, RawGaussians(raw.reshape(-1), sh.reshape(-1)), train_views, settings)
         t.setGraph(True)
         if log:
-            t.setDensifyLog(True, 1000)
+            t.setDensifyLog(True, horizon)
         if mlp is not None:
             t.setDensifyMLP(mlp, 0.6)
-        curve, train_s = [], 0.0
-        done = 0
+        curve, train_s, done = [], 0.0, 0
         while done < steps:
             n = min(every, steps - done)
             device.synchronize()
@@ -794,77 +837,114 @@ def run_densify_experiment(args, rank, local):
             device.synchronize()
             train_s += time.perf_counter() - t0
             done += n
-            curve.append({"step": done, "train_s": round(train_s, 3), "psnr": round(t.evaluate(held_views, False)["psnr"], 3),
-                          "gaussians": t.count})
+            curve.append([done, round(train_s, 3), round(t.evaluate(held_views, False)["psnr"], 3), t.count])
         final = t.evaluate(held_views, True)
-        start = time.perf_counter()
-        reps = 3
-        for _ in range(reps):
-            t.evaluate(held_views, False)
-        eval_fps = len(held_views) * reps / (time.perf_counter() - start)
-        result = {"seed": seed, "steps": steps, "train_s": round(train_s, 2), "steps_per_s": round(steps / train_s, 1),
+        result = {"seed": seed, "train_s": round(train_s, 2), "steps_per_s": round(steps / train_s, 1),
                   "psnr": round(final["psnr"], 3), "ssim": round(final["ssim"], 4), "gaussians": t.count,
-                  "densifications": len(t.densifications), "held_out_eval_frames_per_s": round(eval_fps, 1),
-                  "curve": curve}
-        samples = t.takeDensifySamples() if log else None
+                  "densifications": len(t.densifications), "curve": curve}
+        if log:
+            f, y, pending = t.takeDensifySamples()
+            result["logged"] = {"samples": int(y.size), "children_alive_rate": round(float(y.mean()), 4)
+                                if y.size else None, "unlabelled": pending}
+        else:
+            f = y = None
         if mlp is not None:
             result["mlp"] = t.densifyMLPStats
         t.destroy()
-        return result, samples
+        return result, f, y
 
-    logged, features, labels = [], [], []
-    for seed in range(1, args.plain_runs + 1):
-        result, (f, y, pending) = run(seed, log=True)
-        logged.append({k: result[k] for k in ("seed", "psnr", "ssim", "gaussians", "train_s")} |
-                      {"samples": int(y.size), "survived": float(y.mean()) if y.size else None, "unlabelled": pending})
-        features.append(f)
-        labels.append(y)
-    features, labels = np.concatenate(features), np.concatenate(labels)
-    mlp = DensifyMLP(device, seed=7)
-    t0 = time.perf_counter()
-    losses = mlp.train(features, labels, epochs=5, batch=1024, lr=1e-3, weightDecay=0.01, seed=7,
-                       balanceClasses=not args.unbalanced)
-    device.synchronize()
-    train_mlp_s = time.perf_counter() - t0
-    accuracy = float(np.mean((mlp.predictHost(features) >= 0.5) == (labels == 1)))
-    eval_seed = args.plain_runs + 1
-    plain, _ = run(eval_seed)
-    learned, _ = run(eval_seed, mlp=mlp)
-    target = plain["psnr"] - 0.1
+    plain, samples = {}, {}
+    for seed in seeds:
+        plain[seed], f, y = run(seed, log=True)
+        samples[seed] = (f, y)
+    learned, models = {}, {}
+    for seed in seeds:
+        others = [o for o in seeds if o != seed] or [seed]
+        f = np.concatenate([samples[o][0] for o in others])
+        y = np.concatenate([samples[o][1] for o in others])
+        mlp = DensifyMLP(device, seed=7)
+        t0 = time.perf_counter()
+        losses = mlp.train(f, y, epochs=5, batch=1024, lr=1e-3, weightDecay=0.01, seed=7,
+                           balanceClasses=not args.unbalanced)
+        device.synchronize()
+        fit_s = time.perf_counter() - t0
+        # Inference time on every candidate of one run (the model runs once per
+        # densification, on that densification's candidates), CUDA events.
+        fb = device.upload(np.ascontiguousarray(samples[seed][0], np.float32))
+        out = device.createBuffer(max(4, samples[seed][1].size * 4))
+        mlp.predict(fb, samples[seed][1].size, out)
+        start, end = device.event(), device.event()
+        start.record()
+        for _ in range(10):
+            mlp.predict(fb, samples[seed][1].size, out)
+        end.record()
+        predict_us = start.elapsed_ms(end) * 100.0  # per call
+        accuracy = float(np.mean((mlp.predictHost(samples[seed][0]) >= 0.5) == (samples[seed][1] == 1)))
+        fb.destroy()
+        out.destroy()
+        learned[seed], _, _ = run(seed, mlp=mlp)
+        models[seed] = {"trained_on_seeds": others, "samples": int(y.size), "loss": [round(x, 4) for x in losses],
+                        "fit_s": round(fit_s, 3), "accuracy_on_this_seed": round(accuracy, 4),
+                        "predict_us_for_all_candidates_of_a_run": round(predict_us, 1),
+                        "candidates_per_run": int(samples[seed][1].size)}
+        mlp.destroy()
+    per_seed = []
+    for seed in seeds:
+        p, q = plain[seed], learned[seed]
+        target = p["psnr"] - 0.1
+        per_seed.append({
+            "seed": seed, "target_psnr": round(target, 3),
+            "plain": {k: p[k] for k in ("psnr", "ssim", "gaussians", "train_s", "steps_per_s", "logged")}
+            | {"time_to_target_s": time_to_target(p["curve"], target)},
+            "learned": {k: q[k] for k in ("psnr", "ssim", "gaussians", "train_s", "steps_per_s", "mlp")}
+            | {"time_to_target_s": time_to_target(q["curve"], target)},
+            "model": models[seed],
+            "curves": {"plain": p["curve"], "learned": q["curve"]}})
 
-    def time_to(curve):
-        for c in curve:
-            if c["psnr"] >= target:
-                return c["train_s"]
-        return None
+    def stats(values):
+        values = [v for v in values if v is not None]
+        if not values:
+            return None
+        return {"mean": round(float(np.mean(values)), 4), "min": round(float(min(values)), 4),
+                "max": round(float(max(values)), 4)}
 
-    def time_to_sustained(curve):
-        # From the first evaluation after which the PSNR never drops below the target.
-        at = None
-        for c in curve:
-            if c["psnr"] < target:
-                at = None
-            elif at is None:
-                at = c["train_s"]
-        return at
+    def ratio(a, b):
+        return a / b if a is not None and b else None
 
-    for r in (plain, learned):
-        r["time_to_target_s"] = time_to(r["curve"])
-        r["time_to_sustained_target_s"] = time_to_sustained(r["curve"])
-    mlp.destroy()
+    summary = {
+        "psnr_learned_minus_plain_db": stats([r["learned"]["psnr"] - r["plain"]["psnr"] for r in per_seed]),
+        "ssim_learned_minus_plain": stats([r["learned"]["ssim"] - r["plain"]["ssim"] for r in per_seed]),
+        "gaussians_learned_over_plain": stats([r["learned"]["gaussians"] / r["plain"]["gaussians"] for r in per_seed]),
+        "train_s_learned_over_plain": stats([r["learned"]["train_s"] / r["plain"]["train_s"] for r in per_seed]),
+        "time_to_target_learned_over_plain": stats(
+            [ratio(r["learned"]["time_to_target_s"], r["plain"]["time_to_target_s"]) for r in per_seed]),
+        "learned_within_0.1_db_or_better": sum(r["learned"]["psnr"] >= r["target_psnr"] for r in per_seed),
+        "seeds": len(per_seed),
+    }
     for v in train_views + held_views:
         v.image.destroy()
+    return {"metric": "time to held-out PSNR, learned vs plain densify", "unit": "s",
+            "workload": f"planes-and-boxes scene (500k ground truth), 263 + 37 views at 980x545, {steps} steps "
+                        f"from 100k noisy surface samples, densify threshold {threshold:g} (the reference's "
+                        f"30,000-step schedule scaled by {steps / 30_000:g})",
+            "schedule": {"steps": steps, "densify_from": settings.densifyFrom, "densify_until": settings.densifyUntil,
+                         "densify_interval": settings.densifyInterval,
+                         "opacity_reset_interval": settings.opacityResetInterval,
+                         "sh_degree_interval": settings.shDegreeInterval, "label_horizon": horizon,
+                         "grad_threshold": threshold, "opacity_lr": settings.opacityLr},
+            "summary": summary, "per_seed": per_seed}
+
+
+def run_densify_experiment(args, rank, local):
+    """--workload densify: the learned-vs-plain comparison alone."""
+    if rank != 0:
+        return None
+    from diorama_gb300 import Device
+
+    device = Device(local)
+    result = densify_comparison(device, args)
     device.destroy()
-    return {
-        "metric": "time to held-out PSNR, learned vs plain densify", "unit": "s",
-        "workload": "planes-and-boxes scene (500k ground truth), 263 + 37 views at 980x545, "
-                    f"{steps} steps from 100k noisy surface samples", "target_psnr": round(target, 3),
-        "plain_runs_logged": logged, "samples": int(labels.size), "survived_rate": float(labels.mean()),
-        "mlp": {"epochs": 5, "batch": 1024, "lr": 1e-3, "weight_decay": 0.01, "balanced_classes": not args.unbalanced,
-                "losses": [round(x, 5) for x in losses],
-                "train_accuracy": round(accuracy, 4), "train_s": round(train_mlp_s, 3)},
-        "plain": plain, "learned": learned,
-    }
+    return result
 
 
 def free_port() -> int:
