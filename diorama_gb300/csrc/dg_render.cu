@@ -561,9 +561,12 @@ struct PixelBlend {
       done = true;
       return false;
     }
-    r = r + c.x * alpha * T;
-    g = g + c.y * alpha * T;
-    b = b + c.z * alpha * T;
+    // color += c alpha T (src/shaders/rasterize.wgsl:88) as c (alpha T) + color,
+    // one fused multiply-add per channel (the oracle's same sequence).
+    const float w = __fmul_rn(alpha, T);
+    r = __fmaf_rn(c.x, w, r);
+    g = __fmaf_rn(c.y, w, g);
+    b = __fmaf_rn(c.z, w, b);
     T = remaining;
     last = pos + 1;
     return true;

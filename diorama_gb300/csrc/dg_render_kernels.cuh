@@ -203,14 +203,16 @@ __device__ __forceinline__ void sh_basis_gradient(const float d[3], float g[15][
 
 // ------------------------------------------------------------------ blending
 // The exponent of a splat at a pixel, `power = -0.5 (a dx^2 + c dy^2) - b dx dy`
-// (src/shaders/rasterize.wgsl:68), from A = -0.5 a and C = -0.5 c. Scaling by
-// -0.5 is exact, so ((A dx) dx + (C dy) dy) equals -0.5 ((a dx) dx + (c dy) dy)
-// bit for bit. Written with round-to-nearest intrinsics, which the compiler never
-// fuses, so the forward and backward passes compute identical powers whatever
-// their --fmad setting.
+// (src/shaders/rasterize.wgsl:68), from A = -0.5 a and C = -0.5 c (exact
+// scalings), evaluated as dx (A dx - b dy) + (C dy) dy: three products and two
+// fused multiply-adds instead of five products and three sums (WGSL leaves
+// contraction to the implementation; the oracle evaluates this same sequence).
+// Written with round-to-nearest intrinsics, which the compiler neither fuses
+// further nor splits, so the forward and backward passes compute identical powers
+// whatever their --fmad setting.
 __device__ __forceinline__ float blend_power(float A, float b, float C, float dx, float dy) {
-  const float s = __fadd_rn(__fmul_rn(__fmul_rn(A, dx), dx), __fmul_rn(__fmul_rn(C, dy), dy));
-  return __fsub_rn(s, __fmul_rn(__fmul_rn(b, dx), dy));
+  const float t = __fmaf_rn(A, dx, -__fmul_rn(b, dy));
+  return __fmaf_rn(t, dx, __fmul_rn(__fmul_rn(C, dy), dy));
 }
 
 // A power below which alpha = opacity * exp(power) is certainly under 1/255, so

@@ -457,7 +457,19 @@ static uint8_t to_unorm8(float v) {
   return (uint8_t)rintf(c * 255.0f);
 }
 
-/* src/shaders/rasterize.wgsl:32-100. pixel_color is vec4 per pixel, rgba8 may be NULL. */
+/* power = -0.5 (a dx^2 + c dy^2) - b dx dy (src/shaders/rasterize.wgsl:68) as
+ * dx (A dx - b dy) + (C dy) dy, A = -0.5 a and C = -0.5 c (exact scalings), with
+ * two fused multiply-adds: the kernels' sequence (WGSL leaves contraction to the
+ * implementation), so both round alike. */
+static float blend_power(const float* s, float dx, float dy) {
+  const float A = -0.5f * s[4], C = -0.5f * s[6];
+  const float t = fmaf(A, dx, -(s[5] * dy));
+  return fmaf(t, dx, (C * dy) * dy);
+}
+
+/* src/shaders/rasterize.wgsl:32-100. pixel_color is vec4 per pixel, rgba8 may be NULL.
+ * The colour accumulates as c (alpha T) + colour, one fused multiply-add per
+ * channel, as the kernels do. */
 void or_rasterize(const float* cam, const float* bg, const float* splats, const uint32_t* pair_splats,
                   const uint32_t* ranges, float* pixel_color, uint32_t* pixel_last, uint8_t* rgba8) {
   uint32_t tiles[2];
@@ -480,15 +492,16 @@ void or_rasterize(const float* cam, const float* bg, const float* splats, const 
           const float* s = splats + (size_t)pair_splats[k] * FPS;
           visited++;
           float dx = cx - s[0], dy = cy - s[1];
-          float power = -0.5f * (s[4] * dx * dx + s[6] * dy * dy) - s[5] * dx * dy;
+          float power = blend_power(s, dx, dy);
           if (power > 0.0f) continue;
           float alpha = minf(0.99f, s[11] * dg_exp_ref(power));
           if (alpha < 1.0f / 255.0f) continue;
           float remaining = T * (1.0f - alpha);
           if (remaining < 0.0001f) break;
-          r = r + s[8] * alpha * T;
-          g = g + s[9] * alpha * T;
-          b = b + s[10] * alpha * T;
+          const float w = alpha * T;
+          r = fmaf(s[8], w, r);
+          g = fmaf(s[9], w, g);
+          b = fmaf(s[10], w, b);
           T = remaining;
           last = visited;
         }
@@ -569,7 +582,7 @@ void or_rasterize_backward(const float* cam, const float* bg, const float* splat
         for (int v = 0; v < 9; v++) share[t][v] = 0.0f;
         if (!(inside[t] && j < last[t])) continue;
         float dx = cxs[t] - s[0], dy = cys[t] - s[1];
-        float power = -0.5f * (s[4] * dx * dx + s[6] * dy * dy) - s[5] * dx * dy;
+        float power = blend_power(s, dx, dy);
         if (!(power <= 0.0f)) continue;
         float G = dg_exp_ref(power);
         float alpha = minf(0.99f, s[11] * G);
