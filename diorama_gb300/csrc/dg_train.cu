@@ -62,26 +62,34 @@ __global__ void stats_kernel(const AdamParams* __restrict__ ap, const float* __r
   accumulate_stats_one(ap->viewport, splats, splat_grads, stats, aux, i);
 }
 
-// What happens to Gaussian i (src/shaders/densify.wgsl:72-85): 0 drop, 1 keep, 2 clone, 3 split.
-// With a veto (the learned proposal's), a candidate the model declined is kept
-// as it is, subject to the same pruning.
-__device__ __forceinline__ uint32_t densify_action(const DensifyParams& dp, const float* __restrict__ params,
-                                                   const float4* __restrict__ stats, uint32_t i,
-                                                   const uint8_t* __restrict__ veto = nullptr) {
-  const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
-  const float4 s = stats[i];
+// What happens to a Gaussian (src/shaders/densify.wgsl:72-85): 0 drop, 1 keep,
+// 2 clone, 3 split. p0, p1: the first 32 bytes of its record (slots 3-6: opacity
+// logit, log-scales); s: its statistics. A candidate the learned proposal
+// declined (vetoed) is kept as it is, subject to the same pruning.
+__device__ __forceinline__ uint32_t densify_decide(const DensifyParams& dp, float4 p0, float4 p1, float4 s,
+                                                   bool vetoed) {
   const float grad = s.y > 0.0f ? s.x / s.y : 0.0f;
-  const float size = expf(fmaxf(p[4], fmaxf(p[5], p[6])));
-  const float opacity = sigmoidf_(p[3]);
+  const float size = expf(fmaxf(p1.x, fmaxf(p1.y, p1.z)));
+  const float opacity = sigmoidf_(p0.w);
   auto removed = [&](float o, float sz) { return o < dp.min_opacity || (dp.max_size > 0.0f && sz > dp.max_size); };
-  if (grad >= dp.grad_threshold && !(veto && veto[i])) {
+  if (grad >= dp.grad_threshold && !vetoed) {
     if (size <= dp.clone_max_size) return removed(opacity, size) ? 0u : 2u;
     return removed(opacity, size / SPLIT_SHRINK) ? 0u : 3u;
   }
   return removed(opacity, size) ? 0u : 1u;
 }
 
-// src/shaders/densify.wgsl:96-107
+__device__ __forceinline__ uint32_t densify_action(const DensifyParams& dp, const float* __restrict__ params,
+                                                   const float4* __restrict__ stats, uint32_t i,
+                                                   const uint8_t* __restrict__ veto = nullptr) {
+  const float4* record = reinterpret_cast<const float4*>(params + (size_t)i * FLOATS_PER_GAUSSIAN);
+  return densify_decide(dp, record[0], record[1], stats[i], veto && veto[i]);
+}
+
+// src/shaders/densify.wgsl:96-107. Grid-stride over the resident CTAs: the tallies
+// go to four global counters once per CTA, not once per 256 Gaussians. (Four
+// Gaussians a thread with their loads issued together measured slower: 26.3
+// against 23.8 us at 1.1M.)
 __global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, const float* __restrict__ params,
                                                             const float4* __restrict__ stats,
                                                             const uint8_t* __restrict__ veto, uint32_t count,
@@ -91,19 +99,23 @@ __global__ void __launch_bounds__(256) densify_count_kernel(DensifyParams dp, co
   __shared__ uint32_t local[4];
   if (threadIdx.x < 4) local[threadIdx.x] = 0;
   __syncthreads();
-  const uint32_t i = blockIdx.x * 256 + threadIdx.x;
-  uint32_t a = 4;  // none
-  if (i < count) {
-    a = densify_action(dp, params, stats, i, veto);
-    outputs[i] = a == 0 ? 0u : (a >= 2 ? 2u : 1u);
-    actions[i] = (uint8_t)a;  // for the copy and place kernels, decided once
-  }
-  // One shared-memory atomic per warp and action instead of one per thread.
+  uint32_t mine[4] = {0, 0, 0, 0};
+  for (uint32_t base = blockIdx.x * 256; base < count; base += gridDim.x * 256) {
+    const uint32_t i = base + threadIdx.x;
+    uint32_t a = 4;  // none
+    if (i < count) {
+      a = densify_action(dp, params, stats, i, veto);
+      outputs[i] = a == 0 ? 0u : (a >= 2 ? 2u : 1u);
+      actions[i] = (uint8_t)a;  // for the copy kernel, decided once
+    }
 #pragma unroll
-  for (uint32_t v = 0; v < 4; v++) {
-    const uint32_t votes = __ballot_sync(0xffffffffu, a == v);
-    if ((threadIdx.x & 31u) == 0 && votes) atomicAdd(&local[v], (uint32_t)__popc(votes));
+    for (uint32_t v = 0; v < 4; v++) mine[v] += __popc(__ballot_sync(0xffffffffu, a == v));
   }
+  // One shared-memory atomic per warp and action, one global one per CTA and action.
+  if ((threadIdx.x & 31u) == 0)
+#pragma unroll
+    for (uint32_t v = 0; v < 4; v++)
+      if (mine[v]) atomicAdd(&local[v], mine[v]);
   __syncthreads();
   if (threadIdx.x < 4 && local[threadIdx.x]) atomicAdd(&counters[threadIdx.x], local[threadIdx.x]);
 }
@@ -150,13 +162,56 @@ __device__ __forceinline__ void densify_load(const float* __restrict__ params, c
   }
 }
 
+// Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and
+// Box-Muller, for Gaussian i (raw record p) whose children are outputs o and o + 1.
+__device__ __forceinline__ void place_split(const DensifyParams& dp, const float* __restrict__ p, uint32_t i,
+                                            uint32_t o, float* __restrict__ new_params,
+                                            float* __restrict__ new_gaussians) {
+  // rotation_matrix (src/shaders/gaussianMath.wgsl:13-25)
+  float dot = p[8] * p[8];
+  dot = dot + p[9] * p[9];
+  dot = dot + p[10] * p[10];
+  dot = dot + p[11] * p[11];
+  const float len = sqrtf(dot);
+  const float qw = p[8] / len, qx = p[9] / len, qy = p[10] / len, qz = p[11] / len;
+  float r[3][3];
+  r[0][0] = 1.0f - 2.0f * (qy * qy + qz * qz);
+  r[0][1] = 2.0f * (qx * qy + qw * qz);
+  r[0][2] = 2.0f * (qx * qz - qw * qy);
+  r[1][0] = 2.0f * (qx * qy - qw * qz);
+  r[1][1] = 1.0f - 2.0f * (qx * qx + qz * qz);
+  r[1][2] = 2.0f * (qy * qz + qw * qx);
+  r[2][0] = 2.0f * (qx * qz + qw * qy);
+  r[2][1] = 2.0f * (qy * qz - qw * qx);
+  r[2][2] = 1.0f - 2.0f * (qx * qx + qy * qy);
+  for (uint32_t c = 0; c < 2; c++) {
+    const uint32_t h1 = pcg(dp.seed ^ pcg(2u * i + c));
+    const uint32_t h2 = pcg(h1), h3 = pcg(h2), h4 = pcg(h3);
+    const float tau = 6.283185307179586f;
+    const float r1 = sqrtf(-2.0f * logf(unit_of(h1)));
+    const float r2 = sqrtf(-2.0f * logf(unit_of(h3)));
+    const float n0 = r1 * cosf(tau * unit_of(h2)), n1 = r1 * sinf(tau * unit_of(h2)), n2 = r2 * cosf(tau * unit_of(h4));
+    const float sv[3] = {expf(p[4]) * n0, expf(p[5]) * n1, expf(p[6]) * n2};
+    float* out = new_params + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
+    float* act = new_gaussians + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      float v = r[0][row] * sv[0];
+      v = v + r[1][row] * sv[1];
+      v = v + r[2][row] * sv[2];
+      out[row] = p[row] + v;
+      act[row] = out[row];  // positions activate to themselves
+    }
+  }
+}
+
 // Writes the outputs of Gaussian i, whose action is a (1 keep, 2 clone, 3 split)
 // and whose first output is o (src/shaders/densify.wgsl:148-180): a kept Gaussian
 // and a clone's original keep their moments, identity and steps seen; new ones
 // get zero moments, identity first_id + their output index and zero statistics;
 // a clone's copy and split children are stamped with their kind and the step
-// (slots 7 and 15), split children shrink by 1.6 (densify_place_kernel then sets
-// their positions). The activated values follow (src/shaders/adam.wgsl:74-77).
+// (slots 7 and 15), split children shrink by 1.6 (their positions are left to
+// place_split). The activated values follow (src/shaders/adam.wgsl:74-77).
 __device__ __forceinline__ void densify_store(const DensifyParams& dp, uint32_t first_id, uint32_t new_count,
                                               uint32_t a, uint32_t o, uint32_t lane, const SlotPair& s,
                                               float* __restrict__ new_params, float* __restrict__ new_sh,
@@ -183,6 +238,7 @@ __device__ __forceinline__ void densify_store(const DensifyParams& dp, uint32_t 
           if (k == 15) v = (float)dp.seed;
         }
         if (a == 3) {
+          if (k < 3) continue;  // place_split's
           if (k >= 4 && k <= 6) v = s.v[h] - LOG_SPLIT_SHRINK;
           if (k == 7) v = 2.0f;
           if (k == 15) v = (float)dp.seed;
@@ -201,8 +257,8 @@ __device__ __forceinline__ void densify_store(const DensifyParams& dp, uint32_t 
 // of Gaussian l in one coalesced pass, then the warp copies the live ones two at
 // a time, a moment slot per lane (lanes l and l + 32 of the 61; each slot's
 // moment, raw value or SH coefficient is a contiguous run across the lanes), with
-// both Gaussians' reads issued before their writes. densify_place_kernel then
-// places split children.
+// both Gaussians' reads issued before their writes; split children's positions
+// come last.
 __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, const float* __restrict__ params,
                                                            const uint8_t* __restrict__ actions,
                                                            const float* __restrict__ sh,
@@ -242,54 +298,11 @@ __global__ void __launch_bounds__(256) densify_copy_kernel(DensifyParams dp, con
                       new_gaussians);
     }
   }
-}
-
-// Split children's positions: center + R (scale ⊙ n), n ~ N(0, I) from PCG and Box-Muller.
-__global__ void densify_place_kernel(DensifyParams dp, const float* __restrict__ params,
-                                     const uint8_t* __restrict__ actions, const uint32_t* __restrict__ outputs,
-                                     uint32_t count, float* __restrict__ new_params,
-                                     float* __restrict__ new_gaussians) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  if (actions[i] != 3) return;
-  const float* p = params + (size_t)i * FLOATS_PER_GAUSSIAN;
-  // rotation_matrix (src/shaders/gaussianMath.wgsl:13-25)
-  float dot = p[8] * p[8];
-  dot = dot + p[9] * p[9];
-  dot = dot + p[10] * p[10];
-  dot = dot + p[11] * p[11];
-  const float len = sqrtf(dot);
-  const float qw = p[8] / len, qx = p[9] / len, qy = p[10] / len, qz = p[11] / len;
-  float r[3][3];
-  r[0][0] = 1.0f - 2.0f * (qy * qy + qz * qz);
-  r[0][1] = 2.0f * (qx * qy + qw * qz);
-  r[0][2] = 2.0f * (qx * qz - qw * qy);
-  r[1][0] = 2.0f * (qx * qy - qw * qz);
-  r[1][1] = 1.0f - 2.0f * (qx * qx + qz * qz);
-  r[1][2] = 2.0f * (qy * qz + qw * qx);
-  r[2][0] = 2.0f * (qx * qz + qw * qy);
-  r[2][1] = 2.0f * (qy * qz - qw * qx);
-  r[2][2] = 1.0f - 2.0f * (qx * qx + qy * qy);
-  const uint32_t o = outputs[i];
-  for (uint32_t c = 0; c < 2; c++) {
-    const uint32_t h1 = pcg(dp.seed ^ pcg(2u * i + c));
-    const uint32_t h2 = pcg(h1), h3 = pcg(h2), h4 = pcg(h3);
-    const float tau = 6.283185307179586f;
-    const float r1 = sqrtf(-2.0f * logf(unit_of(h1)));
-    const float r2 = sqrtf(-2.0f * logf(unit_of(h3)));
-    const float n0 = r1 * cosf(tau * unit_of(h2)), n1 = r1 * sinf(tau * unit_of(h2)), n2 = r2 * cosf(tau * unit_of(h4));
-    const float sv[3] = {expf(p[4]) * n0, expf(p[5]) * n1, expf(p[6]) * n2};
-    float* out = new_params + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
-    float* act = new_gaussians + (size_t)(o + c) * FLOATS_PER_GAUSSIAN;
-#pragma unroll
-    for (int row = 0; row < 3; row++) {
-      float v = r[0][row] * sv[0];
-      v = v + r[1][row] * sv[1];
-      v = v + r[2][row] * sv[2];
-      out[row] = p[row] + v;
-      act[row] = out[row];  // positions activate to themselves
-    }
-  }
+  // Then the split children's positions, a thread per Gaussian (no other thread
+  // writes those three values).
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    if (actions[i] == 3) place_split(dp, params + (size_t)i * FLOATS_PER_GAUSSIAN, i, outputs[i], new_params,
+                                     new_gaussians);
 }
 
 // The learned densification's inputs (see DG_MLP_FEATURES in the header),
@@ -609,6 +622,17 @@ static void camera_center(const float* view, float* out) {
 
 }  // namespace dg
 
+// A grid-stride kernel's grid of 256-thread CTAs over `units` items: at most one
+// wave of the CTAs that fit on the GPU at once (a second, partial wave would
+// leave most SMs idle while it finishes).
+template <typename Kernel>
+static uint32_t resident_grid(const dg_context* ctx, Kernel kernel, uint32_t units) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  return std::max(1u, std::min(ceil_div(units, 256u), (uint32_t)(ctx->sm_count * per_sm)));
+}
+
 extern "C" {
 
 void dg_training_settings_default(dg_training_settings* s, double extent) {
@@ -837,7 +861,7 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   }
   const uint8_t* veto_ptr = veto ? typed<uint8_t>(veto) : nullptr;
   DG_LAUNCH(ctx, "densify_count",
-            densify_count_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
+            densify_count_kernel<<<resident_grid(ctx, densify_count_kernel, count), 256, 0, ctx->stream>>>(
                 dp, typed<float>(t->params), typed<float4>(t->stats), veto_ptr, count, typed<uint32_t>(outputs),
                 typed<uint8_t>(actions), typed<uint32_t>(counters)));
   uint32_t* total_ptr = typed<uint32_t>(outputs) + count;
@@ -907,16 +931,11 @@ dg_status dg_trainer_densify(dg_trainer* t, int32_t prune_large) {
   }
   dg_renderer* r = t->renderer;
   DG_LAUNCH(ctx, "densify_copy",
-            densify_copy_kernel<<<std::max(1u, std::min(ceil_div(count, 256), (uint32_t)ctx->sm_count * 8u)), 256, 0,
-                                  ctx->stream>>>(
+            densify_copy_kernel<<<resident_grid(ctx, densify_copy_kernel, count), 256, 0, ctx->stream>>>(
                 dp, typed<float>(t->params), typed<uint8_t>(actions), typed<float>(r->sh),
                 typed<float2>(t->moments), typed<uint32_t>(t->ids), typed<float2>(t->aux), typed<uint32_t>(outputs),
                 count, new_count, first_id, typed<float>(params), typed<float>(sh), typed<float2>(moments),
                 typed<uint32_t>(ids), typed<float2>(aux), typed<float>(gaussians)));
-  DG_LAUNCH(ctx, "densify_place",
-            densify_place_kernel<<<ceil_div(count, 256), 256, 0, ctx->stream>>>(
-                dp, typed<float>(t->params), typed<uint8_t>(actions), typed<uint32_t>(outputs), count,
-                typed<float>(params), typed<float>(gaussians)));
   // The last frame's pair count (every queued readback has arrived: the counts
   // above were read back), scaled to the new count with 10% to spare, sizes the
   // new set's pair buffers, so the frames after a densification do not overflow
