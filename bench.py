@@ -454,8 +454,14 @@ def measure_held_out(device, renderer, held, repeats: int) -> dict:
     same = bool(np.array_equal(tex.buffer.read(np.uint8), targets.read(np.uint8, offset=(n - 1) * W * H * 4)))
     tex.destroy()
     targets.destroy()
+    # The tuner's last three candidates are the larger blend tiles at the best
+    # 16x16 candidate's batch and threshold.
+    secs = tuned["seconds"]
+    by_tile = {"16x16": min(secs[:-3]), "32x16": secs[-3], "16x32": secs[-2], "32x32": secs[-1]}
     return {"views": n, "frames_per_s": round(batched, 1), "per_view_frames_per_s": round(per_view, 1),
-            "batch": tuned["batch"], "coop_min": tuned["coopMin"], "tuner_candidates": len(tuned["seconds"]),
+            "batch": tuned["batch"], "coop_min": tuned["coopMin"], "blend_tile": "%dx%d" % tuned["tile"],
+            "tuner_candidates": len(secs),
+            "tuner_frames_per_s_by_blend_tile": {k: round(n / v, 1) for k, v in by_tile.items()},
             "last_view_identical": same, "kernels_one_batch": kernels}
 
 

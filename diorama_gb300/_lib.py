@@ -152,6 +152,8 @@ SIGNATURES = {
     "dg_renderer_render_views": (None, [_P, POINTER(Camera), c_uint32, _fp, _P, _P]),
     "dg_renderer_set_view_batching": (None, [_P, c_uint32, c_uint32, c_int32]),
     "dg_renderer_view_batching": (None, [_P, POINTER(c_uint32), POINTER(c_uint32)]),
+    "dg_renderer_set_view_tile": (None, [_P, c_uint32, c_uint32]),
+    "dg_renderer_view_tile": (None, [_P, POINTER(c_uint32), POINTER(c_uint32)]),
     "dg_renderer_tune_views": (None, [_P, POINTER(Camera), c_uint32, _fp, _P, POINTER(c_uint32), POINTER(c_uint32),
                                       POINTER(c_double), POINTER(c_uint32)]),
     "dg_renderer_views_pixel_last": (c_void_p, [_P]),

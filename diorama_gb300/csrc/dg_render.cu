@@ -27,13 +27,15 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
 // src/shaders/preprocess.wgsl:21-88 for one Gaussian g (16 activated floats)
 // seen by camera cam, its SH coefficients at shv: writes the 48-byte splat to out
 // (zeros when culled) and returns the tiles it touches
-// (src/shaders/tiles.wgsl:24-35) and its depth's bits (0 when culled).
+// (src/shaders/tiles.wgsl:24-35; blend tiles of 2^twl x 2^thl tiles for a batch
+// of views) and its depth's bits (0 when culled).
 struct Projected {
   uint32_t tiles, depth_bits;
 };
 
 __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const float (&g)[16], const float* shv,
-                                                    uint32_t basis_count, float4* __restrict__ out) {
+                                                    uint32_t basis_count, float4* __restrict__ out,
+                                                    uint32_t twl = 0, uint32_t thl = 0) {
   const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
   auto culled = [&]() {
     out[0] = zero;
@@ -85,7 +87,7 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
   out[0] = make_float4(mx, my, p.depth, radius);
   out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, 0.0f);
   out[2] = make_float4(fmaxf(color[0], 0.0f), fmaxf(color[1], 0.0f), fmaxf(color[2], 0.0f), g[3]);
-  const uint4 rect = tile_rect(mx, my, radius, tile_grid(cam));
+  const uint4 rect = blend_rect(tile_rect(mx, my, radius, tile_grid(cam)), twl, thl);
   return Projected{(rect.z - rect.x) * (rect.w - rect.y), __float_as_uint(p.depth)};
 }
 
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_views_kernel(
     const Camera* __restrict__ cameras, uint32_t views, const float* __restrict__ gaussians,
     const float* __restrict__ sh, uint32_t count, const uint32_t* __restrict__ scene_params,
     float* __restrict__ splats, uint32_t* __restrict__ tile_counts, uint2* __restrict__ depth_keys,
-    uint32_t* __restrict__ depth_order) {
+    uint32_t* __restrict__ depth_order, uint32_t twl, uint32_t thl) {
   __shared__ float s_sh[PRE_THREADS * SH_REST_FLOATS];
   const uint32_t degree = scene_params[0];
   const uint32_t basis_count = (degree + 1u) * (degree + 1u) - 1u;
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_views_kernel(
   for (uint32_t v = 0; v < views; v++) {
     const size_t at = (size_t)v * count + i;
     const Projected pr = preprocess_one(cameras[v], g, s_sh + threadIdx.x * SH_REST_FLOATS, basis_count,
-                                        reinterpret_cast<float4*>(splats + at * FLOATS_PER_SPLAT));
+                                        reinterpret_cast<float4*>(splats + at * FLOATS_PER_SPLAT), twl, thl);
     tile_counts[at] = pr.tiles;
     depth_keys[at] = make_uint2(pr.depth_bits, v);
     depth_order[at] = (uint32_t)at;
@@ -224,7 +226,8 @@ inline uint32_t stride_grid(const dg_context* ctx, uint64_t n, uint32_t threads)
 // pairs of 32 consecutive sorted splats are one contiguous run of slots. Keys are
 // the tile index alone (u32), values the splat index. For a batch of views
 // (splat v * per_view + i is Gaussian i in view v), the key of a tile of view v
-// is v << view_shift | its tile index within the view.
+// is v << view_shift | its tile index within the view; the tiles are blend tiles
+// of 2^twl x 2^thl 16x16 tiles (1 x 1 outside batches of views).
 __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Camera* __restrict__ camera,
                                                                        const float* __restrict__ splats,
                                                                        const uint32_t* __restrict__ order,
@@ -232,7 +235,8 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
                                                                        uint32_t count, uint32_t per_view,
                                                                        uint32_t view_shift, uint32_t capacity,
                                                                        uint32_t* __restrict__ keys,
-                                                                       uint32_t* __restrict__ values) {
+                                                                       uint32_t* __restrict__ values, uint32_t twl,
+                                                                       uint32_t thl) {
   __shared__ uint32_t s_excl[DUP_THREADS];
   __shared__ uint32_t s_w[DUP_THREADS];       // the splat's tile rectangle's width
   __shared__ float s_inv[DUP_THREADS];        // 1 / width
@@ -243,14 +247,15 @@ __global__ void __launch_bounds__(DUP_THREADS) duplicate_sorted_kernel(const Cam
   const uint32_t first = blockIdx.x * DUP_THREADS + warp * 32;
   if (first >= count) return;  // warp-uniform
   const Camera& cam = *camera;
-  const uint2 tiles = tile_grid(cam);
+  const uint2 tiles16 = tile_grid(cam);
+  const uint2 tiles = make_uint2(blend_tiles_along(tiles16.x, twl), blend_tiles_along(tiles16.y, thl));
   uint32_t n = 0, index = 0;
   uint4 rect = make_uint4(0, 0, 0, 0);
   if (j < count) {
     index = order[j];
     const float4 s = reinterpret_cast<const float4*>(splats + (size_t)index * FLOATS_PER_SPLAT)[0];
     if (s.w != 0.0f) {
-      rect = tile_rect(s.x, s.y, s.w, tiles);
+      rect = blend_rect(tile_rect(s.x, s.y, s.w, tiles16), twl, thl);
       n = (rect.z - rect.x) * (rect.w - rect.y);
     }
   }
@@ -606,16 +611,23 @@ __device__ __forceinline__ void publish_blended(uint32_t* __restrict__ mask, uin
 
 // The geometry of a blend item: tile `tile` (of the view tile / tiles_per_view
 // when several views are blended together), 8x4 block `block`, this lane's pixel.
+// A blend tile of 2^twl x 2^thl 16x16 tiles has 8 blocks per 16x16 tile, those
+// of its 16x16 tile k numbered 8k to 8k + 7 (k row-major within the blend tile).
 struct BlendItem {
   uint32_t px, py;
   size_t pixel;  // index in the views' stacked pixel buffers
   bool inside;
   float x0, y0;  // the block's first pixel center
   uint2 run;
+  uint32_t tx, ty;  // the block's 16x16 tile
   __device__ __forceinline__ BlendItem(uint32_t tile, uint32_t block, uint32_t lane, uint32_t tiles_x,
-                                       uint32_t tiles_per_view, float vpx, float vpy, const uint2* __restrict__ ranges) {
+                                       uint32_t tiles_per_view, float vpx, float vpy, const uint2* __restrict__ ranges,
+                                       uint32_t twl = 0, uint32_t thl = 0) {
     const uint32_t view = tile / tiles_per_view, local = tile - view * tiles_per_view;
-    const uint32_t bx = (local % tiles_x) * TILE + (block & 1u) * 8u, by = (local / tiles_x) * TILE + (block >> 1) * 4u;
+    const uint32_t blend_x = blend_tiles_along(tiles_x, twl), sub = block >> 3;
+    tx = ((local % blend_x) << twl) + (sub & ((1u << twl) - 1u));
+    ty = ((local / blend_x) << thl) + (sub >> twl);
+    const uint32_t bx = tx * TILE + (block & 1u) * 8u, by = ty * TILE + ((block >> 1) & 3u) * 4u;
     px = bx + (lane & 7u);
     py = by + (lane >> 3);
     inside = (float)px < vpx && (float)py < vpy;
@@ -639,7 +651,9 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 
 // src/shaders/rasterize.wgsl:32-100. The work is split into items, one per (tile,
 // 8x4 pixel block): 8 per 16x16 tile, taken from counters by persistent CTAs and
-// warps in the plan's order. Whatever the split, each pixel blends the tile's list
+// warps in the plan's order. With blend tiles of 2^TWL x 2^THL 16x16 tiles (a
+// batch of views only: no checkpoints or blend mask), each block keeps only its
+// own 16x16 tile's entries of the blend tile's list. Whatever the split, each pixel blends the tile's list
 // front to back exactly as the plain loop over every entry does, so results are
 // bit-identical to it; the split only decides who does the work:
 //
@@ -659,6 +673,7 @@ __device__ __forceinline__ void write_pixel(const BlendItem& it, const PixelBlen
 // all of its pixels, and a power under the splat's cutoff skips the exp: none of
 // these changes a result. The pixel state at each CHUNK boundary of the list is
 // saved for the backward pass, and which entries each block blended.
+template <uint32_t TWL, uint32_t THL>
 __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
@@ -673,10 +688,13 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
   __shared__ uint32_t s_qpos[2][PRODUCERS][32];
   __shared__ uint32_t s_qlive[2][PRODUCERS];
   __shared__ uint32_t s_item, s_stop, s_done;  // s_done: warp 0's pixels that have stopped
+  constexpr uint32_t BLOCK_SHIFT = 3u + TWL + THL, BLOCK_MASK = (1u << BLOCK_SHIFT) - 1u;
+  constexpr bool MEMBER = TWL + THL > 0;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   WarpStage& st = stages[warp];
   const float vpx = camera->viewport[0], vpy = camera->viewport[1];
   const uint32_t tiles_x = ((uint32_t)vpx + TILE - 1u) / TILE;
+  const uint2 tiles16 = make_uint2(tiles_x, ((uint32_t)vpy + TILE - 1u) / TILE);
   const float4 bg = raster_params[0];
   const uint32_t cooperative = plan[0], tiles = plan[1];
   const uint32_t* order = plan + PLAN_HEADER;
@@ -697,9 +715,10 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     }
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= cooperative * 8u) break;
-    const uint32_t block = item & 7u;
-    const BlendItem it(order[item >> 3], block, lane, tiles_x, tiles_per_view, vpx, vpy, ranges);
+    if (item >= cooperative << BLOCK_SHIFT) break;
+    const uint32_t block = item & BLOCK_MASK;
+    const BlendItem it(order[item >> BLOCK_SHIFT], block, lane, tiles_x, tiles_per_view, vpx, vpy, ranges, TWL, THL);
+    const TileMember tm{MEMBER, it.tx, it.ty, tiles16};
     const uint2 run = it.run;
     PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
     uint32_t next_k = 1;  // the next checkpoint boundary (warp 0)
@@ -718,7 +737,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
       if (warp > 0) {
         const uint32_t start = run.x + r * STRIDE + 32u * pw;
         if (r < rounds && start < run.y) {
-          const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
+          const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, tm);
           {
             const uint32_t k = start + STRIDE + lane;
             stage_issue(st, splats, next_index, k < run.y);
@@ -789,9 +808,11 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     uint32_t item = 0;
     if (lane == 0) item = atomicAdd(&counters[1], 1u);
     item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= (tiles - cooperative) * 8u) break;
-    const uint32_t block = item & 7u;
-    const BlendItem it(order[cooperative + (item >> 3)], block, lane, tiles_x, tiles_per_view, vpx, vpy, ranges);
+    if (item >= (tiles - cooperative) << BLOCK_SHIFT) break;
+    const uint32_t block = item & BLOCK_MASK;
+    const BlendItem it(order[cooperative + (item >> BLOCK_SHIFT)], block, lane, tiles_x, tiles_per_view, vpx, vpy,
+                       ranges, TWL, THL);
+    const TileMember tm{MEMBER, it.tx, it.ty, tiles16};
     const uint2 run = it.run;
     PixelBlend pb{(float)it.px + 0.5f, (float)it.py + 0.5f, 1.0f, 0.0f, 0.0f, 0.0f, 0u, !it.inside};
     uint32_t next_k = 1;
@@ -808,7 +829,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
         save_checkpoints(checkpoints, run.x, next_k, next_k + 1, block, lane, pb.T, pb.r, pb.g, pb.b);
         next_k++;
       }
-      const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0);
+      const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, tm);
       {
         const uint32_t k = start + 32u + lane;
         stage_issue(st, splats, next_index, k < run.y);
@@ -956,7 +977,7 @@ dg_status rasterizer_launch(dg_tile_rasterizer* tr, dg_buffer* target, bool coun
       DG_LAUNCH(ctx, "duplicate",
                 duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, st>>>(
                     cam, typed<float>(tr->splats), order, typed<uint32_t>(tr->counts_sorted), count, count, 0u,
-                    tr->pair_capacity, typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values)));
+                    tr->pair_capacity, typed<uint32_t>(tr->keys), typed<uint32_t>(tr->values), 0u, 0u));
     }
     DG_TRY(sort_launch(ctx, tr->tile_plan, tr->keys->ptr, typed<uint32_t>(tr->values), tr->keys_alt->ptr,
                        typed<uint32_t>(tr->values_alt), typed<uint32_t>(tr->scan_total), tr->sort_scratch->ptr));
@@ -1015,16 +1036,29 @@ dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   return blend_forward(ctx, f);
 }
 
+template <uint32_t TWL, uint32_t THL>
+static dg_status launch_rasterize_kernel(dg_context* ctx, const BlendForward& f) {
+  const auto kernel = rasterize_kernel<TWL, THL>;
+  const uint32_t items = f.tiles << (3u + TWL + THL);
+  DG_LAUNCH(ctx, "rasterize",
+            kernel<<<blend_grid(ctx, (const void*)kernel, FWD_THREADS, items), FWD_THREADS, 0, ctx->stream>>>(
+                f.camera, f.raster_params, f.splats, f.pair_splats, f.ranges, f.plan, f.tiles_per_view, f.target,
+                f.pixel_color, f.pixel_last, f.checkpoints, f.blend_mask, f.counters));
+  return DG_OK;
+}
+
 dg_status blend_forward(dg_context* ctx, const BlendForward& f) {
+  const BlendShape sh = f.shape;
+  DG_REQUIRE(sh.twl <= MAX_BLEND_TILE_LOG2 && sh.thl <= MAX_BLEND_TILE_LOG2, "blend tiles of at most 2 x 2 tiles");
+  DG_REQUIRE(sh.twl + sh.thl == 0 || (!f.checkpoints && !f.blend_mask && !f.chunks),
+             "blend tiles larger than 16x16 have no backward pass");
   DG_CUDA(cudaMemsetAsync(f.counters, 0, 16, ctx->stream));
   DG_LAUNCH(ctx, "plan",
             plan_kernel<<<1, PLAN_THREADS, 0, ctx->stream>>>(f.ranges, f.tiles, f.coop_min, f.plan, f.chunks));
-  DG_LAUNCH(ctx, "rasterize",
-            rasterize_kernel<<<blend_grid(ctx, (const void*)rasterize_kernel, FWD_THREADS, f.tiles * 8u), FWD_THREADS,
-                               0, ctx->stream>>>(f.camera, f.raster_params, f.splats, f.pair_splats, f.ranges, f.plan,
-                                                 f.tiles_per_view, f.target, f.pixel_color, f.pixel_last,
-                                                 f.checkpoints, f.blend_mask, f.counters));
-  return DG_OK;
+  if (sh.twl == 0 && sh.thl == 0) return launch_rasterize_kernel<0, 0>(ctx, f);
+  if (sh.twl == 1 && sh.thl == 0) return launch_rasterize_kernel<1, 0>(ctx, f);
+  if (sh.twl == 0 && sh.thl == 1) return launch_rasterize_kernel<0, 1>(ctx, f);
+  return launch_rasterize_kernel<1, 1>(ctx, f);
 }
 
 uint32_t blend_grid(dg_context* ctx, const void* kernel, uint32_t threads, uint32_t items) {
@@ -1040,20 +1074,22 @@ uint32_t blend_grid(dg_context* ctx, const void* kernel, uint32_t threads, uint3
 
 dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32_t views, const float* gaussians,
                                   const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
-                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order) {
+                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order, BlendShape shape) {
   DG_LAUNCH(ctx, "preprocess",
             preprocess_views_kernel<<<ceil_div(count, PRE_THREADS), PRE_THREADS, 0, ctx->stream>>>(
-                cameras, views, gaussians, sh, count, scene_params, splats, tile_counts, depth_keys, order));
+                cameras, views, gaussians, sh, count, scene_params, splats, tile_counts, depth_keys, order,
+                shape.twl, shape.thl));
   return DG_OK;
 }
 
 
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
                                   const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t view_shift,
-                                  uint32_t capacity, uint32_t* keys, uint32_t* values) {
+                                  uint32_t capacity, uint32_t* keys, uint32_t* values, BlendShape shape) {
   DG_LAUNCH(ctx, "duplicate",
             duplicate_sorted_kernel<<<ceil_div(count, DUP_THREADS), DUP_THREADS, 0, ctx->stream>>>(
-                camera, splats, order, offsets, count, per_view, view_shift, capacity, keys, values));
+                camera, splats, order, offsets, count, per_view, view_shift, capacity, keys, values, shape.twl,
+                shape.thl));
   return DG_OK;
 }
 
@@ -1297,6 +1333,7 @@ dg_status dg_renderer_create(dg_context* ctx, uint32_t initial_pair_capacity, dg
   r->ctx = ctx;
   r->initial_pair_capacity = initial_pair_capacity;
   r->view_coop_min = COOP_MIN;
+  r->view_shape = BlendShape{0u, 0u};
   r->view_graph = true;
   dg_status st = alloc_buffer(ctx, sizeof(Camera), &r->camera);
   if (st != DG_OK) {

@@ -77,9 +77,17 @@ dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
 // warp items.
 uint32_t blend_grid(dg_context* ctx, const void* kernel, uint32_t threads, uint32_t items);
 
+// Blend tiles of 2^twl x 2^thl 16x16 tiles (dg_render_kernels.cuh, blend_rect):
+// {0, 0} everywhere but batches of views.
+struct BlendShape {
+  uint32_t twl, thl;
+  bool operator==(const BlendShape& o) const { return twl == o.twl && thl == o.thl; }
+};
+constexpr uint32_t MAX_BLEND_TILE_LOG2 = 1;  // blend tiles of up to 2 x 2 16x16 tiles
+
 // The forward blend (plan + rasterize kernels) over `tiles` tiles of
 // tiles_per_view each; checkpoints, blend_mask and chunks may be NULL when no
-// backward pass follows.
+// backward pass follows, and must be with blend tiles larger than 16x16.
 struct BlendForward {
   const Camera* camera;
   const float4* raster_params;
@@ -95,15 +103,16 @@ struct BlendForward {
   float4* checkpoints;
   uint32_t* blend_mask;
   uint32_t* counters;  // 4 words, cleared here
+  BlendShape shape;
 };
 dg_status blend_forward(dg_context* ctx, const BlendForward& f);
 // The batched views' stages (dg_render.cu; used by dg_views.cu).
 dg_status views_preprocess_launch(dg_context* ctx, const Camera* cameras, uint32_t views, const float* gaussians,
                                   const float* sh, uint32_t count, const uint32_t* scene_params, float* splats,
-                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order);
+                                  uint32_t* tile_counts, uint2* depth_keys, uint32_t* order, BlendShape shape);
 dg_status duplicate_sorted_launch(dg_context* ctx, const Camera* camera, const float* splats, const uint32_t* order,
                                   const uint32_t* offsets, uint32_t count, uint32_t per_view, uint32_t view_shift,
-                                  uint32_t capacity, uint32_t* keys, uint32_t* values);
+                                  uint32_t capacity, uint32_t* keys, uint32_t* values, BlendShape shape);
 // Per-tile ranges of the sorted pairs of a batch of views (dg_views.cu), whose
 // keys are view << view_shift | the view's tile index.
 dg_status find_view_ranges_launch(dg_context* ctx, const uint32_t* tile_keys, const uint32_t* pair_total,
@@ -133,10 +142,12 @@ struct dg_renderer {
   dg_buffer* grad_sh;
   dg_tile_rasterizer* draw_rasterizer;
   // Batched views (dg_views.cu): buffers, views per batch (0: all), the blend's
-  // cooperative threshold, and whether a batch is replayed as a CUDA graph.
+  // cooperative threshold, the blend tiles, and whether a batch is replayed as a
+  // CUDA graph.
   dg_view_batch* views;
   uint32_t view_batch;
   uint32_t view_coop_min;
+  dg::BlendShape view_shape;
   bool view_graph;
 };
 
@@ -159,8 +170,8 @@ dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam
                                          float4* stats, float2* aux, bool keep_gradients);
 // Batched views (dg_views.cu): renders count views in batches of `batch` into
 // targets (count rgba8 images, may be NULL) and pixel_colors (count vec4 images,
-// may be NULL).
+// may be NULL), blending in tiles of `shape`.
 dg_status views_render(dg_renderer* r, const dg_camera* cams, uint32_t count, const float bg[3], uchar4* targets,
-                       float4* pixel_colors, uint32_t batch, uint32_t coop_min);
+                       float4* pixel_colors, uint32_t batch, uint32_t coop_min, BlendShape shape);
 void view_batch_destroy(dg_view_batch* b);
 }  // namespace dg

@@ -393,13 +393,26 @@ __device__ __forceinline__ void stage_issue(WarpStage& st, const float* __restri
   }
 }
 
+__device__ __forceinline__ uint4 tile_rect(float mx, float my, float radius, uint2 tiles);
+
+// The 16x16 tile a blend item's block lies in, for blend tiles of several 16x16
+// tiles: the block keeps only the entries of that tile's own list (the splats
+// whose tile rectangle holds it). Unused (member == false) for 16x16 blend tiles.
+struct TileMember {
+  bool member;
+  uint32_t tx, ty;
+  uint2 tiles;
+};
+
 // Waits for the window [lo, min(lo + 32, hi)) issued by stage_issue (lane l holds
 // entry lo + l, splat `index`) and keeps, in list order, the splats that can reach
-// the warp's block, whose pixel centers span [x0, x0 + 7] x [y0, y0 + 3]. Returns
-// how many were kept. All 32 lanes must call it. Every value read from `raw` is
-// consumed before this returns, so the caller may issue the next window at once.
+// the warp's block, whose pixel centers span [x0, x0 + 7] x [y0, y0 + 3] (and,
+// with a TileMember, belong to its 16x16 tile's list). Returns how many were
+// kept. All 32 lanes must call it. Every value read from `raw` is consumed before
+// this returns, so the caller may issue the next window at once.
 __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, uint32_t lo, uint32_t hi,
-                                                 uint32_t index, float x0, float y0) {
+                                                 uint32_t index, float x0, float y0,
+                                                 const TileMember& tm = TileMember{false, 0u, 0u, {0u, 0u}}) {
   cp_async_wait_all();
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t k = lo + lane;
@@ -415,6 +428,10 @@ __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, 
     quad = make_float4(A, b, C, cut);
     keep = cut < 0.0f && rect_reachable(A, b, C, b / (2.0f * A), b / (2.0f * C), cut, x0 - mean.x, x0 + 7.0f - mean.x,
                                         y0 - mean.y, y0 + 3.0f - mean.y);
+    if (tm.member && keep) {
+      const uint4 rect = tile_rect(mean.x, mean.y, s0.w, tm.tiles);
+      keep = tm.tx >= rect.x && tm.tx < rect.z && tm.ty >= rect.y && tm.ty < rect.w;
+    }
   }
   const uint32_t kept = __ballot_sync(0xffffffffu, keep);
   if (keep) {
@@ -472,6 +489,25 @@ __device__ __forceinline__ uint4 tile_rect(float mx, float my, float radius, uin
   float hix = clampf(floorf((mx + radius) / 16.0f) + 1.0f, 0.0f, (float)tiles.x);
   float hiy = clampf(floorf((my + radius) / 16.0f) + 1.0f, 0.0f, (float)tiles.y);
   return make_uint4((uint32_t)lox, (uint32_t)loy, (uint32_t)hix, (uint32_t)hiy);
+}
+
+// Blend tiles: a batch of views may blend and sort in tiles of 2^twl x 2^thl
+// 16x16 tiles (32x16, 32x32 pixels). A splat is listed once for each blend tile
+// its 16x16-tile rectangle touches, so there are fewer pairs than 16x16 ones, and
+// each 8x4 block keeps only the entries of its own 16x16 tile's list
+// (TileMember): every pixel blends exactly the splats, in exactly the order, of
+// the 16x16 tiling. Coverage itself stays 16x16: a splat's square of half-size
+// ceil(3 sigma) does not bound where its alpha reaches 1/255 (opacity above
+// 0.36 reaches it past 3 sigma), so tiles cut smaller than 16x16 would drop
+// contributions the reference blends.
+__host__ __device__ __forceinline__ uint32_t blend_tiles_along(uint32_t tiles, uint32_t log2) {
+  return (tiles + (1u << log2) - 1u) >> log2;
+}
+
+// The blend tiles that a 16x16-tile rectangle touches (empty stays empty).
+__device__ __forceinline__ uint4 blend_rect(uint4 rect, uint32_t twl, uint32_t thl) {
+  if (rect.z <= rect.x || rect.w <= rect.y) return make_uint4(0u, 0u, 0u, 0u);
+  return make_uint4(rect.x >> twl, rect.y >> thl, blend_tiles_along(rect.z, twl), blend_tiles_along(rect.w, thl));
 }
 
 }  // namespace dg

@@ -1087,7 +1087,7 @@ dg_status dg_trainer_evaluate(dg_trainer* t, const dg_training_view* views, uint
   // Every view rendered in batches (dg_views.cu), then scored on the GPU.
   dg_renderer* r = t->renderer;
   DG_TRY(views_render(r, cameras.data(), view_count, t->settings.background, nullptr, typed<float4>(rendered),
-                      r->view_batch, r->view_coop_min));
+                      r->view_batch, r->view_coop_min, r->view_shape));
   for (uint32_t k = 0; k < view_count; k++) {
     dg_buffer view_rendered{ctx, static_cast<char*>(rendered->ptr) + pixels * 16 * k, pixels * 16, false};
     dg_buffer view_slot{ctx, static_cast<char*>(slot->ptr) + 8 * k, 8, false};

@@ -4,9 +4,10 @@
 // sort over the views' stacked tile numbers, one blend over all their tiles),
 // and a batch whose pair count is known is replayed as one CUDA graph. Each view
 // gets exactly the pairs, order and blend of a single-view render, so its image
-// is bit-identical to GaussianRenderer.encode's. The views per batch and the
-// blend's cooperative threshold come from a small autotuner (dg_renderer_tune_views)
-// or are set by the caller.
+// is bit-identical to GaussianRenderer.encode's. The views per batch, the
+// blend's cooperative threshold and the blend tiles (16x16, 32x16, 16x32 or
+// 32x32 pixels; dg_render_kernels.cuh, blend_rect) come from a small autotuner
+// (dg_renderer_tune_views) or are set by the caller.
 #include "dg_render.cuh"
 #include "dg_render_kernels.cuh"  // plan layout and blend constants (no kernels here)
 
@@ -45,6 +46,7 @@ using namespace dg;
 struct dg_view_batch {
   dg_context* ctx = nullptr;
   uint32_t views = 0, count = 0, tiles_per_view = 0, pixels = 0;
+  BlendShape shape{0u, 0u};
   uint32_t pair_capacity = 0;
   dg_buffer *cameras = nullptr, *raster_params = nullptr, *splats = nullptr, *tile_counts = nullptr;
   dg_buffer *depth_keys = nullptr, *depth_keys_alt = nullptr, *order = nullptr, *order_alt = nullptr;
@@ -56,10 +58,11 @@ struct dg_view_batch {
   cudaGraphExec_t graph = nullptr;
   struct Key {
     uint32_t views, count, capacity, coop_min;
+    BlendShape shape;
     const void *gaussians, *targets, *keys;
     bool operator==(const Key& o) const {
       return views == o.views && count == o.count && capacity == o.capacity && coop_min == o.coop_min &&
-             gaussians == o.gaussians && targets == o.targets && keys == o.keys;
+             shape == o.shape && gaussians == o.gaussians && targets == o.targets && keys == o.keys;
     }
   } key{};
   uint32_t last_total = 0;
@@ -94,7 +97,7 @@ dg_status grow_pairs(dg_view_batch* b, uint32_t capacity) {
 }
 
 // Sizes the batch for `views` views of `count` Gaussians at `pixels` pixels in
-// tiles_per_view tiles each.
+// tiles_per_view blend tiles each.
 dg_status prepare(dg_view_batch* b, uint32_t views, uint32_t count, uint32_t tiles_per_view, uint32_t pixels) {
   dg_context* ctx = b->ctx;
   const size_t n = (size_t)views * count;
@@ -142,7 +145,7 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   DG_TRY(views_preprocess_launch(ctx, typed<Camera>(b->cameras), b->views, typed<float>(r->gaussians),
                                  typed<float>(r->sh), b->count, typed<uint32_t>(r->scene_params),
                                  typed<float>(b->splats), typed<uint32_t>(b->tile_counts), typed<uint2>(b->depth_keys),
-                                 typed<uint32_t>(b->order)));
+                                 typed<uint32_t>(b->order), b->shape));
   // (view, depth) keys: 4 passes over the depth bits and one per 8 bits of view.
   const SortPlan depth_plan = sort_plan_digits(n, 2, bits_for(b->views));
   DG_TRY(sort_launch(ctx, depth_plan, b->depth_keys->ptr, typed<uint32_t>(b->order), b->depth_keys_alt->ptr,
@@ -156,7 +159,7 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   const uint32_t shift = view_shift_for(b->tiles_per_view);
   DG_TRY(duplicate_sorted_launch(ctx, typed<Camera>(b->cameras), typed<float>(b->splats), order,
                                  typed<uint32_t>(b->counts_sorted), n, b->count, shift, b->pair_capacity,
-                                 typed<uint32_t>(b->keys), typed<uint32_t>(b->values)));
+                                 typed<uint32_t>(b->keys), typed<uint32_t>(b->values), b->shape));
   const SortPlan tile_plan = sort_plan_digits(b->pair_capacity, 1, bits_for(b->tiles_per_view));
   DG_TRY(sort_launch(ctx, tile_plan, b->keys->ptr, typed<uint32_t>(b->values), b->keys_alt->ptr,
                      typed<uint32_t>(b->values_alt), typed<uint32_t>(b->scan_total), b->sort_scratch->ptr));
@@ -180,6 +183,7 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   f.pixel_color = typed<float4>(b->pixel_color);
   f.pixel_last = typed<uint32_t>(b->pixel_last);
   f.counters = typed<uint32_t>(b->work);
+  f.shape = b->shape;
   DG_TRY(blend_forward(ctx, f));
   DG_CUDA(cudaMemcpyAsync(b->pinned_total, b->scan_total->ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   return DG_OK;
@@ -188,11 +192,13 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
 // Renders one batch (views[0..count)), replaying its graph when the key matches
 // and growing the pair buffers (then rendering again) when the pairs overflowed.
 dg_status render_batch(dg_renderer* r, dg_view_batch* b, const dg_camera* cams, uint32_t count, const float bg[3],
-                       uchar4* targets, uint32_t coop_min, bool use_graph) {
+                       uchar4* targets, uint32_t coop_min, BlendShape shape, bool use_graph) {
   dg_context* ctx = r->ctx;
   const uint32_t w = (uint32_t)cams[0].viewport[0], h = (uint32_t)cams[0].viewport[1];
-  const uint32_t tiles_per_view = ceil_div(w, TILE) * ceil_div(h, TILE);
+  const uint32_t tiles_per_view =
+      blend_tiles_along(ceil_div(w, TILE), shape.twl) * blend_tiles_along(ceil_div(h, TILE), shape.thl);
   DG_TRY(prepare(b, count, r->count, tiles_per_view, w * h));
+  b->shape = shape;
   std::vector<Camera> cameras(count);
   for (uint32_t k = 0; k < count; k++) {
     Camera& c = cameras[k];
@@ -206,7 +212,7 @@ dg_status render_batch(dg_renderer* r, dg_view_batch* b, const dg_camera* cams, 
   const float params[4] = {bg[0], bg[1], bg[2], 1.0f};
   DG_TRY(write_async(ctx, b->raster_params->ptr, params, sizeof(params)));
   for (int attempt = 0; attempt < 2; attempt++) {
-    const dg_view_batch::Key key{count, r->count, b->pair_capacity, coop_min, r->gaussians->ptr, targets,
+    const dg_view_batch::Key key{count, r->count, b->pair_capacity, coop_min, shape, r->gaussians->ptr, targets,
                                  b->keys->ptr};
     if (use_graph) {
       if (!b->graph || !(key == b->key)) {
@@ -264,7 +270,7 @@ dg_status check_views(dg_renderer* r, const dg_camera* cams, uint32_t count) {
 }  // namespace
 
 dg_status views_render(dg_renderer* r, const dg_camera* cams, uint32_t count, const float bg[3], uchar4* targets,
-                       float4* pixel_colors, uint32_t batch, uint32_t coop_min) {
+                       float4* pixel_colors, uint32_t batch, uint32_t coop_min, BlendShape shape) {
   DG_TRY(check_views(r, cams, count));
   dg_context* ctx = r->ctx;
   dg_view_batch* b = batch_of(r);
@@ -272,7 +278,7 @@ dg_status views_render(dg_renderer* r, const dg_camera* cams, uint32_t count, co
   const size_t pixels = (size_t)cams[0].viewport[0] * (uint32_t)cams[0].viewport[1];
   for (uint32_t first = 0; first < count; first += batch) {
     const uint32_t n = std::min(batch, count - first);
-    DG_TRY(render_batch(r, b, cams + first, n, bg, targets ? targets + first * pixels : nullptr, coop_min,
+    DG_TRY(render_batch(r, b, cams + first, n, bg, targets ? targets + first * pixels : nullptr, coop_min, shape,
                         r->view_graph));
     if (pixel_colors)
       DG_CUDA(cudaMemcpyAsync(pixel_colors + first * pixels, b->pixel_color->ptr, n * pixels * 16,
@@ -294,7 +300,8 @@ dg_status dg_renderer_render_views(dg_renderer* r, const dg_camera* cameras, uin
   DG_REQUIRE(!pixel_colors || pixel_colors->bytes >= pixels * count * 16,
              "pixel_colors hold fewer than count vec4 images");
   return views_render(r, cameras, count, background, targets ? typed<uchar4>(targets) : nullptr,
-                      pixel_colors ? typed<float4>(pixel_colors) : nullptr, r->view_batch, r->view_coop_min);
+                      pixel_colors ? typed<float4>(pixel_colors) : nullptr, r->view_batch, r->view_coop_min,
+                      r->view_shape);
 }
 
 dg_status dg_renderer_set_view_batching(dg_renderer* r, uint32_t batch, uint32_t coop_min, int32_t graph) {
@@ -312,10 +319,26 @@ dg_status dg_renderer_view_batching(const dg_renderer* r, uint32_t* batch, uint3
   return DG_OK;
 }
 
+dg_status dg_renderer_set_view_tile(dg_renderer* r, uint32_t width, uint32_t height) {
+  DG_REQUIRE(r, "NULL argument");
+  if ((width != 16 && width != 32) || (height != 16 && height != 32))
+    return fail(DG_ERROR_INVALID_ARGUMENT, "blend tiles are 16 or 32 pixels wide and 16 or 32 high");
+  r->view_shape = BlendShape{width == 32 ? 1u : 0u, height == 32 ? 1u : 0u};
+  return DG_OK;
+}
+
+dg_status dg_renderer_view_tile(const dg_renderer* r, uint32_t* width, uint32_t* height) {
+  DG_REQUIRE(r && width && height, "NULL argument");
+  *width = TILE << r->view_shape.twl;
+  *height = TILE << r->view_shape.thl;
+  return DG_OK;
+}
+
 // The autotuner: times every candidate (views per batch) x (cooperative
-// threshold) on the given views, each after a warm-up render, and keeps the
-// fastest for later dg_renderer_render_views calls. seconds[k] (optional, room
-// for 32) gets the time of candidate k in the order tried.
+// threshold) on the given views with 16x16 blend tiles, then the 32x16, 16x32
+// and 32x32 blend tiles at the fastest of those, each after a warm-up render,
+// and keeps the fastest for later dg_renderer_render_views calls. seconds[k]
+// (optional, room for 32) gets the time of candidate k in the order tried.
 dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint32_t count, const float background[3],
                                  dg_buffer* targets, uint32_t* best_batch, uint32_t* best_coop_min, double* seconds,
                                  uint32_t* tried) {
@@ -333,28 +356,41 @@ dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint3
   DG_CUDA(cudaEventCreate(&start));
   DG_CUDA(cudaEventCreate(&stop));
   double best = 1e30;
+  BlendShape best_shape{0u, 0u};
   uint32_t k = 0;
+  // One candidate: a warm-up render (sizes, graphs), then the timed one.
+  auto time_candidate = [&](uint32_t b, uint32_t t, BlendShape shape) -> dg_status {
+    DG_TRY(views_render(r, cameras, count, background, out, nullptr, b, t, shape));
+    DG_CUDA(cudaEventRecord(start, ctx->stream));
+    DG_TRY(views_render(r, cameras, count, background, out, nullptr, b, t, shape));
+    DG_CUDA(cudaEventRecord(stop, ctx->stream));
+    DG_CUDA(cudaEventSynchronize(stop));
+    float ms = 0.0f;
+    DG_CUDA(cudaEventElapsedTime(&ms, start, stop));
+    if (seconds && k < 32) seconds[k] = ms * 1e-3;
+    k++;
+    if (ms * 1e-3 < best) {
+      best = ms * 1e-3;
+      *best_batch = b;
+      *best_coop_min = t;
+      best_shape = shape;
+    }
+    return DG_OK;
+  };
   dg_status st = DG_OK;
   for (uint32_t b : batches) {
     for (uint32_t t : thresholds) {
-      st = views_render(r, cameras, count, background, out, nullptr, b, t);  // warm-up (sizes, graphs)
+      st = time_candidate(b, t, BlendShape{0u, 0u});
       if (st != DG_OK) break;
-      cudaEventRecord(start, ctx->stream);
-      st = views_render(r, cameras, count, background, out, nullptr, b, t);
-      if (st != DG_OK) break;
-      cudaEventRecord(stop, ctx->stream);
-      cudaEventSynchronize(stop);
-      float ms = 0.0f;
-      cudaEventElapsedTime(&ms, start, stop);
-      if (seconds && k < 32) seconds[k] = ms * 1e-3;
-      k++;
-      if (ms * 1e-3 < best) {
-        best = ms * 1e-3;
-        *best_batch = b;
-        *best_coop_min = t;
-      }
     }
     if (st != DG_OK) break;
+  }
+  if (st == DG_OK) {
+    const uint32_t b = *best_batch, t = *best_coop_min;
+    for (BlendShape shape : {BlendShape{1u, 0u}, BlendShape{0u, 1u}, BlendShape{1u, 1u}}) {
+      st = time_candidate(b, t, shape);
+      if (st != DG_OK) break;
+    }
   }
   cudaEventDestroy(start);
   cudaEventDestroy(stop);
@@ -362,6 +398,7 @@ dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint3
   if (st != DG_OK) return st;
   r->view_batch = *best_batch;
   r->view_coop_min = *best_coop_min;
+  r->view_shape = best_shape;
   return DG_OK;
 }
 

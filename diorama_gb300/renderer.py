@@ -221,16 +221,30 @@ class GaussianRenderer:
         _lib.call("dg_renderer_view_batching", self.handle, ctypes.byref(batch), ctypes.byref(coop))
         return {"batch": batch.value, "coopMin": coop.value}
 
+    def setViewTile(self, width: int = 16, height: int = 16) -> None:
+        """The blend tiles of batched views: 16 or 32 pixels each way. Images do
+        not change with them (each pixel blends its own 16x16 tile's list)."""
+        _lib.call("dg_renderer_set_view_tile", self.handle, width, height)
+
+    @property
+    def viewTile(self) -> tuple[int, int]:
+        width, height = c_uint32(), c_uint32()
+        _lib.call("dg_renderer_view_tile", self.handle, ctypes.byref(width), ctypes.byref(height))
+        return width.value, height.value
+
     def tuneViews(self, cameras: list[CameraData], background, targets: Buffer | None = None) -> dict:
-        """Times the (views per batch, cooperative threshold) candidates on these
-        views and keeps the fastest; returns it and every candidate's seconds."""
+        """Times the (views per batch, cooperative threshold) candidates with 16x16
+        blend tiles on these views, then the 32x16, 16x32 and 32x32 blend tiles at
+        the fastest, and keeps the fastest; returns it and every candidate's
+        seconds (in that order)."""
         arr = _cameras_c(cameras)
         batch, coop, tried = c_uint32(), c_uint32(), c_uint32()
         seconds = (c_double * 32)()
         _lib.call("dg_renderer_tune_views", self.handle, arr, len(cameras), _lib.floats(background),
                   targets.handle if targets is not None else None, ctypes.byref(batch), ctypes.byref(coop),
                   seconds, ctypes.byref(tried))
-        return {"batch": batch.value, "coopMin": coop.value, "seconds": list(seconds[: tried.value])}
+        return {"batch": batch.value, "coopMin": coop.value, "tile": self.viewTile,
+                "seconds": list(seconds[: tried.value])}
 
     @property
     def viewsPixelLast(self) -> Buffer | None:

@@ -219,13 +219,25 @@ dg_status dg_renderer_render_views(dg_renderer* r, const dg_camera* cameras, uin
  * default) and whether a batch replays as one CUDA graph. */
 dg_status dg_renderer_set_view_batching(dg_renderer* r, uint32_t batch, uint32_t coop_min, int32_t graph);
 dg_status dg_renderer_view_batching(const dg_renderer* r, uint32_t* batch, uint32_t* coop_min);
-/* The autotuner: times each (views per batch, cooperative threshold) candidate on
- * these views and keeps the fastest. seconds (NULL or room for 32) receives each
+/* The blend tiles of batched views, in pixels: 16 or 32 wide, 16 or 32 high
+ * (default 16x16, the reference's tile). A splat is listed once per blend tile its
+ * 16x16-tile rectangle touches, and each pixel blends only its own 16x16 tile's
+ * entries, so images are identical for every blend tile; larger ones make fewer
+ * pairs to sort and longer lists to walk. No reference counterpart: the
+ * reference renders one view at a time in 16x16 tiles
+ * (src/shaders/common.wgsl:29). */
+dg_status dg_renderer_set_view_tile(dg_renderer* r, uint32_t width, uint32_t height);
+dg_status dg_renderer_view_tile(const dg_renderer* r, uint32_t* width, uint32_t* height);
+/* The autotuner: times each (views per batch, cooperative threshold) candidate
+ * with 16x16 blend tiles on these views, then 32x16, 16x32 and 32x32 blend tiles
+ * at the fastest of those, and keeps the fastest (read the blend tile back with
+ * dg_renderer_view_tile). seconds (NULL or room for 32) receives each
  * candidate's time in the order tried; tried, how many were tried. */
 dg_status dg_renderer_tune_views(dg_renderer* r, const dg_camera* cameras, uint32_t count, const float background[3],
                                  dg_buffer* targets, uint32_t* best_batch, uint32_t* best_coop_min, double* seconds,
                                  uint32_t* tried);
-/* The last batch's pixel_last (views x pixels u32), for inspection. */
+/* The last batch's pixel_last (views x pixels u32), for inspection: positions in
+ * the blend tile's list (the 16x16 tile's with 16x16 blend tiles). */
 dg_buffer* dg_renderer_views_pixel_last(dg_renderer* r);
 
 /* ---- TrainingLoss (src/trainingLoss.ts:16-130): 0.8 L1 + 0.2 (1 - SSIM). */

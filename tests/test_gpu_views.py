@@ -4,7 +4,9 @@ held-out views one at a time, src/trainer.ts:371-386).
 Held-out views of the planes-and-boxes scene rendered together must give, view
 by view, the same pixel colours, last indices and rgba8 images as
 GaussianRenderer.encode, bit for bit: in one batch, in several, with and
-without graph replay, and with whatever the autotuner picks."""
+without graph replay, in blend tiles of 32x16, 16x32 and 32x32 pixels (pixel
+colours and images; the last indices then count positions in the blend tile's
+list), and with whatever the autotuner picks."""
 
 from __future__ import annotations
 
@@ -54,7 +56,7 @@ def small_scene(device):
     s[0].destroy()
 
 
-def _check(device, r, cams, colors, lasts, images, batch):
+def _check(device, r, cams, colors, lasts, images, batch, same_lists=True):
     W, H = cams[0].viewport
     n = len(cams)
     targets = device.createBuffer(n * W * H * 4)
@@ -69,7 +71,11 @@ def _check(device, r, cams, colors, lasts, images, batch):
     size = n - (batch * ((n - 1) // batch) if batch else 0)
     last = r.viewsPixelLast.read(np.uint32)[: size * W * H].reshape(size, -1)
     for j in range(size):
-        assert np.array_equal(last[j], lasts[n - size + j]), (batch, j)
+        want = lasts[n - size + j]
+        if same_lists:
+            assert np.array_equal(last[j], want), (batch, j)
+        else:  # positions in a longer list: a pixel blended something exactly where it did in 16x16 tiles
+            assert np.array_equal(last[j] > 0, want > 0) and np.all(last[j] >= want), (batch, j)
     targets.destroy()
     pixel_colors.destroy()
 
@@ -122,10 +128,40 @@ def test_300_views_in_one_batch(device):
     r.destroy()
 
 
+@pytest.mark.parametrize("tile", [(32, 16), (16, 32), (32, 32)])
+@pytest.mark.parametrize("batch,coop", [(0, 0), (4, 128)])
+def test_blend_tiles_match_single_view_renders(device, scene, small_scene, tile, batch, coop):
+    """Blend tiles of several 16x16 tiles: fewer pairs, longer lists, each block
+    keeping its own 16x16 tile's entries; the images must not change. The small
+    views (13 x 10 tiles) end in half-empty blend tiles; coop 128 sends many
+    tiles through the cooperative blend."""
+    for r, cams, colors, lasts, images in (scene, small_scene):
+        r.setViewTile(*tile)
+        assert r.viewTile == tile
+        r.setViewBatching(batch, coop, True)
+        _check(device, r, cams, colors, lasts, images, batch, same_lists=False)
+        _check(device, r, cams, colors, lasts, images, batch, same_lists=False)  # graph replay
+        r.setViewTile(16, 16)
+    assert device.check() == 0
+
+
+def test_view_tile_rejects_other_sizes(device, scene):
+    from diorama_gb300 import DioramaError
+    r = scene[0]
+    for bad in ((8, 8), (64, 16), (16, 0)):
+        with pytest.raises(DioramaError):
+            r.setViewTile(*bad)
+    assert r.viewTile == (16, 16)
+
+
 def test_autotuned_views_match(device, scene):
     r, cams, colors, lasts, images = scene
     tuned = r.tuneViews(cams, BG)
     assert tuned["batch"] in {1, 4, len(cams)} and tuned["coopMin"] in {128, 512, 1024, 2048}
-    assert len(tuned["seconds"]) >= 4 and min(tuned["seconds"]) > 0
+    assert tuned["tile"] in {(16, 16), (32, 16), (16, 32), (32, 32)}
+    # 3 batch sizes x 4 thresholds in 16x16 blend tiles, then 3 larger blend tiles.
+    assert len(tuned["seconds"]) == 15 and min(tuned["seconds"]) > 0
     assert r.viewBatching == {"batch": tuned["batch"], "coopMin": tuned["coopMin"]}
-    _check(device, r, cams, colors, lasts, images, tuned["batch"])
+    assert r.viewTile == tuned["tile"]
+    _check(device, r, cams, colors, lasts, images, tuned["batch"], same_lists=tuned["tile"] == (16, 16))
+    r.setViewTile(16, 16)
