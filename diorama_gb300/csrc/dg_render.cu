@@ -577,6 +577,23 @@ struct PixelBlend {
     return true;
   }
 
+  // blend() without branches, for the cooperative consumer: a splat this pixel
+  // does not take adds c * 0 (colours are non-negative, so the sums do not change)
+  // and keeps T and last. The same results as blend().
+  __device__ __forceinline__ void blend_queued(float alpha, float4 c, uint32_t pos) {
+    const float remaining = T * (1.0f - alpha);
+    const bool live = alpha != 0.0f && !done;
+    const bool stop = live && remaining < 0.0001f;
+    const bool take = live && !stop;
+    done = done || stop;
+    const float w = take ? __fmul_rn(alpha, T) : 0.0f;
+    r = __fmaf_rn(c.x, w, r);
+    g = __fmaf_rn(c.y, w, g);
+    b = __fmaf_rn(c.z, w, b);
+    T = take ? remaining : T;
+    last = take ? pos + 1 : last;
+  }
+
   // Applies up to 4 staged entries e[0..n) of `st` in list order. Sets bit
   // (position - base) of `blended` for each entry with a nonzero alpha at some
   // pixel of the warp that had not stopped: every entry a pixel blends, and at
@@ -682,10 +699,9 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     uint32_t* __restrict__ counters) {
   __shared__ WarpStage stages[FWD_WARPS];
   // Cooperative blending, double-buffered by round: each producer's queued entries
-  // (alpha per pixel, colour, position) and their count.
+  // (alpha per pixel; colour with the list position's bits in w) and their count.
   __shared__ float s_alpha[2][PRODUCERS][32][32];
   __shared__ float4 s_qcolor[2][PRODUCERS][32];
-  __shared__ uint32_t s_qpos[2][PRODUCERS][32];
   __shared__ uint32_t s_qlive[2][PRODUCERS];
   __shared__ uint32_t s_item, s_stop, s_done;  // s_done: warp 0's pixels that have stopped
   constexpr uint32_t BLOCK_SHIFT = 3u + TWL + THL, BLOCK_MASK = (1u << BLOCK_SHIFT) - 1u;
@@ -758,8 +774,8 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
             for (uint32_t u = 0; u < 4; u++) {
               if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
                 if (lane == 0) {
-                  s_qcolor[buf][pw][live] = st.color[e[u]];
-                  s_qpos[buf][pw][live] = st.pos[e[u]];
+                  const float4 c = st.color[e[u]];
+                  s_qcolor[buf][pw][live] = make_float4(c.x, c.y, c.z, __uint_as_float(st.pos[e[u]]));
                 }
                 s_alpha[buf][pw][live][lane] = alpha[u];
                 blended |= 1u << (st.pos[e[u]] - (start - run.x));
@@ -786,7 +802,10 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
           }
           const uint32_t n = s_qlive[prev][w];
 #pragma unroll 4
-          for (uint32_t m = 0; m < n; m++) pb.blend(s_alpha[prev][w][m][lane], s_qcolor[prev][w][m], s_qpos[prev][w][m]);
+          for (uint32_t m = 0; m < n; m++) {
+            const float4 q = s_qcolor[prev][w][m];
+            pb.blend_queued(s_alpha[prev][w][m][lane], q, __float_as_uint(q.w));
+          }
           const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
           if (lane == 0) *reinterpret_cast<volatile uint32_t*>(&s_done) = done;
         }

@@ -245,7 +245,10 @@ __device__ __forceinline__ bool rect_reachable(float A, float b, float C, float 
 // tile list together (3 computing alphas, 1 blending; 96 and 160 threads measured
 // slower: 331 and 363 us against 323 at 1.1M Gaussians); otherwise every warp
 // takes items of its own.
-constexpr uint32_t FWD_THREADS = 128;
+#ifndef DG_FWD_THREADS
+#define DG_FWD_THREADS 128
+#endif
+constexpr uint32_t FWD_THREADS = DG_FWD_THREADS;  // 96 or 128 (measured 324 and 288 us at 1.1M)
 constexpr uint32_t FWD_WARPS = FWD_THREADS / 32;
 constexpr uint32_t PRODUCERS = FWD_WARPS - 1;  // cooperative blending: warps computing alphas for warp 0
 constexpr uint32_t BWD_THREADS = 128;
