@@ -557,35 +557,18 @@ struct PixelBlend {
   }
 
   // Blends one splat of alpha `alpha` (0: not blended here) and colour c at list
-  // position pos; stops before the splat that would take the transmittance
-  // below 1e-4. Returns whether the pixel blended it.
-  __device__ __forceinline__ bool blend(float alpha, float4 c, uint32_t pos) {
-    if (alpha == 0.0f || done) return false;
-    const float remaining = T * (1.0f - alpha);
-    if (remaining < 0.0001f) {
-      done = true;
-      return false;
-    }
-    // color += c alpha T (src/shaders/rasterize.wgsl:88) as c (alpha T) + color,
-    // one fused multiply-add per channel (the oracle's same sequence).
-    const float w = __fmul_rn(alpha, T);
-    r = __fmaf_rn(c.x, w, r);
-    g = __fmaf_rn(c.y, w, g);
-    b = __fmaf_rn(c.z, w, b);
-    T = remaining;
-    last = pos + 1;
-    return true;
-  }
-
-  // blend() without branches, for the cooperative consumer: a splat this pixel
+  // position pos; stops before the splat that would take the transmittance below
+  // 1e-4 (src/shaders/rasterize.wgsl:62-92). Without branches: a splat the pixel
   // does not take adds c * 0 (colours are non-negative, so the sums do not change)
-  // and keeps T and last. The same results as blend().
-  __device__ __forceinline__ void blend_queued(float alpha, float4 c, uint32_t pos) {
+  // and keeps T and last.
+  __device__ __forceinline__ void blend(float alpha, float4 c, uint32_t pos) {
     const float remaining = T * (1.0f - alpha);
     const bool live = alpha != 0.0f && !done;
     const bool stop = live && remaining < 0.0001f;
     const bool take = live && !stop;
     done = done || stop;
+    // color += c alpha T (src/shaders/rasterize.wgsl:88) as c (alpha T) + color,
+    // one fused multiply-add per channel (the oracle's same sequence).
     const float w = take ? __fmul_rn(alpha, T) : 0.0f;
     r = __fmaf_rn(c.x, w, r);
     g = __fmaf_rn(c.y, w, g);
@@ -607,8 +590,11 @@ struct PixelBlend {
     const uint32_t any = __reduce_or_sync(0xffffffffu, mine);
 #pragma unroll
     for (uint32_t u = 0; u < 4; u++) {
-      if ((any >> u) & 1u) blended |= 1u << (st.pos[e[u]] - base);
-      if (alpha[u] != 0.0f) blend(alpha[u], st.color[e[u]], st.pos[e[u]]);
+      if ((any >> u) & 1u) {  // the same on every lane
+        const uint32_t pos = st.pos[e[u]];
+        blended |= 1u << (pos - base);
+        blend(alpha[u], st.color[e[u]], pos);
+      }
     }
   }
 };
@@ -770,18 +756,24 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
             const bool active = it.inside && !((done_mask >> lane) & 1u);
             float alpha[4];
             if (!pb.alphas4(st, e, staged - j, active, alpha)) continue;
-#pragma unroll
-            for (uint32_t u = 0; u < 4; u++) {
-              if (__any_sync(0xffffffffu, alpha[u] != 0.0f)) {
-                if (lane == 0) {
-                  const float4 c = st.color[e[u]];
-                  s_qcolor[buf][pw][live] = make_float4(c.x, c.y, c.z, __uint_as_float(st.pos[e[u]]));
-                }
-                s_alpha[buf][pw][live][lane] = alpha[u];
-                blended |= 1u << (st.pos[e[u]] - (start - run.x));
-                live++;
-              }
+            // Entry u is queued when some pixel's alpha is nonzero (then u < the
+            // entries left, and e[u] = j + u). Lane u < 4 queues entry u's colour and
+            // position and its blend-mask bit; every lane its alphas.
+            const uint32_t mine = (alpha[0] != 0.0f ? 1u : 0u) | (alpha[1] != 0.0f ? 2u : 0u) |
+                                  (alpha[2] != 0.0f ? 4u : 0u) | (alpha[3] != 0.0f ? 8u : 0u);
+            const uint32_t any = __reduce_or_sync(0xffffffffu, mine);
+            uint32_t bit = 0;
+            if (lane < 4 && ((any >> lane) & 1u)) {
+              const uint32_t slot = live + __popc(any & ((1u << lane) - 1u));
+              const float4 c = st.color[j + lane];
+              const uint32_t pos = st.pos[j + lane];
+              s_qcolor[buf][pw][slot] = make_float4(c.x, c.y, c.z, __uint_as_float(pos));
+              bit = 1u << (pos - (start - run.x));
             }
+            blended |= __reduce_or_sync(0xffffffffu, bit);
+#pragma unroll
+            for (uint32_t u = 0; u < 4; u++)
+              if ((any >> u) & 1u) s_alpha[buf][pw][live++][lane] = alpha[u];
           }
           if (lane == 0) {
             s_qlive[buf][pw] = live;
@@ -804,7 +796,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
 #pragma unroll 4
           for (uint32_t m = 0; m < n; m++) {
             const float4 q = s_qcolor[prev][w][m];
-            pb.blend_queued(s_alpha[prev][w][m][lane], q, __float_as_uint(q.w));
+            pb.blend(s_alpha[prev][w][m][lane], q, __float_as_uint(q.w));
           }
           const uint32_t done = __ballot_sync(0xffffffffu, pb.done);
           if (lane == 0) *reinterpret_cast<volatile uint32_t*>(&s_done) = done;
