@@ -21,7 +21,10 @@ namespace dg {
 // xyz, opacity, scale xyz, pad, rotation (w,x,y,z), color rgb, pad.
 constexpr uint32_t FLOATS_PER_GAUSSIAN = 16;
 // struct Splat2D (src/shaders/common.wgsl:20-26): mean xy, depth, radius, conic
-// (a,b,c), pad, color rgb, opacity.
+// (a,b,c), pad, color rgb, opacity. The reference leaves the pad unwritten; this
+// build's preprocess stores the splat's blend cutoff there (blend_cutoff, 0 when
+// culled), so the blend kernels read it instead of taking a log per tile.
+constexpr uint32_t SPLAT_CUTOFF_SLOT = 7;
 constexpr uint32_t FLOATS_PER_SPLAT = 12;
 // Spherical-harmonic coefficients 1..15, rgb each, coefficient-major (src/gaussians.ts:34-36).
 constexpr uint32_t SH_REST_FLOATS = 45;

@@ -85,7 +85,7 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
     }
   }
   out[0] = make_float4(mx, my, p.depth, radius);
-  out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, 0.0f);
+  out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, blend_cutoff(g[3]));
   out[2] = make_float4(fmaxf(color[0], 0.0f), fmaxf(color[1], 0.0f), fmaxf(color[2], 0.0f), g[3]);
   const uint4 rect = blend_rect(tile_rect(mx, my, radius, tile_grid(cam)), twl, thl);
   return Projected{(rect.z - rect.x) * (rect.w - rect.y), __float_as_uint(p.depth)};
@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
     uint32_t tiles_per_view, uchar4* __restrict__ target, float4* __restrict__ pixel_color,
     uint32_t* __restrict__ pixel_last, float4* __restrict__ checkpoints, uint32_t* __restrict__ blend_mask,
-    uint32_t* __restrict__ counters) {
+    uint32_t* __restrict__ counters, bool cut_in_record) {
   __shared__ WarpStage stages[FWD_WARPS];
   // Cooperative blending, double-buffered by round: each producer's queued entries
   // (alpha per pixel; colour with the list position's bits in w) and their count.
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
       if (warp > 0) {
         const uint32_t start = run.x + r * STRIDE + 32u * pw;
         if (r < rounds && start < run.y) {
-          const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, tm);
+          const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, cut_in_record, tm);
           {
             const uint32_t k = start + STRIDE + lane;
             stage_issue(st, splats, next_index, k < run.y);
@@ -840,7 +840,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
         save_checkpoints(checkpoints, run.x, next_k, next_k + 1, block, lane, pb.T, pb.r, pb.g, pb.b);
         next_k++;
       }
-      const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, tm);
+      const uint32_t staged = stage_commit(st, run.x, start, run.y, index, it.x0, it.y0, cut_in_record, tm);
       {
         const uint32_t k = start + 32u + lane;
         stage_issue(st, splats, next_index, k < run.y);
@@ -897,8 +897,10 @@ static dg_status make_pairs(dg_tile_rasterizer* tr, uint32_t capacity) {
 
 
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
-                            uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out) {
+                            uint32_t initial_pair_capacity, bool depth_first, bool own_splats,
+                            dg_tile_rasterizer** out) {
   auto* tr = new dg_tile_rasterizer();
+  tr->splat_cutoffs = own_splats;
   tr->ctx = ctx;
   tr->camera = camera;
   tr->splats = splats;
@@ -1044,6 +1046,7 @@ dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target) {
   f.checkpoints = typed<float4>(tr->checkpoints);
   f.blend_mask = typed<uint32_t>(tr->blend_mask);
   f.counters = typed<uint32_t>(tr->work);
+  f.splat_cutoffs = tr->splat_cutoffs;
   return blend_forward(ctx, f);
 }
 
@@ -1054,7 +1057,7 @@ static dg_status launch_rasterize_kernel(dg_context* ctx, const BlendForward& f)
   DG_LAUNCH(ctx, "rasterize",
             kernel<<<blend_grid(ctx, (const void*)kernel, FWD_THREADS, items), FWD_THREADS, 0, ctx->stream>>>(
                 f.camera, f.raster_params, f.splats, f.pair_splats, f.ranges, f.plan, f.tiles_per_view, f.target,
-                f.pixel_color, f.pixel_last, f.checkpoints, f.blend_mask, f.counters));
+                f.pixel_color, f.pixel_last, f.checkpoints, f.blend_mask, f.counters, f.splat_cutoffs));
   return DG_OK;
 }
 
@@ -1221,7 +1224,7 @@ static dg_status create_scene(dg_renderer* r, uint32_t count, dg_buffer* gaussia
   const uint32_t params[4] = {degree, 0, 0, 0};
   DG_TRY(write_async(r->ctx, r->scene_params->ptr, params, sizeof(params)));
   DG_TRY(alloc_buffer(r->ctx, (size_t)count * FLOATS_PER_SPLAT * 4, &r->splats));
-  DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, true, &r->rasterizer));
+  DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, true, true, &r->rasterizer));
   return DG_OK;
 }
 
@@ -1282,7 +1285,7 @@ dg_status dg_tile_rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffe
   DG_REQUIRE(ctx && camera && splats && out, "NULL argument");
   DG_REQUIRE(camera->bytes >= sizeof(Camera), "camera buffer is smaller than the 144-byte Camera uniform");
   DG_REQUIRE(splats->bytes >= (uint64_t)count * FLOATS_PER_SPLAT * 4, "splat buffer too small for count");
-  return rasterizer_create(ctx, camera, splats, count, initial_pair_capacity, false, out);
+  return rasterizer_create(ctx, camera, splats, count, initial_pair_capacity, false, false, out);
 }
 
 dg_status dg_tile_rasterizer_encode(dg_tile_rasterizer* tr, dg_buffer* target, const float viewport[2],

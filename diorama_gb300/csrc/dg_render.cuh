@@ -56,6 +56,7 @@ struct dg_tile_rasterizer {
   dg_buffer* checkpoints;
   dg_buffer* blend_mask;  // which entries each 8x4 block blended (dg_render.cu, publish_blended)
   uint32_t coop_min;      // tiles with more entries are blended by a whole CTA
+  bool splat_cutoffs;     // the splats come from this build's preprocess, cutoffs in slot 7
 };
 
 namespace dg {
@@ -70,8 +71,10 @@ dg_status rasterizer_queue_readback(dg_tile_rasterizer* tr);
 // Grows the pair buffers to 2^ceil(log2(1.25 * pairs)) if pairs exceed them.
 dg_status rasterizer_reserve_pairs(dg_tile_rasterizer* tr, uint64_t pairs);
 dg_status rasterizer_launch_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_grads, dg_buffer* splat_grads);
+// own_splats: `splats` is written by this build's preprocess (blend cutoffs in slot 7).
 dg_status rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
-                            uint32_t initial_pair_capacity, bool depth_first, dg_tile_rasterizer** out);
+                            uint32_t initial_pair_capacity, bool depth_first, bool own_splats,
+                            dg_tile_rasterizer** out);
 dg_status launch_rasterize(dg_tile_rasterizer* tr, dg_buffer* target);
 // Grid of a persistent blend kernel of `threads` threads per CTA over `items`
 // warp items.
@@ -104,6 +107,7 @@ struct BlendForward {
   uint32_t* blend_mask;
   uint32_t* counters;  // 4 words, cleared here
   BlendShape shape;
+  bool splat_cutoffs;  // the splats carry their blend cutoff (this build's preprocess wrote them)
 };
 dg_status blend_forward(dg_context* ctx, const BlendForward& f);
 // The batched views' stages (dg_render.cu; used by dg_views.cu).

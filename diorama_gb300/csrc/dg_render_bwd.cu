@@ -198,7 +198,8 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
     const uint2* __restrict__ chunks, const float4* __restrict__ pixel_color, const uint32_t* __restrict__ pixel_last,
     const float4* __restrict__ checkpoints, const uint32_t* __restrict__ blend_mask,
-    const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads, uint32_t* __restrict__ work_counter) {
+    const float4* __restrict__ pixel_grads, float* __restrict__ splat_grads, uint32_t* __restrict__ work_counter,
+    bool cut_in_record) {
   __shared__ WarpStage stages[BWD_WARPS];
   const uint32_t lane = threadIdx.x & 31u;
   WarpStage& st = stages[threadIdx.x >> 5];
@@ -258,7 +259,7 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     uint32_t next_bits = window_blended(blend_mask, next_lo, lo, block);
     uint32_t next_index = (next_bits >> lane) & 1u ? pair_splats[next_lo + lane] : 0u;
     while (end > chunk_lo) {
-      const uint32_t staged = stage_commit_blended(st, run.x, lo, index, bits);
+      const uint32_t staged = stage_commit_blended(st, run.x, lo, index, bits, cut_in_record);
       {
         stage_issue(st, splats, next_index, (next_bits >> lane) & 1u);
         end = lo;
@@ -753,7 +754,7 @@ dg_status launch_rasterize_backward(dg_tile_rasterizer* tr, dg_buffer* pixel_gra
                 typed<uint32_t>(tr->values), typed<uint2>(tr->ranges), typed<uint32_t>(tr->work_plan),
                 typed<uint2>(tr->chunks), typed<float4>(tr->pixel_color), typed<uint32_t>(tr->pixel_last),
                 typed<float4>(tr->checkpoints), typed<uint32_t>(tr->blend_mask), typed<float4>(pixel_grads),
-                typed<float>(splat_grads), counter));
+                typed<float>(splat_grads), counter, tr->splat_cutoffs));
   return DG_OK;
 }
 

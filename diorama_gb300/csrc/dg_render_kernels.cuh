@@ -412,9 +412,11 @@ struct TileMember {
 // the warp's block, whose pixel centers span [x0, x0 + 7] x [y0, y0 + 3] (and,
 // with a TileMember, belong to its 16x16 tile's list). Returns how many were
 // kept. All 32 lanes must call it. Every value read from `raw` is consumed before
-// this returns, so the caller may issue the next window at once.
+// this returns, so the caller may issue the next window at once. cut_in_record:
+// the splats carry their blend cutoff in slot SPLAT_CUTOFF_SLOT (this build's
+// preprocess wrote them), else it is computed here.
 __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, uint32_t lo, uint32_t hi,
-                                                 uint32_t index, float x0, float y0,
+                                                 uint32_t index, float x0, float y0, bool cut_in_record,
                                                  const TileMember& tm = TileMember{false, 0u, 0u, {0u, 0u}}) {
   cp_async_wait_all();
   const uint32_t lane = threadIdx.x & 31u;
@@ -427,10 +429,10 @@ __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, 
     color = st.raw[lane][2];
     mean = make_float2(s0.x, s0.y);
     const float A = -0.5f * s1.x, b = s1.y, C = -0.5f * s1.z;
-    const float cut = blend_cutoff(color.w);
+    const float cut = cut_in_record ? s1.w : blend_cutoff(color.w);
     quad = make_float4(A, b, C, cut);
-    keep = cut < 0.0f && rect_reachable(A, b, C, b / (2.0f * A), b / (2.0f * C), cut, x0 - mean.x, x0 + 7.0f - mean.x,
-                                        y0 - mean.y, y0 + 3.0f - mean.y);
+    keep = cut < 0.0f && rect_reachable(A, b, C, __fdividef(b, 2.0f * A), __fdividef(b, 2.0f * C), cut,
+                                        x0 - mean.x, x0 + 7.0f - mean.x, y0 - mean.y, y0 + 3.0f - mean.y);
     if (tm.member && keep) {
       const uint4 rect = tile_rect(mean.x, mean.y, s0.w, tm.tiles);
       keep = tm.tx >= rect.x && tm.tx < rect.z && tm.ty >= rect.y && tm.ty < rect.w;
@@ -464,7 +466,7 @@ __device__ __forceinline__ uint32_t read_blended(const uint32_t* __restrict__ ma
 // lane l keeps entry lo + l when bit l of `blended` is set (lanes past hi must
 // have it clear), with no rectangle test.
 __device__ __forceinline__ uint32_t stage_commit_blended(WarpStage& st, uint32_t run_x, uint32_t lo, uint32_t index,
-                                                         uint32_t blended) {
+                                                         uint32_t blended, bool cut_in_record) {
   cp_async_wait_all();
   const uint32_t lane = threadIdx.x & 31u;
   const bool keep = (blended >> lane) & 1u;
@@ -472,7 +474,7 @@ __device__ __forceinline__ uint32_t stage_commit_blended(WarpStage& st, uint32_t
     const uint32_t at = __popc(blended & ((1u << lane) - 1u));
     const float4 s0 = st.raw[lane][0], s1 = st.raw[lane][1], color = st.raw[lane][2];
     st.mean[at] = make_float2(s0.x, s0.y);
-    st.quad[at] = make_float4(-0.5f * s1.x, s1.y, -0.5f * s1.z, blend_cutoff(color.w));
+    st.quad[at] = make_float4(-0.5f * s1.x, s1.y, -0.5f * s1.z, cut_in_record ? s1.w : blend_cutoff(color.w));
     st.color[at] = color;
     st.pos[at] = lo + lane - run_x;
     st.index[at] = index;

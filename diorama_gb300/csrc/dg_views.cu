@@ -184,6 +184,7 @@ dg_status launch_batch(dg_renderer* r, dg_view_batch* b, uchar4* targets, uint32
   f.pixel_last = typed<uint32_t>(b->pixel_last);
   f.counters = typed<uint32_t>(b->work);
   f.shape = b->shape;
+  f.splat_cutoffs = true;  // preprocess_views_kernel's splats
   DG_TRY(blend_forward(ctx, f));
   DG_CUDA(cudaMemcpyAsync(b->pinned_total, b->scan_total->ptr, 4, cudaMemcpyDeviceToHost, ctx->stream));
   return DG_OK;

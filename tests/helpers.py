@@ -22,6 +22,26 @@ def cam_array(camera: CameraData) -> np.ndarray:
     return oracle.camera_array(camera.view, camera.proj, camera.viewport)
 
 
+def assert_splats_match(gpu, cpu) -> None:
+    """The renderer's splat records against the oracle's preprocess: bit for bit,
+    but for slot 7. The reference leaves that padding unwritten; the renderer's
+    preprocess stores each visible splat's blend cutoff there,
+    log(1 / (255 opacity)) - 1e-3 (0 when culled), computed with the GPU's logf,
+    so it is checked against the float64 value to 1e-6."""
+    g = np.asarray(gpu, np.float32).reshape(-1, 12)
+    c = np.asarray(cpu, np.float32).reshape(-1, 12)
+    mask = np.ones(12, bool)
+    mask[7] = False
+    assert np.array_equal(g[:, mask].view(np.uint32), c[:, mask].view(np.uint32))
+    visible = g[:, 3] != 0.0
+    with np.errstate(divide="ignore"):
+        want = np.log(1.0 / (255.0 * g[visible, 11].astype(np.float64))) - 1e-3
+    got = g[visible, 7].astype(np.float64)
+    same_inf = np.isinf(want) & (got == want)  # opacity 0: no pixel blends it
+    assert np.all(same_inf | (np.abs(got - want) <= 1e-6 * np.maximum(1.0, np.abs(want))))
+    assert np.all(g[~visible, 7] == 0.0)
+
+
 def random_scene(count: int, scale=(0.02, 0.4), opacity=(0.2, 0.95)) -> list[Gaussian]:
     """src/checks/tiles.ts:169-186: Gaussians scattered through the view."""
     random = mulberry32(11)

@@ -16,7 +16,7 @@ import pytest
 
 import oracle
 from diorama_gb300 import GaussianRenderer, TileRasterizer, TrainingLoss, scenes
-from helpers import GOLDEN, cam_array, group_errors
+from helpers import GOLDEN, assert_splats_match, cam_array, group_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +36,7 @@ def test_random_16k_forward_loss_backward(device):
 
     cam = cam_array(camera)
     frame = oracle.render(cam, np.zeros(3, np.float32), act, sh, 3)
-    assert np.array_equal(r.splatBuffer.read(np.float32).view(np.uint32), frame["splats"].view(np.uint32))
+    assert_splats_match(r.splatBuffer.read(np.float32), frame["splats"])
     assert np.array_equal(color.view(np.uint32), frame["pixel_color"].view(np.uint32))
     assert np.array_equal(r.pixelLastBuffer.read(np.uint32)[: W * H], frame["pixel_last"])
 
@@ -69,7 +69,7 @@ def test_random_1m_sort_scan_ranges_bit_exact(device):
     debug = tiles.debugBuffers
     cam = cam_array(camera)
     splats = r.splatBuffer.read(np.float32)
-    assert np.array_equal(splats.view(np.uint32), oracle.preprocess(cam, act, sh, 3).view(np.uint32))
+    assert_splats_match(splats, oracle.preprocess(cam, act, sh, 3))
     offsets, total, keys, values, ranges = oracle.tile_stage(cam, splats)
     assert total > 5_000_000
     # The renderer's depth-first tile sort: same pairs, order and ranges.
