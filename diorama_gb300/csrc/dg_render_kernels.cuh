@@ -228,17 +228,21 @@ __device__ __forceinline__ float blend_cutoff(float opacity) {
 // cutoff. The maximum is at the mean if the rectangle holds it, else on an edge,
 // where each 1D maximum is clamped to the edge. The margin covers the rounding
 // of both this maximum and the per-pixel power (a few ulps of the terms' sizes),
-// so a splat this rejects would have been skipped at every pixel anyway.
+// so a splat this rejects would have been skipped at every pixel anyway. The
+// quadratics are fused multiply-adds (one rounding each, inside that margin).
 __device__ __forceinline__ bool rect_reachable(float A, float b, float C, float kx, float ky, float cut, float dxl,
                                                float dxh, float dyl, float dyh) {
   if (dxl <= 0.0f && dxh >= 0.0f && dyl <= 0.0f && dyh >= 0.0f) return 0.0f >= cut;
-  auto q = [&](float dx, float dy) { return A * dx * dx + C * dy * dy - b * dx * dy; };
+  // (A dx - b dy) dx + C dy dy
+  auto q = [&](float dx, float dy) {
+    return __fmaf_rn(__fmaf_rn(A, dx, -__fmul_rn(b, dy)), dx, __fmul_rn(__fmul_rn(C, dy), dy));
+  };
   const float y1 = fminf(fmaxf(ky * dxl, dyl), dyh), y2 = fminf(fmaxf(ky * dxh, dyl), dyh);
   const float x1 = fminf(fmaxf(kx * dyl, dxl), dxh), x2 = fminf(fmaxf(kx * dyh, dxl), dxh);
   const float qmax = fmaxf(fmaxf(q(dxl, y1), q(dxh, y2)), fmaxf(q(x1, dyl), q(x2, dyh)));
   const float mx = fmaxf(fabsf(dxl), fabsf(dxh)), my = fmaxf(fabsf(dyl), fabsf(dyh));
-  const float terms = fabsf(A) * mx * mx + fabsf(C) * my * my + fabsf(b) * mx * my;
-  return qmax + 1e-6f * terms + 1e-6f >= cut;
+  const float terms = __fmaf_rn(__fmaf_rn(fabsf(A), mx, fabsf(b) * my), mx, fabsf(C) * my * my);
+  return __fmaf_rn(1e-6f, terms, qmax) + 1e-6f >= cut;
 }
 
 // CTA sizes of the blend kernels. The forward's 4 warps blend a block of a long
