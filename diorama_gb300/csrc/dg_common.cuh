@@ -64,6 +64,7 @@ static_assert(sizeof(Camera) == 144, "Camera is 144 bytes like the reference's u
 constexpr uint32_t DEVICE_ERROR_SCAN_WAIT = 1u << 0;
 constexpr uint32_t DEVICE_ERROR_SORT_WAIT = 1u << 1;
 constexpr uint32_t DEVICE_ERROR_COPY_WAIT = 1u << 2;  // a bulk copy's mbarrier
+constexpr uint32_t DEVICE_ERROR_MMA_WAIT = 1u << 3;   // a tensor-core product's mbarrier
 // Iteration cap of every spin on another block's status (about a second at worst).
 constexpr uint32_t SPIN_LIMIT = 1u << 22;
 
@@ -247,6 +248,30 @@ __device__ __forceinline__ float f2_hi(F2 a) {
   float hi;
   asm("{\n\t.reg .b32 lo;\n\tmov.b64 {lo, %0}, %1;\n\t}" : "=f"(hi) : "l"(a.v));
   return hi;
+}
+
+// ---- mbarriers in shared memory (bulk copies and tensor-core commits complete on them).
+__device__ __forceinline__ uint32_t smem_address(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t arrivals) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_address(bar)), "r"(arrivals) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(smem_address(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for phase `parity` of the barrier to complete, at most SPIN_LIMIT polls
+// (each try_wait may itself suspend the thread for a while). Returns false if it
+// gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t spin = 0; spin < SPIN_LIMIT; spin++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
 }
 
 // exp_blend_core of two values at once: the polynomial's fused multiply-adds run

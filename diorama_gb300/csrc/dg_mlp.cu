@@ -4,8 +4,13 @@
 // counterpart: the reference densifies by its gradient threshold alone
 // (src/shaders/densify.wgsl:72-85), which stays the fallback.
 //
-// Every product runs on the tensor cores as mma.sync m16n8k16 (BF16 in, FP32
-// accumulate), one warp per 16 samples:
+// Every product runs on the tensor cores with BF16 operands and FP32 accumulation:
+// - inference (mlp_predict_kernel, once per densification over every candidate):
+//   tcgen05.mma, 128 candidates a CTA, each layer one 128 x N product issued by
+//   one thread from shared-memory descriptors into tensor memory, read back with
+//   tcgen05.ld for the bias and GELU;
+// - training (mlp_train_kernel), as mma.sync m16n8k16, one warp per 16 samples
+//   (its backward needs the activations in registers per warp):
 // - forward: X W1, A1 W2, A2 W3, the outputs of one layer feeding the next as
 //   register fragments (the C fragments of two adjacent 8-column tiles are the A
 //   fragment of one 16-deep step);
@@ -172,28 +177,204 @@ __device__ __forceinline__ void forward16(const uint32_t (&ax)[4], const __nv_bf
   }
 }
 
-// P(children survive) for each candidate: softmax of the two logits.
-__global__ void __launch_bounds__(MLP_THREADS) mlp_predict_kernel(const float* __restrict__ features, uint32_t n,
-                                                                  const float* __restrict__ norm,
-                                                                  const __nv_bfloat16* __restrict__ packed,
-                                                                  const float* __restrict__ master,
-                                                                  float* __restrict__ survive) {
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t first = blockIdx.x * ROWS + warp * 16;
-  if (first >= n) return;  // warp-uniform
-  uint32_t ax[4];
-  float x[8];
-  load_input(features, nullptr, first, n, norm, lane, ax, x);
-  float z1[8][4], z2[8][4], z3[4];
-  forward16(ax, packed, master, lane, z1, z2, z3);
-  if ((lane & 3u) == 0) {
-    const uint32_t g = lane >> 2;
+// ---- Inference on the fifth-generation tensor cores (tcgen05). A CTA of 128
+// threads scores 128 candidates: each layer is one 128 x N x K product, issued by
+// one thread as K / 16 tcgen05.mma instructions (BF16 operands in shared memory,
+// FP32 accumulators in tensor memory), completed on an mbarrier; thread t then
+// reads accumulator row t back (tcgen05.ld), adds the bias, applies GELU and
+// writes the row's BF16 activations for the next layer's product.
+constexpr uint32_t TC_ROWS = 128;     // candidates per CTA: the products' M
+constexpr uint32_t TC_THREADS = 128;  // thread t owns row t (tensor-memory lane t)
+constexpr uint32_t TC_COLUMNS = 128;  // tensor-memory columns: layer 1 in [0, 64), 2 in [64, 128), 3 in [0, 16)
+constexpr uint32_t OUT_N = 16;        // layer 3's N, the smallest with M = 128 (outputs 0-1 real)
+
+// Element offset of (row r, column k) of a BF16 matrix with K columns kept as 8 x 8
+// core matrices (8 rows of 16 bytes, 128 contiguous bytes): core matrices along K
+// 128 bytes apart, groups of 8 rows (K / 8) * 128 bytes apart. The no-swizzle
+// K-major layout of the products' shared-memory descriptors.
+__device__ __forceinline__ uint32_t core_offset(uint32_t r, uint32_t k, uint32_t K) {
+  return (((r >> 3) * (K >> 3) + (k >> 3)) << 6) + ((r & 7u) << 3) + (k & 7u);
+}
+
+// Shared-memory matrix descriptor, no swizzle: start address, the byte distance
+// between core matrices along K (leading) and between 8-row groups (stride), and
+// the descriptor version (1) in bits 46-47.
+__device__ __forceinline__ uint64_t smem_descriptor(const void* start, uint32_t lead_bytes, uint32_t stride_bytes) {
+  const uint32_t a = smem_address(start);
+  return (uint64_t)((a >> 4) & 0x3FFFu) | ((uint64_t)((lead_bytes >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((stride_bytes >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and
+// B (bits 7-9 and 10-12 = 1), both K-major, N / 8 in bits 17-22, M / 16 in 24-28.
+constexpr uint32_t mma_descriptor(uint32_t m, uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+// D (+)= A B^T for one 16-deep step; A is M x 16 and B is N x 16, both K-major.
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                       bool accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"((uint32_t)accumulate)
+      : "memory");
+}
+// The barrier's one arrival once every tcgen05.mma this thread issued is complete.
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                   smem_address(bar))
+               : "memory");
+}
+// Columns [col, col + 16) of this warp's 32 tensor-memory lanes: lane t's values to thread t.
+__device__ __forceinline__ void tc_load16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const uint32_t r = first + g + 8 * h;
-      if (r < n) survive[r] = 1.0f / (1.0f + expf(z3[2 * h] - z3[2 * h + 1]));
-    }
+  for (int e = 0; e < 16; e++) v[e] = __uint_as_float(r[e]);
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+// Makes this thread's shared-memory writes visible to the tensor cores' reads.
+__device__ __forceinline__ void async_proxy_fence() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// Eight BF16 values from v[0..8) into 16 bytes of shared memory.
+__device__ __forceinline__ void store8(__nv_bfloat16* dst, const float* v) {
+  *reinterpret_cast<uint4*>(dst) = make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+}
+
+// Copies rows [0, rows_in) of a packed [rows][K] BF16 matrix into the core-matrix
+// layout, rows [rows_in, rows) as zeros. All threads take part.
+__device__ __forceinline__ void stage_weights(__nv_bfloat16* dst, const __nv_bfloat16* __restrict__ src,
+                                              uint32_t rows, uint32_t rows_in, uint32_t K) {
+  for (uint32_t i = threadIdx.x; i < rows * K / 8; i += blockDim.x) {
+    const uint32_t r = i / (K / 8), k = (i % (K / 8)) * 8;
+    const uint4 v = r < rows_in ? *reinterpret_cast<const uint4*>(src + (size_t)r * K + k) : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(dst + core_offset(r, k, K)) = v;
   }
+}
+
+// Waits for the products committed to `bar` (phase `parity`); false on every
+// thread if any gave up (DEVICE_ERROR_MMA_WAIT is then set).
+__device__ __forceinline__ bool tc_layer_done(uint64_t* bar, uint32_t parity, uint32_t* __restrict__ error) {
+  const bool ok = mbar_wait_bounded(bar, parity);
+  const bool failed = __syncthreads_or(!ok);
+  if (failed && threadIdx.x == 0) atomicOr(error, DEVICE_ERROR_MMA_WAIT);
+  tc_fence_after();
+  return !failed;
+}
+
+// Bias, then GELU, of 16 accumulator columns [c0, c0 + 16) of layer `bias`, as
+// BF16 row t of the next layer's A (K = HID).
+__device__ __forceinline__ void tc_hidden(uint32_t taddr, const float* __restrict__ bias, uint32_t c0,
+                                          __nv_bfloat16* h, uint32_t t) {
+  float v[16];
+  tc_load16(taddr, v);
+#pragma unroll
+  for (int e = 0; e < 16; e++) v[e] = gelu(v[e] + bias[c0 + e]);
+  store8(h + core_offset(t, c0, HID), v);
+  store8(h + core_offset(t, c0 + 8, HID), v + 8);
+}
+
+// P(children survive) for each candidate: softmax of the two logits.
+__global__ void __launch_bounds__(TC_THREADS) mlp_predict_kernel(const float* __restrict__ features, uint32_t n,
+                                                                 const float* __restrict__ norm,
+                                                                 const __nv_bfloat16* __restrict__ packed,
+                                                                 const float* __restrict__ master,
+                                                                 float* __restrict__ survive,
+                                                                 uint32_t* __restrict__ error) {
+  __shared__ __align__(128) __nv_bfloat16 s_x[TC_ROWS * IN_PAD];
+  __shared__ __align__(128) __nv_bfloat16 s_h[TC_ROWS * HID];  // layer 1's activations, then layer 2's
+  __shared__ __align__(128) __nv_bfloat16 s_w1[HID * IN_PAD];
+  __shared__ __align__(128) __nv_bfloat16 s_w2[HID * HID];
+  __shared__ __align__(128) __nv_bfloat16 s_w3[OUT_N * HID];
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+  const uint32_t t = threadIdx.x, warp = t >> 5;
+  const uint32_t row = blockIdx.x * TC_ROWS + t;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_address(&s_tmem)),
+                 "r"(TC_COLUMNS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (t == 0) mbar_init(&s_bar, 1);
+  {  // row t's normalized features (then zeros) as BF16
+    float x[IN_PAD];
+#pragma unroll
+    for (uint32_t c = 0; c < IN_PAD; c++)
+      x[c] = row < n && c < IN ? (features[(size_t)row * IN + c] - norm[c]) * norm[IN + c] : 0.0f;
+    store8(s_x + core_offset(t, 0, IN_PAD), x);
+    store8(s_x + core_offset(t, 8, IN_PAD), x + 8);
+  }
+  stage_weights(s_w1, packed + P_W1T, HID, HID, IN_PAD);
+  stage_weights(s_w2, packed + P_W2T, HID, HID, HID);
+  stage_weights(s_w3, packed + P_W3T, OUT_N, OUT_PAD, HID);
+  async_proxy_fence();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = s_tmem;
+  const uint32_t lanes = (warp * 32u) << 16;  // this warp's tensor-memory lanes
+  // Each 16-deep step takes the next two core matrices along K: 256 bytes on.
+  constexpr uint32_t STEP = 128;  // elements
+  bool ok = true;
+  if (t == 0) {
+    tc_mma(tmem, smem_descriptor(s_x, 128, 2 * 128), smem_descriptor(s_w1, 128, 2 * 128),
+           mma_descriptor(TC_ROWS, HID), false);
+    tc_commit(&s_bar);
+  }
+  ok = tc_layer_done(&s_bar, 0, error);
+  if (ok) {
+#pragma unroll
+    for (uint32_t c = 0; c < HID; c += 16) tc_hidden(tmem + lanes + c, master + OFF_B1, c, s_h, t);
+    async_proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (t == 0) {
+#pragma unroll
+      for (uint32_t q = 0; q < HID / 16; q++)
+        tc_mma(tmem + HID, smem_descriptor(s_h + q * STEP, 128, 8 * 128), smem_descriptor(s_w2 + q * STEP, 128, 8 * 128),
+               mma_descriptor(TC_ROWS, HID), q > 0);
+      tc_commit(&s_bar);
+    }
+    ok = tc_layer_done(&s_bar, 1, error);
+  }
+  if (ok) {
+#pragma unroll
+    for (uint32_t c = 0; c < HID; c += 16) tc_hidden(tmem + lanes + HID + c, master + OFF_B2, c, s_h, t);
+    async_proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (t == 0) {
+#pragma unroll
+      for (uint32_t q = 0; q < HID / 16; q++)
+        tc_mma(tmem, smem_descriptor(s_h + q * STEP, 128, 8 * 128), smem_descriptor(s_w3 + q * STEP, 128, 8 * 128),
+               mma_descriptor(TC_ROWS, OUT_N), q > 0);
+      tc_commit(&s_bar);
+    }
+    ok = tc_layer_done(&s_bar, 0, error);
+  }
+  if (ok) {
+    float z[16];
+    tc_load16(tmem + lanes, z);
+    if (row < n) survive[row] = 1.0f / (1.0f + expf((z[0] + master[OFF_B3]) - (z[1] + master[OFF_B3 + 1])));
+  } else {
+    mbar_wait_bounded(&s_bar, 0);  // a product still in flight after a give-up: one more bounded wait
+    mbar_wait_bounded(&s_bar, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_COLUMNS) : "memory");
 }
 
 // Forward and backward over `batch` samples order[first..first+batch): adds the
@@ -482,9 +663,9 @@ namespace dg {
 dg_status mlp_predict_launch(dg_densify_mlp* m, const float* features, uint32_t n, float* survive) {
   if (n == 0) return DG_OK;
   DG_LAUNCH(m->ctx, "mlp_predict",
-            mlp_predict_kernel<<<ceil_div(n, ROWS), MLP_THREADS, 0, m->ctx->stream>>>(
+            mlp_predict_kernel<<<ceil_div(n, TC_ROWS), TC_THREADS, 0, m->ctx->stream>>>(
                 features, n, typed<float>(m->norm), typed<__nv_bfloat16>(m->packed), typed<float>(m->master),
-                survive));
+                survive, m->ctx->device_error));
   return DG_OK;
 }
 

@@ -300,11 +300,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // ---- Bulk copies (the Tensor Memory Accelerator's untiled form) completed on an
 // mbarrier in shared memory.
-__device__ __forceinline__ uint32_t smem_address(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t arrivals) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_address(bar)), "r"(arrivals) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-}
 // One arrival that also announces `bytes` of copies the barrier waits for.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_address(bar)), "r"(bytes)
@@ -354,24 +349,6 @@ __device__ __forceinline__ void st_hinted(void* p, float4 v, uint64_t policy) {
   asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;\n" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
                "f"(v.w), "l"(policy)
                : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(done)
-      : "r"(smem_address(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-// Waits for phase `parity` of the barrier to complete, at most SPIN_LIMIT polls
-// (each try_wait may itself suspend the thread for a while). Returns false if it
-// gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t spin = 0; spin < SPIN_LIMIT; spin++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
 }
 
 // Starts copying n floats from global src to shared dst, spread over the CTA's

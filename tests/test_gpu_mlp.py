@@ -3,7 +3,7 @@ reference densifies by its gradient threshold alone, src/shaders/densify.wgsl,
 which stays the fallback).
 
 The model's tensor-core kernels against a NumPy restatement of the same BF16
-arithmetic (inference within 1e-3; the training kernel's weight and bias
+arithmetic (inference, on tcgen05, within 1e-3; the training kernel's weight and bias
 gradient values tensor by tensor; one AdamW step moves every weight with a
 clear gradient by lr against that gradient's sign), training on a separable rule, and
 the trainer: a model that is never confident reproduces the plain rule exactly,
@@ -72,17 +72,21 @@ def random_weights(rng, scale=0.3):
     return w
 
 
-def test_predict_matches_bf16_restatement(device):
+@pytest.mark.parametrize("count", [1, 127, 128, 129, 1000, 100_003])
+def test_predict_matches_bf16_restatement(device, count):
+    """Inference runs on tcgen05 (128 candidates a CTA, accumulators in tensor
+    memory): full, partial and single-candidate tiles, and many CTAs at once."""
     rng = np.random.default_rng(3)
     mlp = DensifyMLP(device, seed=1)
     w = random_weights(rng)
     mlp.setWeights(w)
     assert np.array_equal(mlp.weights(), w)
-    features = rng.normal(0, 1.5, (1000, MLP_FEATURES)).astype(np.float32)
+    features = rng.normal(0, 1.5, (count, MLP_FEATURES)).astype(np.float32)
     got = mlp.predictHost(features)
     z3 = forward(unpack(w), features)[-1]
     want = 1 / (1 + np.exp(z3[:, 0] - z3[:, 1]))
-    assert np.abs(got - want).max() <= 1e-3
+    assert got.shape == (count,) and np.abs(got - want).max() <= 1e-3
+    assert device.check() == 0  # no product's wait gave up
     mlp.destroy()
 
 
