@@ -58,13 +58,15 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-held-out", action="store_true", help="skip the held-out views' frames/s")
-    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn", "profile"],
+    ap.add_argument("--workload", default="train", choices=["train", "sort", "densify", "knn", "profile", "mlp"],
                     help="train: the headline training step; sort: the sort/scan/ranges stress "
                          "(1.1M random Gaussians at 1960x1090, the reference's 6-pass sort); densify: "
                          "plain vs learned densification on the planes-and-boxes scene (minutes); knn: the "
                          "starting Gaussians' nearest-neighbour distances of a point cloud; profile: one training "
-                         "step bracketed for a profiler started with collection off")
+                         "step bracketed for a profiler started with collection off; mlp: the learned "
+                         "densification's inference (tcgen05) over random candidates")
     ap.add_argument("--knn-points", type=int, default=1_100_000, help="knn workload: points in the cloud")
+    ap.add_argument("--candidates", type=int, default=1_100_000, help="mlp workload: candidates per call")
     ap.add_argument("--densify-steps", type=int, default=15_000,
                     help="learned-vs-plain comparison: steps per training run (the reference's 30,000-step "
                          "schedule scaled to this)")
@@ -694,6 +696,46 @@ def run_profile_step(args, rank, local):
     return result
 
 
+def run_mlp_inference(args, rank, local):
+    """The learned densification's inference (DensifyMLP.predict, tcgen05) on
+    `--candidates` random candidates with random weights, resident on the GPU:
+    --steps calls timed with CUDA events after --warmup."""
+    if rank != 0:
+        return None
+    import torch
+
+    torch.cuda.set_device(local)
+    from diorama_gb300 import DensifyMLP, Device
+    from diorama_gb300.training import MLP_FEATURES, MLP_PARAMS
+
+    device = Device(local)
+    rng = np.random.default_rng(1)
+    mlp = DensifyMLP(device, seed=1)
+    w = rng.normal(0, 0.3, MLP_PARAMS + 24).astype(np.float32)
+    w[MLP_PARAMS + 12:] = 1.0  # the input normalization's scales
+    mlp.setWeights(w)
+    n = args.candidates
+    features = device.upload(rng.normal(0, 1.5, (n, MLP_FEATURES)).astype(np.float32))
+    out = device.createBuffer(max(4, n * 4))
+    for _ in range(args.warmup):
+        mlp.predict(features, n, out)
+    device.synchronize()
+    start, end = device.event(), device.event()
+    start.record()
+    for _ in range(args.steps):
+        mlp.predict(features, n, out)
+    end.record()
+    us = start.elapsed_ms(end) * 1000.0 / args.steps
+    flops = 2.0 * (16 * 64 + 64 * 64 + 64 * 16) * n  # the padded product shapes
+    result = {"metric": "densification MLP inference", "candidates": n, "us_per_call": round(us, 1),
+              "tflops_padded": round(flops / us / 1e6, 1), "steps": args.steps, "warmup": args.warmup,
+              "device_errors": device.check()}
+    features.destroy()
+    out.destroy()
+    mlp.destroy()
+    return result
+
+
 def run_knn(args, rank, local):
     """The starting Gaussians' neighbour distances (src/loadDataset.ts:124-149) of
     a structure-from-motion-like cloud (clusters, a plane, 1% far outliers,
@@ -996,6 +1038,8 @@ def main():
         result = run_knn(args, rank, local) if args.impl == "ours" else None
     elif args.workload == "profile":
         result = run_profile_step(args, rank, local) if args.impl == "ours" else None
+    elif args.workload == "mlp":
+        result = run_mlp_inference(args, rank, local) if args.impl == "ours" else None
     elif args.impl == "reference":
         result = run_reference(args, rank, world, group)
     else:
