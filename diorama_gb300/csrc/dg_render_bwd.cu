@@ -168,11 +168,22 @@ __device__ __forceinline__ uint32_t window_start(uint32_t end, uint32_t floor) {
   return end - floor > 32u ? end - 32u : floor;
 }
 
-// The blend mask bits of window [lo, hi) for `block` (none when the window is empty).
-__device__ __forceinline__ uint32_t window_blended(const uint32_t* __restrict__ mask, uint32_t lo, uint32_t hi,
-                                                   uint32_t block) {
+// The blend mask words of `block` covering a chunk's positions [lo, hi) (at most
+// CHUNK / 32 + 1 words): lane l holds word (lo / 32) + l, or 0 past them.
+__device__ __forceinline__ uint32_t chunk_mask_words(const uint32_t* __restrict__ mask, uint32_t lo, uint32_t hi,
+                                                     uint32_t block, uint32_t lane) {
+  static_assert(CHUNK / 32 + 1 <= 32, "a chunk's mask words fit in the warp's lanes");
+  const uint32_t w = (lo >> 5) + lane;
+  return w <= ((hi - 1u) >> 5) ? mask[(size_t)w * 8u + block] : 0u;
+}
+
+// The blend mask bits of window [lo, hi) (none when it is empty) from the chunk's
+// words in the lanes (chunk_mask_words from position base). All lanes must call it.
+__device__ __forceinline__ uint32_t window_blended(uint32_t words, uint32_t base, uint32_t lo, uint32_t hi) {
+  const uint32_t at = (lo >> 5) - (base >> 5), shift = lo & 31u;
+  const uint32_t a = __shfl_sync(0xffffffffu, words, at & 31u), b = __shfl_sync(0xffffffffu, words, (at + 1u) & 31u);
   if (hi <= lo) return 0u;
-  const uint32_t bits = read_blended(mask, lo, block);
+  const uint32_t bits = shift ? (a >> shift) | (b << (32u - shift)) : a;
   return hi - lo >= 32u ? bits : bits & ((1u << (hi - lo)) - 1u);
 }
 
@@ -250,13 +261,14 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
     // Windows run back to front: [lo, end) with lo = max(chunk_lo, end - 32). Only
     // the entries some pixel of the block blended (the forward pass's mask) are
     // staged. This lane's entry of the window in flight and of the next one.
+    const uint32_t words = chunk_mask_words(blend_mask, chunk_lo, end_all, block, lane);
     uint32_t end = end_all;
     uint32_t lo = window_start(end, chunk_lo);
-    uint32_t bits = window_blended(blend_mask, lo, end, block);
+    uint32_t bits = window_blended(words, chunk_lo, lo, end);
     uint32_t index = (bits >> lane) & 1u ? pair_splats[lo + lane] : 0u;
     stage_issue(st, splats, index, (bits >> lane) & 1u);
     uint32_t next_lo = window_start(lo, chunk_lo);
-    uint32_t next_bits = window_blended(blend_mask, next_lo, lo, block);
+    uint32_t next_bits = window_blended(words, chunk_lo, next_lo, lo);
     uint32_t next_index = (next_bits >> lane) & 1u ? pair_splats[next_lo + lane] : 0u;
     while (end > chunk_lo) {
       const uint32_t staged = stage_commit_blended(st, run.x, lo, index, bits, cut_in_record);
@@ -267,7 +279,7 @@ __global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
         bits = next_bits;
         index = next_index;
         next_lo = window_start(lo, chunk_lo);
-        next_bits = window_blended(blend_mask, next_lo, lo, block);
+        next_bits = window_blended(words, chunk_lo, next_lo, lo);
         next_index = (next_bits >> lane) & 1u ? pair_splats[next_lo + lane] : 0u;
       }
       for (uint32_t slot = staged; slot > 0;) {

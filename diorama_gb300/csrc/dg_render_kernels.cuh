@@ -262,7 +262,10 @@ constexpr uint32_t BWD_WARPS = BWD_THREADS / 32;
 // CHUNK entries). A multiple of the 32-entry window.
 constexpr uint32_t CHUNK = 512;
 // Tiles with more entries than this are blended by a whole CTA in the forward pass.
-constexpr uint32_t COOP_MIN = 128;
+#ifndef DG_COOP_MIN
+#define DG_COOP_MIN 128
+#endif
+constexpr uint32_t COOP_MIN = DG_COOP_MIN;
 // The frame's work plan (dg_render.cu, plan_kernel): a header of PLAN_HEADER
 // words (cooperative tiles, tiles, backward chunks, spare), the tiles in the
 // order the forward pass takes them, then the backward's (tile, chunk) pairs.
@@ -432,16 +435,6 @@ __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, 
   return __popc(kept);
 }
 
-// The bits of positions [p0, p0 + 32) of the pair list in the blend mask of
-// 8x4 block `block`: bit p % 32 of word (p / 32) * 8 + block is set when some
-// pixel of the block blended pair p's splat in the forward pass.
-__device__ __forceinline__ uint32_t read_blended(const uint32_t* __restrict__ mask, uint32_t p0, uint32_t block) {
-  const uint32_t w = p0 >> 5, shift = p0 & 31u;
-  const uint32_t lo = mask[(size_t)w * 8u + block];
-  if (!shift) return lo;
-  const uint32_t hi = mask[(size_t)(w + 1) * 8u + block];
-  return (lo >> shift) | (hi << (32u - shift));
-}
 
 // Like stage_commit for a window whose entries the block blended are known:
 // lane l keeps entry lo + l when bit l of `blended` is set (lanes past hi must
