@@ -198,14 +198,16 @@ NCU_TRAFFIC = {"preprocess_backward_adam": 1_838_054_656, "preprocess": 313_713_
 
 
 # Algorithmic bytes per unit: what each kernel must move at minimum.
-def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6) -> float | None:
+def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, passes: int = 6,
+                      drawn: float = 0.0) -> float | None:
     return {
         # The preprocess backward fused with Adam: read the activated Gaussian 64, SH 180,
         # splat gradients 36 and visibility 4, raw parameters 56 and moments 472 (59 used
-        # slots); write SH 180, parameters 56, moments 472 and activated values 56. The
-        # densification statistics it also updates (up to 48 B, for drawn Gaussians
-        # only) are not counted.
-        "preprocess_backward_adam": 1576.0 * n,
+        # slots); write SH 180, parameters 56, moments 472 and activated values 56; and for
+        # each drawn Gaussian (splat radius > 0) the densification statistics it updates,
+        # every step like the reference (src/trainer.ts:230-234): read and write stats 16
+        # and aux 8.
+        "preprocess_backward_adam": 1576.0 * n + 48.0 * drawn,
         "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
         "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
         "sort_pass": 24.0 * pairs,  # per pass: read and write 8 B key + 4 B value
@@ -318,10 +320,15 @@ def run_ours(args, rank, world, local, group):
     device.synchronize()
     device.setKernelTiming(True)
     device.kernelTimingReport()
+    drawn_counts = []
     for _ in range(args.steps):
         trainer.step()
+        # Gaussians drawn this step (splat radius > 0): the fused kernel updates their statistics.
+        radius = trainer.renderer.splatBuffer.read(np.float32)[: trainer.count * 12].reshape(-1, 12)[:, 3]
+        drawn_counts.append(int(np.count_nonzero(radius)))
     report = device.kernelTimingReport()
     device.setKernelTiming(False)
+    drawn = float(np.mean(drawn_counts))
     pairs = trainer.renderer.tiles.lastPairCount
     n = trainer.count
     tiles = math.ceil(W / 16) * math.ceil(H / 16)
@@ -337,11 +344,12 @@ def run_ours(args, rank, world, local, group):
     dom_mem = max(memory_kernels, key=lambda k: kernels[k]["share"]) if memory_kernels else None
     if dom_mem:
         launches_per_step = kernels[dom_mem]["launches"] / args.steps
-        by = algorithmic_bytes(dom_mem, n, pairs, W * H, tiles)
+        by = algorithmic_bytes(dom_mem, n, pairs, W * H, tiles, drawn=drawn)
         achieved = by / (kernels[dom_mem]["avg_us"] * 1e-6) / 1e9
         roofline = {"kernel": dom_mem, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                     "unit": "GB/s", "frac": round(achieved / hbm_peak, 3), "peak_source": peak_source,
                     "algorithmic_bytes_per_launch": by, "launches_per_step": launches_per_step,
+                    "drawn_gaussians_per_step": round(drawn, 1),
                     "traffic": NCU_TRAFFIC.get(dom_mem) if n == 1_100_000 else None}
     # The blend's work: the splats each pixel walks, counted as the forward's
     # pixel_last (the 1-based position of the last splat the pixel blended) summed
@@ -688,6 +696,8 @@ def run_profile_step(args, rank, local):
     result = {"workload": "one training step for a profiler", "gaussians": trainer.count, "viewport": [W, H],
               "view": view, "warmup_steps": args.warmup, "pairs": trainer.renderer.tiles.lastPairCount,
               "blend_evaluations": int(last.astype(np.int64).sum()),
+              "drawn_gaussians": int(np.count_nonzero(
+                  trainer.renderer.splatBuffer.read(np.float32)[: trainer.count * 12].reshape(-1, 12)[:, 3])),
               "kernels_us": {k: round(1000 * t / c, 2) for k, (c, t) in report.items()}}
     trainer.destroy()
     for v in views:
