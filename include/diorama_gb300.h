@@ -152,8 +152,9 @@ dg_status dg_radix_sort_encode(dg_radix_sort* sort);
 dg_status dg_radix_sort_destroy(dg_radix_sort* sort);
 
 /* ---- TileRasterizer (src/tileRasterizer.ts:29-317). camera is a buffer holding the
- * 144-byte Camera uniform; splats FLOATS_PER_SPLAT floats each. initial_pair_capacity
- * 0 picks max(2^16, 8*count) as the reference does. */
+ * 144-byte Camera uniform; splats FLOATS_PER_SPLAT floats each (Splat2D,
+ * src/shaders/common.wgsl:20-26; its padding float, element 7, is not read).
+ * initial_pair_capacity 0 picks max(2^16, 8*count) as the reference does. */
 dg_status dg_tile_rasterizer_create(dg_context* ctx, dg_buffer* camera, dg_buffer* splats, uint32_t count,
                                     uint32_t initial_pair_capacity, dg_tile_rasterizer** out);
 /* target: rgba8 bytes (width*height*4), may be NULL. */
@@ -195,6 +196,9 @@ dg_status dg_renderer_encode_draw(dg_renderer* r, dg_buffer* target, dg_buffer* 
 dg_status dg_renderer_encode_backward(dg_renderer* r, dg_buffer* pixel_grads);
 dg_status dg_renderer_after_submit(dg_renderer* r, int32_t wait);
 uint32_t dg_renderer_count(const dg_renderer* r);
+/* The renderer's Splat2D records. Element 7, the padding the reference leaves
+ * unwritten, holds the splat's blend cutoff ln(1 / (255 opacity)) - 1e-3 (0 when
+ * culled), which the blend kernels read instead of computing it per tile. */
 dg_buffer* dg_renderer_splat_buffer(dg_renderer* r);
 dg_buffer* dg_renderer_gaussian_buffer(dg_renderer* r);
 dg_buffer* dg_renderer_sh_buffer(dg_renderer* r);
