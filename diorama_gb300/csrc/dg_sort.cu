@@ -26,7 +26,16 @@ namespace {
 
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / 32;
-constexpr int SORT_ITEMS = 15;
+#ifndef DG_SORT_ITEMS
+#define DG_SORT_ITEMS 15
+#endif
+#ifndef DG_SORT_MIN_BLOCKS
+#define DG_SORT_MIN_BLOCKS 3  // resident CTAs per SM the pass kernel's registers allow
+#endif
+// Keys per thread: 15 at 3 CTAs per SM measured fastest (per in-step pass 29.0 us,
+// 26M keys 1,319 us) against 8 and 11 (36.0, 30.8 us: smaller tiles, longer
+// look-backs) and 19 and 23 at 2 CTAs per SM (31.5, 30.7 us).
+constexpr int SORT_ITEMS = DG_SORT_ITEMS;
 constexpr uint32_t WARP_ITEMS = 32 * SORT_ITEMS;             // 480
 constexpr uint32_t SORT_TILE = SORT_THREADS * SORT_ITEMS;    // 3840
 constexpr uint32_t RADIX = 256;
@@ -140,7 +149,7 @@ __device__ __forceinline__ uint32_t block_exclusive_256(uint32_t v, uint32_t* s_
 }
 
 template <int KW>
-__global__ void __launch_bounds__(SORT_THREADS, 3)
+__global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
     sort_pass_kernel(const typename KeyOf<KW>::type* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                      typename KeyOf<KW>::type* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                      uint32_t capacity, const uint32_t* __restrict__ count, uint32_t shift,
