@@ -110,7 +110,7 @@ __device__ __forceinline__ void blend_terms(const WarpStage& st, uint32_t e0, ui
 // A pixel's state on its back-to-front walk: the transmittance in front of the
 // current splat, the colour composited behind it and the last splat passed.
 struct PixelBackward {
-  float Tf, T, pgx, pgy, pgz, bg_grad;
+  float T, pgx, pgy, pgz, tf_bg;  // tf_bg: the final T times (background . pixel gradient)
   float bhx, bhy, bhz;  // colour of everything behind
   float na, ncx, ncy, ncz;
 
@@ -118,12 +118,11 @@ struct PixelBackward {
   // composited behind, relative to T0, is `behind`.
   __device__ __forceinline__ void begin(float final_T, float T0, float3 behind, float gx, float gy, float gz,
                                         float4 bg) {
-    Tf = final_T;
     T = T0;
     pgx = gx;
     pgy = gy;
     pgz = gz;
-    bg_grad = bg.x * gx + bg.y * gy + bg.z * gz;
+    tf_bg = final_T * (bg.x * gx + bg.y * gy + bg.z * gz);
     bhx = behind.x;
     bhy = behind.y;
     bhz = behind.z;
@@ -138,23 +137,26 @@ struct PixelBackward {
     float inv;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(1.0f - alpha));
     T = T * inv;
-    bhx = na * ncx + (1.0f - na) * bhx;
-    bhy = na * ncy + (1.0f - na) * bhy;
-    bhz = na * ncz + (1.0f - na) * bhz;
+    // The colour behind, na nc + (1 - na) bh, as bh + na (nc - bh).
+    bhx = fmaf(na, ncx - bhx, bhx);
+    bhy = fmaf(na, ncy - bhy, bhy);
+    bhz = fmaf(na, ncz - bhz, bhz);
     na = alpha;
     ncx = c.x;
     ncy = c.y;
     ncz = c.z;
     const float dotv = (c.x - bhx) * pgx + (c.y - bhy) * pgy + (c.z - bhz) * pgz;
-    const float alpha_grad = T * dotv - Tf * inv * bg_grad;
+    const float alpha_grad = T * dotv - inv * tf_bg;
     const float power_grad = alpha_grad * c.w * G;
-    // The conic is (a, b, c) = (-2A, b, -2C).
-    const float ca = -2.0f * q.x, cb = q.y, cc = -2.0f * q.z;
-    w[0] = power_grad * (ca * dx + cb * dy);
-    w[1] = power_grad * (cb * dx + cc * dy);
-    w[2] = power_grad * (-0.5f * dx * dx);
-    w[3] = power_grad * (-dx * dy);
-    w[4] = power_grad * (-0.5f * dy * dy);
+    // The conic is (a, b, c) = (-2A, b, -2C): the power's gradient is
+    // -(a dx + b dy, b dx + c dy) for the mean and (-dx^2 / 2, -dx dy, -dy^2 / 2)
+    // for the conic, here as multiples of (power_grad dx, power_grad dy).
+    const float pdx = power_grad * dx, pdy = power_grad * dy;
+    w[0] = -2.0f * q.x * pdx + q.y * pdy;
+    w[1] = q.y * pdx - 2.0f * q.z * pdy;
+    w[2] = -0.5f * pdx * dx;
+    w[3] = -pdx * dy;
+    w[4] = -0.5f * pdy * dy;
     w[5] = alpha_grad * G;
     const float wt = alpha * T;
     w[6] = wt * pgx;
