@@ -530,13 +530,14 @@ struct PixelBlend {
   // no lane reaches any of the 4 cutoffs.
   __device__ __forceinline__ bool alphas4(const WarpStage& st, const uint32_t (&e)[4], uint32_t n, bool active,
                                           float (&alpha)[4]) const {
-    float power[4];
+    float power[4], opacity[4];
     bool need[4], any = false;
 #pragma unroll
     for (uint32_t u = 0; u < 4; u++) {
-      const float2 m = st.mean[e[u]];
+      const float4 m = st.mean[e[u]];
       const float4 q = st.quad[e[u]];
       power[u] = blend_power(q.x, q.y, q.z, cx - m.x, cy - m.y);
+      opacity[u] = m.z;
       need[u] = active && u < n && power[u] >= q.w && power[u] <= 0.0f;
       any |= need[u];
     }
@@ -550,7 +551,7 @@ struct PixelBlend {
     exp_blend_core2(need[2] ? power[2] : 0.0f, need[3] ? power[3] : 0.0f, G[2], G[3]);
 #pragma unroll
     for (uint32_t u = 0; u < 4; u++) {
-      const float a = fminf(0.99f, st.color[e[u]].w * G[u]);
+      const float a = fminf(0.99f, opacity[u] * G[u]);
       alpha[u] = need[u] && a >= 1.0f / 255.0f ? a : 0.0f;
     }
     return true;

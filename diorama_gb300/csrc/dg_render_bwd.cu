@@ -90,7 +90,7 @@ struct BlendTerm {
 // The terms of two entries at once (their exps as one packed pair).
 __device__ __forceinline__ void blend_terms(const WarpStage& st, uint32_t e0, uint32_t e1, bool eligible0,
                                             bool eligible1, float cx, float cy, BlendTerm& t0, BlendTerm& t1) {
-  const float2 m0 = st.mean[e0], m1 = st.mean[e1];
+  const float4 m0 = st.mean[e0], m1 = st.mean[e1];  // .z: opacity
   const float4 q0 = st.quad[e0], q1 = st.quad[e1];
   t0.dx = cx - m0.x;
   t0.dy = cy - m0.y;
@@ -101,8 +101,8 @@ __device__ __forceinline__ void blend_terms(const WarpStage& st, uint32_t e0, ui
   const bool need0 = eligible0 && power0 >= q0.w && power0 <= 0.0f;
   const bool need1 = eligible1 && power1 >= q1.w && power1 <= 0.0f;
   exp_blend_core2(need0 ? power0 : 0.0f, need1 ? power1 : 0.0f, t0.G, t1.G);
-  t0.alpha = fminf(0.99f, __fmul_rn(st.color[e0].w, t0.G));
-  t1.alpha = fminf(0.99f, __fmul_rn(st.color[e1].w, t1.G));
+  t0.alpha = fminf(0.99f, __fmul_rn(m0.z, t0.G));
+  t1.alpha = fminf(0.99f, __fmul_rn(m1.z, t1.G));
   t0.blended = need0 && t0.alpha >= 1.0f / 255.0f;
   t1.blended = need1 && t1.alpha >= 1.0f / 255.0f;
 }
@@ -206,7 +206,7 @@ __device__ __forceinline__ uint32_t window_blended(uint32_t words, uint32_t base
 // gradient shares of the pair are summed over the warp's 32 pixels in one
 // reduce-scatter and added to the splats' global gradients, one atomic add per
 // nonzero total.
-__global__ void __launch_bounds__(BWD_THREADS) rasterize_backward_kernel(
+__global__ void __launch_bounds__(BWD_THREADS, 6) rasterize_backward_kernel(
     const Camera* __restrict__ camera, const float4* __restrict__ raster_params, const float* __restrict__ splats,
     const uint32_t* __restrict__ pair_splats, const uint2* __restrict__ ranges, const uint32_t* __restrict__ plan,
     const uint2* __restrict__ chunks, const float4* __restrict__ pixel_color, const uint32_t* __restrict__ pixel_last,

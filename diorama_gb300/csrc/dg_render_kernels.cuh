@@ -276,7 +276,7 @@ constexpr uint32_t PLAN_HEADER = 4;
 // order. `raw` receives the splat records of the next window by cp.async while
 // the current one blends.
 struct WarpStage {
-  float2 mean[32];
+  float4 mean[32];   // mean x, y, opacity, 0
   float4 quad[32];   // A = -0.5 a, b, C = -0.5 c, cutoff
   float4 color[32];  // rgb, opacity
   uint32_t pos[32];  // position in the tile's list
@@ -425,7 +425,7 @@ __device__ __forceinline__ uint32_t stage_commit(WarpStage& st, uint32_t run_x, 
   const uint32_t kept = __ballot_sync(0xffffffffu, keep);
   if (keep) {
     const uint32_t at = __popc(kept & ((1u << lane) - 1u));
-    st.mean[at] = mean;
+    st.mean[at] = make_float4(mean.x, mean.y, color.w, 0.0f);
     st.quad[at] = quad;
     st.color[at] = color;
     st.pos[at] = k - run_x;
@@ -447,7 +447,7 @@ __device__ __forceinline__ uint32_t stage_commit_blended(WarpStage& st, uint32_t
   if (keep) {
     const uint32_t at = __popc(blended & ((1u << lane) - 1u));
     const float4 s0 = st.raw[lane][0], s1 = st.raw[lane][1], color = st.raw[lane][2];
-    st.mean[at] = make_float2(s0.x, s0.y);
+    st.mean[at] = make_float4(s0.x, s0.y, color.w, 0.0f);
     st.quad[at] = make_float4(-0.5f * s1.x, s1.y, -0.5f * s1.z, cut_in_record ? s1.w : blend_cutoff(color.w));
     st.color[at] = color;
     st.pos[at] = lo + lane - run_x;
