@@ -949,6 +949,11 @@ dg_status rasterizer_prepare(dg_tile_rasterizer* tr, const float viewport[2], co
   tr->viewport[0] = viewport[0];
   tr->viewport[1] = viewport[1];
   const uint32_t tiles = tiles_x * tiles_y;
+  // The depth-first path's tile keys are tile indices below `tiles`: its last
+  // pass sorts 4 bits when they cover the rest (up to 4096 tiles).
+  uint32_t tile_bits = 1;
+  while (tile_bits < 32 && (1u << tile_bits) < tiles) tile_bits++;
+  sort_plan_key_bits(tr->tile_plan, tile_bits);
   if (!tr->ranges || tr->ranges_tiles < tiles) {
     free_buffer(tr->ranges);
     tr->ranges = nullptr;

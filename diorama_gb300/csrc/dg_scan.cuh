@@ -22,6 +22,7 @@ struct SortPlan {
   uint32_t high_bits;
   uint32_t passes;     // even in the reference's plans, so the result lands back in keys/values
   uint32_t shift[8];   // bit offset of each pass's 8-bit digit within the key
+  bool narrow_last;    // the key's bits above the last pass's low 4 are all zero: a 4-bit last pass
 };
 SortPlan sort_plan(uint32_t capacity, uint32_t high_bits);
 // u32 keys of which only the low `bits` bits vary (bits a multiple of 16).
@@ -30,6 +31,9 @@ SortPlan sort_plan_low_bits(uint32_t capacity, uint32_t bits);
 // keys) or all 32 low-word bits plus `bits` high-word bits (u64 keys). With an
 // odd number of passes the result lands in keys_alt/values_alt.
 SortPlan sort_plan_digits(uint32_t capacity, uint32_t key_words, uint32_t bits);
+// Tells a plan that only the key's low `bits` bits (of the low and high words
+// together) vary; its last pass then sorts a 4-bit digit when that covers them.
+void sort_plan_key_bits(SortPlan& p, uint32_t bits);
 // Per-device kernel attributes; called once when a context is created.
 dg_status sort_init();
 size_t sort_scratch_bytes(const SortPlan& plan);

@@ -148,7 +148,10 @@ __device__ __forceinline__ uint32_t block_exclusive_256(uint32_t v, uint32_t* s_
   return before + incl - v;
 }
 
-template <int KW>
+// One pass over digits of DBITS bits (8, or 4 for a last pass whose key bits
+// above it are all zero): fewer ballots per key, and with 16 digits the per-tile
+// prefix work and look-back run on 16 threads instead of 256.
+template <int KW, int DBITS>
 __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
     sort_pass_kernel(const typename KeyOf<KW>::type* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                      typename KeyOf<KW>::type* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
@@ -165,6 +168,7 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
   uint32_t* s_tmp = s_base + RADIX;
   __shared__ uint32_t s_tile;
 
+  constexpr uint32_t DIGITS = 1u << DBITS, DMASK = DIGITS - 1u;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t n = count ? min(*count, capacity) : capacity;
   const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
@@ -188,14 +192,14 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
     val[j] = valid ? vals_in[idx] : 0u;
   }
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint32_t* my_hist = s_whist + warp * RADIX;
+  uint32_t* my_hist = s_whist + warp * DIGITS;
 #pragma unroll
   for (int j = 0; j < SORT_ITEMS; j++) {
     bool valid = base + j * 32 < n;
-    uint32_t d = (uint32_t)(key[j] >> shift) & 0xffu;
+    uint32_t d = (uint32_t)(key[j] >> shift) & DMASK;
     uint32_t peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
-    for (int b = 0; b < 8; b++) {
+    for (int b = 0; b < DBITS; b++) {
       uint32_t bit = (d >> b) & 1u;
       uint32_t vote = __ballot_sync(0xffffffffu, bit);
       peers &= bit ? vote : ~vote;
@@ -212,26 +216,30 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
   }
   __syncthreads();
 
-  // Per digit (thread = digit): offsets of each warp's run, and the tile's count.
+  // Per digit (thread = digit, threads past the digits idle): offsets of each
+  // warp's run, and the tile's count.
   const uint32_t d = tid;
+  const bool digit = d < DIGITS;
   uint32_t running = 0;
+  if (digit) {
 #pragma unroll
-  for (int w = 0; w < SORT_WARPS; w++) {
-    uint32_t c = s_whist[w * RADIX + d];
-    s_whist[w * RADIX + d] = running;
-    running += c;
+    for (int w = 0; w < SORT_WARPS; w++) {
+      uint32_t c = s_whist[w * DIGITS + d];
+      s_whist[w * DIGITS + d] = running;
+      running += c;
+    }
+    store_status(&status[tile * RADIX + d], (tile == 0 ? FLAG_PREFIX : FLAG_AGGREGATE) | running);
   }
   const uint32_t tile_count = running;
-  store_status(&status[tile * RADIX + d], (tile == 0 ? FLAG_PREFIX : FLAG_AGGREGATE) | tile_count);
   const uint32_t block_start = block_exclusive_256(tile_count, s_tmp);
-  const uint32_t global_start = block_exclusive_256(pass_hist[d], s_tmp);
-  s_block_start[d] = block_start;
+  const uint32_t global_start = block_exclusive_256(digit ? pass_hist[d] : 0u, s_tmp);
+  if (digit) s_block_start[d] = block_start;
 
   // Decoupled look-back over earlier tiles, for this thread's digit: the states
   // of LOOK_WIDTH predecessors are read together (one round trip instead of
   // LOOK_WIDTH), then taken in order back to the first inclusive prefix.
   uint32_t prefix = 0;
-  if (tile > 0) {
+  if (digit && tile > 0) {
     int32_t look = (int32_t)tile - 1;
     uint32_t spins = 0;
     bool found = false;
@@ -259,15 +267,15 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
     }
     store_status(&status[tile * RADIX + d], FLAG_PREFIX | ((prefix + tile_count) & VALUE_MASK));
   }
-  s_base[d] = global_start + prefix - block_start;
+  if (digit) s_base[d] = global_start + prefix - block_start;
   __syncthreads();
 
   // Place each key at its rank within the tile, grouped by digit.
 #pragma unroll
   for (int j = 0; j < SORT_ITEMS; j++) {
     if (base + j * 32 < n) {
-      uint32_t dj = (uint32_t)(key[j] >> shift) & 0xffu;
-      uint32_t pos = s_block_start[dj] + s_whist[warp * RADIX + dj] + rank[j];
+      uint32_t dj = (uint32_t)(key[j] >> shift) & DMASK;
+      uint32_t pos = s_block_start[dj] + s_whist[warp * DIGITS + dj] + rank[j];
       s_keys[pos] = key[j];
       s_vals[pos] = val[j];
     }
@@ -276,7 +284,7 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
   const uint32_t here = min(SORT_TILE, n - tile * SORT_TILE);
   for (uint32_t k = tid; k < here; k += SORT_THREADS) {
     K kk = s_keys[k];
-    uint32_t dk = (uint32_t)(kk >> shift) & 0xffu;
+    uint32_t dk = (uint32_t)(kk >> shift) & DMASK;
     uint32_t out = s_base[dk] + k;
     // Only a look-back that gave up (error bit already set) can place a key
     // outside the output; drop it rather than write out of bounds.
@@ -329,8 +337,9 @@ dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32
   K* out_k = static_cast<K*>(keys_alt);
   uint32_t* out_v = values_alt;
   for (uint32_t p = 0; p < plan.passes; p++) {
+    const auto kernel = plan.narrow_last && p + 1 == plan.passes ? sort_pass_kernel<KW, 4> : sort_pass_kernel<KW, 8>;
     DG_LAUNCH(ctx, "sort_pass",
-              sort_pass_kernel<KW><<<l.max_tiles, SORT_THREADS, smem, ctx->stream>>>(
+              kernel<<<l.max_tiles, SORT_THREADS, smem, ctx->stream>>>(
                   in_k, in_v, out_k, out_v, plan.capacity, count, shifts.shift[p], hist + p * RADIX,
                   status + (size_t)p * l.max_tiles * RADIX, tickets + p, ctx->device_error));
     std::swap(in_k, out_k);
@@ -343,9 +352,13 @@ dg_status launch_typed(dg_context* ctx, const SortPlan& plan, void* keys, uint32
 
 dg_status sort_init() {
   // The pass kernels use more than the default 48 KB of dynamic shared memory.
-  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<1, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)pass_smem_bytes<1>()));
-  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pass_smem_bytes<1>()));
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<2, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pass_smem_bytes<2>()));
+  DG_CUDA(cudaFuncSetAttribute(sort_pass_kernel<2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)pass_smem_bytes<2>()));
   return DG_OK;
 }
@@ -377,7 +390,14 @@ SortPlan sort_plan_digits(uint32_t capacity, uint32_t key_words, uint32_t bits) 
   p.high_bits = key_words == 2 ? bits : 0;
   p.passes = key_words == 2 ? 4 + (bits + 7) / 8 : std::max(1u, (bits + 7) / 8);
   for (uint32_t k = 0; k < p.passes; k++) p.shift[k] = k * 8;
+  sort_plan_key_bits(p, key_words == 2 ? 32 + bits : bits);
   return p;
+}
+
+void sort_plan_key_bits(SortPlan& p, uint32_t bits) {
+  // The last pass's digit: bits [shift, shift + 8) of the key; only `bits` vary.
+  const uint32_t last = p.shift[p.passes - 1];
+  p.narrow_last = bits <= last + 4;
 }
 
 size_t sort_scratch_bytes(const SortPlan& plan) { return layout_of(plan).total; }
