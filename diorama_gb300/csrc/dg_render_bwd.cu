@@ -584,7 +584,6 @@ __global__ void __launch_bounds__(PBWD_THREADS) preprocess_backward_kernel(
 #endif
 
 __device__ __forceinline__ float4 f4_load(const float* p) { return *reinterpret_cast<const float4*>(p); }
-__device__ __forceinline__ void f4_store(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
 // The training step's preprocess backward with Adam applied at once
 // (src/shaders/preprocessBackward.wgsl:28-181, then src/shaders/adam.wgsl:80-107).
