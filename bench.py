@@ -194,7 +194,7 @@ def build_scene(args):
 # `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
 # --clock-control none --profile-from-start off -k regex:<kernel> -c 1
 # python bench.py --workload profile --views 8 --warmup 3`.
-NCU_TRAFFIC = {"preprocess_backward_adam": 1_838_054_656, "preprocess": 313_713_664}
+NCU_TRAFFIC = {"preprocess_backward_adam": 1_781_186_048, "preprocess": 315_799_040}
 
 
 # Algorithmic bytes per unit: what each kernel must move at minimum.
@@ -208,7 +208,7 @@ def algorithmic_bytes(name: str, n: int, pairs: int, pixels: int, tiles: int, pa
         # every step like the reference (src/trainer.ts:230-234): read and write stats 16
         # and aux 8.
         "preprocess_backward_adam": 1576.0 * n + 48.0 * drawn,
-        "preprocess": 296.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4
+        "preprocess": 300.0 * n,  # read Gaussian 64 + SH 180, write splat 48 + tile count 4 + radius 4
         "preprocess_backward": (64 + 180 + 48 + 36 + 64 + 180) * float(n),
         "sort_pass": 24.0 * pairs,  # per pass: read and write 8 B key + 4 B value
         "sort_histogram": 8.0 * pairs,

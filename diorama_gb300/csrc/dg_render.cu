@@ -31,6 +31,7 @@ __device__ __forceinline__ void load_camera(Camera& dst, const Camera* src) {
 // of views) and its depth's bits (0 when culled).
 struct Projected {
   uint32_t tiles, depth_bits;
+  float radius;  // 0 when culled
 };
 
 __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const float (&g)[16], const float* shv,
@@ -41,7 +42,7 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
     out[0] = zero;
     out[1] = zero;
     out[2] = zero;
-    return Projected{0u, 0u};
+    return Projected{0u, 0u, 0.0f};
   };
   if (-view_z(cam, g) <= 0.2f) return culled();
   Projection p;
@@ -88,7 +89,7 @@ __device__ __forceinline__ Projected preprocess_one(const Camera& cam, const flo
   out[1] = make_float4(p.c / p.det, -p.b / p.det, p.a / p.det, blend_cutoff(g[3]));
   out[2] = make_float4(fmaxf(color[0], 0.0f), fmaxf(color[1], 0.0f), fmaxf(color[2], 0.0f), g[3]);
   const uint4 rect = blend_rect(tile_rect(mx, my, radius, tile_grid(cam)), twl, thl);
-  return Projected{(rect.z - rect.x) * (rect.w - rect.y), __float_as_uint(p.depth)};
+  return Projected{(rect.z - rect.x) * (rect.w - rect.y), __float_as_uint(p.depth), radius};
 }
 
 // Stages the SH coefficients of Gaussians [first, first + n) into shared memory
@@ -114,7 +115,9 @@ __device__ __forceinline__ void load_gaussian(const float* __restrict__ gaussian
 // One thread per Gaussian, one view. When tile_counts is given, the tiles each
 // splat touches are written too (src/shaders/tiles.wgsl:24-35, fused); when
 // depth_keys is given, the depth's bits (0 when culled) and the splat's index,
-// the input of the depth sort.
+// the input of the depth sort; when radii is given, each splat's radius densely
+// (the training step's fused backward reads it there, not from the 48-byte
+// splat records).
 //
 // Persistent CTAs over blocks of PRE_THREADS Gaussians: while a CTA projects one
 // block, the next block's SH coefficients are already copying into the other
@@ -128,7 +131,8 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
                                                                  float* __restrict__ splats,
                                                                  uint32_t* __restrict__ tile_counts,
                                                                  uint32_t* __restrict__ depth_keys,
-                                                                 uint32_t* __restrict__ depth_order) {
+                                                                 uint32_t* __restrict__ depth_order,
+                                                                 float* __restrict__ radii) {
   __shared__ Camera s_cam;
   __shared__ __align__(16) float s_sh[2][PRE_THREADS * SH_REST_FLOATS];
   load_camera(s_cam, camera);
@@ -159,6 +163,7 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
       if (tile_counts) tile_counts[i] = pr.tiles;
       if (depth_keys) depth_keys[i] = pr.depth_bits;
       if (depth_order) depth_order[i] = i;
+      if (radii) radii[i] = pr.radius;
     }
     if (step + 1 < mine) {
 #pragma unroll
@@ -1212,8 +1217,9 @@ static void destroy_scene(dg_renderer* r) {
   free_buffer(r->grad_splats);
   free_buffer(r->grad_gaussians);
   free_buffer(r->grad_sh);
+  free_buffer(r->radii);
   if (r->rasterizer) dg_tile_rasterizer_destroy(r->rasterizer);
-  r->gaussians = r->splats = r->sh = r->scene_params = nullptr;
+  r->gaussians = r->splats = r->sh = r->scene_params = r->radii = nullptr;
   r->grad_splats = r->grad_gaussians = r->grad_sh = nullptr;
   r->rasterizer = nullptr;
   r->has_scene = false;
@@ -1230,6 +1236,7 @@ static dg_status create_scene(dg_renderer* r, uint32_t count, dg_buffer* gaussia
   const uint32_t params[4] = {degree, 0, 0, 0};
   DG_TRY(write_async(r->ctx, r->scene_params->ptr, params, sizeof(params)));
   DG_TRY(alloc_buffer(r->ctx, (size_t)count * FLOATS_PER_SPLAT * 4, &r->splats));
+  DG_TRY(alloc_buffer(r->ctx, (size_t)std::max(count, 1u) * 4, &r->radii));
   DG_TRY(rasterizer_create(r->ctx, r->camera, r->splats, count, pair_capacity, true, true, &r->rasterizer));
   return DG_OK;
 }
@@ -1259,7 +1266,7 @@ dg_status renderer_launch_forward(dg_renderer* r, dg_buffer* target) {
                   typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
                   typed<uint32_t>(r->scene_params), typed<float>(r->splats),
                   typed<uint32_t>(r->rasterizer->tile_offsets), typed<uint32_t>(r->rasterizer->depth_keys),
-                  typed<uint32_t>(r->rasterizer->depth_values)));
+                  typed<uint32_t>(r->rasterizer->depth_values), typed<float>(r->radii)));
   }
   return rasterizer_launch(r->rasterizer, target, true);
 }

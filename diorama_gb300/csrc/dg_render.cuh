@@ -140,6 +140,7 @@ struct dg_renderer {
   dg_buffer* splats;
   dg_buffer* sh;
   dg_buffer* scene_params;  // element 0: SH degree
+  dg_buffer* radii;         // each splat's radius of the last preprocess, densely
   dg_tile_rasterizer* rasterizer;
   dg_buffer* grad_splats;
   dg_buffer* grad_gaussians;

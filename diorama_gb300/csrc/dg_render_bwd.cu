@@ -608,7 +608,7 @@ __device__ __forceinline__ float4 f4_load(const float* p) { return *reinterpret_
 // the wait limit sets DEVICE_ERROR_COPY_WAIT and the CTA returns.
 __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
     const Camera* __restrict__ camera, float* __restrict__ gaussians, float* __restrict__ sh, uint32_t count,
-    const uint32_t* __restrict__ scene_params, const float* __restrict__ splats, const float* __restrict__ splat_grads,
+    const uint32_t* __restrict__ scene_params, const float* __restrict__ radii, const float* __restrict__ splat_grads,
     const AdamParams* __restrict__ adam, float* __restrict__ params, float2* __restrict__ moments,
     float4* __restrict__ stats, float2* __restrict__ aux, float* __restrict__ gaussian_grads,
     float* __restrict__ sh_grads, uint32_t* __restrict__ error) {
@@ -644,13 +644,14 @@ __global__ void DG_PBWD_BOUNDS preprocess_backward_adam_kernel(
   const uint32_t i = block_start + threadIdx.x;
   if (i < count) {
     float out[16];
+    const float radius = radii[i];
+    const float* grads = splat_grads + (size_t)i * SPLAT_GRADS;
     preprocess_backward_one(s_cam, gaussians + (size_t)i * FLOATS_PER_GAUSSIAN, s_sh + threadIdx.x * SH_REST_FLOATS,
-                            basis_count, splats[(size_t)i * FLOATS_PER_SPLAT + 3],
-                            splat_grads + (size_t)i * SPLAT_GRADS, out);
+                            basis_count, radius, grads, out);
 #pragma unroll
     for (int k = 0; k < 16; k++) s_pg[threadIdx.x * GP + k] = out[k];
     if (gaussian_grads) store16(gaussian_grads + (size_t)i * FLOATS_PER_GAUSSIAN, out);
-    accumulate_stats_one(s_ap.viewport, splats, splat_grads, stats, aux, i);
+    accumulate_stats_values(s_ap.viewport, radius, grads[0], grads[1], stats, aux, i);
   }
   __syncthreads();
   if (sh_grads) copy_floats(sh_grads + (size_t)block_start * SH_REST_FLOATS, s_sh, sh_total);
@@ -780,7 +781,7 @@ dg_status launch_preprocess_backward_adam(dg_renderer* r, const AdamParams* adam
   DG_LAUNCH(r->ctx, "preprocess_backward_adam",
             preprocess_backward_adam_kernel<<<ceil_div(r->count, PBWD_THREADS), PBWD_THREADS, 0, r->ctx->stream>>>(
                 typed<const Camera>(r->camera), typed<float>(r->gaussians), typed<float>(r->sh), r->count,
-                typed<uint32_t>(r->scene_params), typed<float>(r->splats), typed<float>(r->grad_splats), adam, params,
+                typed<uint32_t>(r->scene_params), typed<float>(r->radii), typed<float>(r->grad_splats), adam, params,
                 moments, stats, aux, keep_gradients ? typed<float>(r->grad_gaussians) : nullptr,
                 keep_gradients ? typed<float>(r->grad_sh) : nullptr, r->ctx->device_error));
   return DG_OK;
