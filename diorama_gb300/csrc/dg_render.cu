@@ -13,7 +13,10 @@
 namespace dg {
 namespace {
 
-constexpr int PRE_THREADS = 128;
+#ifndef DG_PRE_THREADS
+#define DG_PRE_THREADS 128
+#endif
+constexpr int PRE_THREADS = DG_PRE_THREADS;  // 64 and 96 measured slower (84.8, 88.8 us against 75.8 at 1.1M)
 constexpr int DUP_THREADS = 256;
 constexpr int RANGE_THREADS = 256;
 
