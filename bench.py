@@ -524,7 +524,7 @@ def run_reference(args, rank, world, group):
     for cam in cams[: max(1, min(4, len(cams)))]:
         c = oracle.camera_array(cam.view, cam.proj, (W, H))
         photos.append(oracle.render(c, np.zeros(3, np.float32), truth, truth_sh.reshape(-1), 3)["rgba8"])
-    base = cpu_baseline(args, raw, sh, photos, cams, samples=1)  # warm-up and per-step estimate
+    base = cpu_baseline(args, raw, sh, photos, cams, samples=args.warmup)  # warm-up and per-step estimate
     per_step = 1.0 / base["value"]
     budget = 180.0
     steps = max(1, min(args.steps, int(budget / per_step)))
@@ -533,7 +533,7 @@ def run_reference(args, rank, world, group):
     timed["sample"] = (f"{steps} of {args.steps} requested full optimize() steps (capped at ~{int(budget)} s of CPU "
                        f"work), {timed['sample']}")
     return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": 1,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
         "ms_per_step": round(1000.0 / value, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded planes-and-boxes scene)", "config": config(args, world),
         "impl": "reference", "cpu_baseline": timed,
