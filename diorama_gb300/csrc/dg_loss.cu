@@ -47,12 +47,23 @@ __device__ __forceinline__ float3 load_x(const float4* rendered, int w, int h, i
   return make_float3(v.x, v.y, v.z);
 }
 
-__device__ __forceinline__ float3 load_y(const uchar4* target, int w, int h, int x, int y, bool exact_quotient) {
+// A byte's value as float, v / 255: the loss's float quotient, or for metrics
+// (exact_quotient) Float32Array.from(bytes, v => v / 255), the double quotient
+// rounded to float.
+__device__ __forceinline__ float unorm8(uint32_t v, bool exact_quotient) {
+  return exact_quotient ? __double2float_rn(v / 255.0) : (float)v / 255.0f;
+}
+
+// The 256 values of unorm8 in shared memory (thread t writes entry t of each
+// 256-thread CTA), so a pixel's three channels take three loads, not divisions.
+__device__ __forceinline__ void fill_unorm8(float* table, bool exact_quotient) {
+  table[threadIdx.x] = unorm8(threadIdx.x, exact_quotient);
+}
+
+__device__ __forceinline__ float3 load_y(const uchar4* target, int w, int h, int x, int y, const float* unorm) {
   if (x < 0 || y < 0 || x >= w || y >= h) return make_float3(0.f, 0.f, 0.f);
   uchar4 t = target[(size_t)y * w + x];
-  if (exact_quotient)  // Float32Array.from(bytes, v => v / 255): the double quotient rounded to float
-    return make_float3(__double2float_rn(t.x / 255.0), __double2float_rn(t.y / 255.0), __double2float_rn(t.z / 255.0));
-  return make_float3((float)t.x / 255.0f, (float)t.y / 255.0f, (float)t.z / 255.0f);
+  return make_float3(unorm[t.x], unorm[t.y], unorm[t.z]);
 }
 
 // Moments, both blurs and the SSIM partials for one 16x16 block. mode 0 (loss):
@@ -72,13 +83,16 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
   __shared__ float2 s_h23[LS][LT][3];  // of x^2 and y^2
   __shared__ float s_h4[LS][LT][3];    // of xy
   __shared__ double s_red[2][8];
+  __shared__ float s_unorm[256];
   const uchar4* target = *target_slot;
   const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
   const bool metrics = mode == 1;
+  fill_unorm8(s_unorm, metrics);
+  __syncthreads();
   for (int k = threadIdx.x; k < LS * LS; k += 256) {
     const int ly = k / LS, lx = k % LS;
     float3 xv = load_x(rendered, w, h, x0 + lx, y0 + ly, metrics);
-    float3 yv = load_y(target, w, h, x0 + lx, y0 + ly, metrics);
+    float3 yv = load_y(target, w, h, x0 + lx, y0 + ly, s_unorm);
     s_xy[ly][lx][0] = make_float2(xv.x, yv.x);
     s_xy[ly][lx][1] = make_float2(xv.y, yv.y);
     s_xy[ly][lx][2] = make_float2(xv.z, yv.z);
@@ -181,8 +195,10 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
   __shared__ float s_p2[LS][LS][3];
   __shared__ float2 s_h01[LS][LT][3];
   __shared__ float s_h2[LS][LT][3];
+  __shared__ float s_unorm[256];  // read after the barriers below
   const uchar4* target = *target_slot;
   const int x0 = blockIdx.x * LT - HALO, y0 = blockIdx.y * LT - HALO;
+  fill_unorm8(s_unorm, false);
   for (int k = threadIdx.x; k < LS * LS; k += 256) {
     const int ly = k / LS, lx = k % LS;
     const int gx = x0 + lx, gy = y0 + ly;
@@ -227,7 +243,7 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
   const float4 xv4 = rendered[p];
   const uchar4 t4 = target[p];
   const float xs[3] = {xv4.x, xv4.y, xv4.z};
-  const float ys[3] = {(float)t4.x / 255.0f, (float)t4.y / 255.0f, (float)t4.z / 255.0f};
+  const float ys[3] = {s_unorm[t4.x], s_unorm[t4.y], s_unorm[t4.z]};
   const float* own = partials + p * 12;
   float grad[3];
   float lsum = 0.0f;
