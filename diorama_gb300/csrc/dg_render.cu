@@ -565,17 +565,16 @@ struct PixelBlend {
     return true;
   }
 
-  // Blends one splat of alpha `alpha` (0: not blended here) and colour c at list
-  // position pos; stops before the splat that would take the transmittance below
-  // 1e-4 (src/shaders/rasterize.wgsl:62-92). Without branches: a splat the pixel
-  // does not take adds c * 0 (colours are non-negative, so the sums do not change)
-  // and keeps T and last.
-  __device__ __forceinline__ void blend(float alpha, float4 c, uint32_t pos) {
+  // Blends one splat of alpha `alpha` (0: not blended here) and colour c whose
+  // 1-based list position is pos1; stops before the splat that would take the
+  // transmittance below 1e-4 (src/shaders/rasterize.wgsl:62-92). Without
+  // branches: a splat the pixel does not take adds c * 0 (colours are
+  // non-negative, so the sums do not change) and keeps T and last. While the pixel
+  // runs T >= 1e-4, so alpha 0 (remaining = T) never stops it.
+  __device__ __forceinline__ void blend(float alpha, float4 c, uint32_t pos1) {
     const float remaining = T * (1.0f - alpha);
-    const bool live = alpha != 0.0f && !done;
-    const bool stop = live && remaining < 0.0001f;
-    const bool take = live && !stop;
-    done = done || stop;
+    done = done || remaining < 0.0001f;
+    const bool take = !done && alpha != 0.0f;
     // color += c alpha T (src/shaders/rasterize.wgsl:88) as c (alpha T) + color,
     // one fused multiply-add per channel (the oracle's same sequence).
     const float w = take ? __fmul_rn(alpha, T) : 0.0f;
@@ -583,7 +582,7 @@ struct PixelBlend {
     g = __fmaf_rn(c.y, w, g);
     b = __fmaf_rn(c.z, w, b);
     T = take ? remaining : T;
-    last = take ? pos + 1 : last;
+    last = take ? pos1 : last;
   }
 
   // Applies up to 4 staged entries e[0..n) of `st` in list order. Sets bit
@@ -602,7 +601,7 @@ struct PixelBlend {
       if ((any >> u) & 1u) {  // the same on every lane
         const uint32_t pos = st.pos[e[u]];
         blended |= 1u << (pos - base);
-        blend(alpha[u], st.color[e[u]], pos);
+        blend(alpha[u], st.color[e[u]], pos + 1);
       }
     }
   }
@@ -694,7 +693,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
     uint32_t* __restrict__ counters, bool cut_in_record) {
   __shared__ WarpStage stages[FWD_WARPS];
   // Cooperative blending, double-buffered by round: each producer's queued entries
-  // (alpha per pixel; colour with the list position's bits in w) and their count.
+  // (alpha per pixel; colour with the 1-based list position's bits in w) and their count.
   __shared__ float s_alpha[2][PRODUCERS][32][32];
   __shared__ float4 s_qcolor[2][PRODUCERS][32];
   __shared__ uint32_t s_qlive[2][PRODUCERS];
@@ -776,7 +775,7 @@ __global__ void __launch_bounds__(FWD_THREADS) rasterize_kernel(
               const uint32_t slot = live + __popc(any & ((1u << lane) - 1u));
               const float4 c = st.color[j + lane];
               const uint32_t pos = st.pos[j + lane];
-              s_qcolor[buf][pw][slot] = make_float4(c.x, c.y, c.z, __uint_as_float(pos));
+              s_qcolor[buf][pw][slot] = make_float4(c.x, c.y, c.z, __uint_as_float(pos + 1));
               bit = 1u << (pos - (start - run.x));
             }
             blended |= __reduce_or_sync(0xffffffffu, bit);
