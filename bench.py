@@ -402,7 +402,7 @@ def run_ours(args, rank, world, local, group):
         v.image.destroy()
     for p in pinned:
         p.free()
-    # The benchmark spec's second measure: learned against plain densification at the
+    # The second measure of the path: learned against plain densification at the
     # ~1.1M-Gaussian scale (rank 0 of a replica run; minutes).
     if rank == 0 and not args.no_densify_comparison:
         result["densify_comparison"] = densify_comparison(device, args)
