@@ -265,6 +265,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return done != 0;
 }
+// L2 eviction priorities. A kernel that streams far more data than L2 holds but
+// reads a small part of it twice marks the stream evict-first and the part it
+// will read again evict-last, so the stream does not push that part out first.
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+
 // Waits for phase `parity` of the barrier to complete, at most SPIN_LIMIT polls
 // (each try_wait may itself suspend the thread for a while). Returns false if it
 // gave up.

@@ -327,19 +327,7 @@ __device__ __forceinline__ void bulk_copy_to_shared(void* dst, const void* src, 
       : "memory");
 }
 
-// ---- L2 eviction priorities. A kernel that streams far more data than L2 holds
-// but reads a small part of it twice marks the stream evict-first and the part it
-// will read again evict-last, so the stream does not push that part out first.
-__device__ __forceinline__ uint64_t l2_policy_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_evict_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
-  return p;
-}
+// ---- Loads and stores with an L2 eviction policy (l2_policy_*, dg_common.cuh).
 __device__ __forceinline__ float4 ld_hinted(const void* p, uint64_t policy) {
   float4 v;
   asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;\n"

@@ -155,17 +155,32 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   }
 }
 
-// Loads a thread's SCAN_ITEMS consecutive values of tile `tile` (zeros past n).
-// `full`: all of them are in range and 16-byte aligned.
+__device__ __forceinline__ uint4 ld_u4_hinted(const uint4* p, uint64_t policy) {
+  uint4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;\n"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p), "l"(policy)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_u4_hinted(uint4* p, uint4 v, uint64_t policy) {
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %2, %3, %4}, %5;\n" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+               "r"(v.w), "l"(policy)
+               : "memory");
+}
+
+// Loads a thread's SCAN_ITEMS consecutive values of tile `tile` (zeros past n),
+// with L2 eviction policy `policy` (l2_policy_*). `full`: all of them are in
+// range and 16-byte aligned.
 __device__ __forceinline__ void load_items(const uint32_t* __restrict__ data, uint32_t n, uint32_t tile,
-                                           uint32_t (&v)[SCAN_ITEMS], bool& full, uint64_t& base) {
+                                           uint32_t (&v)[SCAN_ITEMS], bool& full, uint64_t& base, uint64_t policy) {
   base = (uint64_t)tile * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
   full = base + SCAN_ITEMS <= n && (reinterpret_cast<uintptr_t>(data) & 15) == 0;
   if (full) {
     const uint4* p = reinterpret_cast<const uint4*>(data + base);
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS / 4; k++) {
-      uint4 q = p[k];
+      const uint4 q = ld_u4_hinted(p + k, policy);
       v[4 * k] = q.x; v[4 * k + 1] = q.y; v[4 * k + 2] = q.z; v[4 * k + 3] = q.w;
     }
   } else {
@@ -174,11 +189,15 @@ __device__ __forceinline__ void load_items(const uint32_t* __restrict__ data, ui
   }
 }
 
-// Large scans without a gather: reduce, then scan the tile sums, then re-scan each
-// tile from its prefix. Three launches and a second read of the values, but no
-// look-back: in one wave of single-pass CTAs, a tile early in the wave waits on a
-// chain of look-backs about as long as its place in the wave (at 12M values the
-// single-pass scan ran at ~0.3 of the copy rate).
+// Large scans without a gather: reduce, then re-scan each tile from its prefix, the
+// sum of the tile sums before it, which each CTA adds up itself from L2 (up to
+// FOLD_MAX_TILES tiles; past that a single-pass scan of the tile sums runs in
+// between). A second read of the values, but no look-back: in one wave of
+// single-pass CTAs, a tile early in the wave waits on a chain of look-backs about
+// as long as its place in the wave (at 12M values the single-pass scan ran at
+// ~0.3 of the copy rate). The reduce reads the values with an L2 evict-last
+// policy (48 MB at 12M values, well inside L2), so the re-scan reads them from
+// L2, with evict-first loads and stores as their last use.
 __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_t* __restrict__ data, uint32_t capacity,
                                                                    const uint32_t* __restrict__ count,
                                                                    uint32_t* __restrict__ tile_sums) {
@@ -187,7 +206,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_
   uint32_t v[SCAN_ITEMS];
   bool full;
   uint64_t base;
-  load_items(data, n, blockIdx.x, v, full, base);
+  load_items(data, n, blockIdx.x, v, full, base, l2_policy_evict_last());
   uint32_t sum = 0;
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; k++) sum += v[k];
@@ -203,25 +222,47 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const uint32_
   }
 }
 
-// tile_prefix: the scanned tile sums (each tile's exclusive prefix).
+// fold: tile_sums holds each tile's sum, and each CTA adds up those before its
+// own; the last tile's CTA writes the grand total. Otherwise tile_sums holds the
+// scanned tile sums (each tile's exclusive prefix) and `total` is not touched.
 __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_kernel(uint32_t* __restrict__ data, uint32_t capacity,
                                                                   const uint32_t* __restrict__ count,
-                                                                  const uint32_t* __restrict__ tile_prefix) {
+                                                                  const uint32_t* __restrict__ tile_sums, bool fold,
+                                                                  uint32_t* __restrict__ total) {
   __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_part[SCAN_THREADS / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t n = count ? min(*count, capacity) : capacity;
-  if ((uint64_t)blockIdx.x * SCAN_TILE >= n) return;  // the whole CTA
+  const uint32_t tiles = (uint32_t)(((uint64_t)n + SCAN_TILE - 1) / SCAN_TILE);  // tiles holding values
+  if (blockIdx.x >= tiles) {  // the whole CTA
+    if (fold && n == 0 && blockIdx.x == 0 && tid == 0) *total = 0;
+    return;
+  }
+  // The tile sums before this tile (L2 reads, issued with the tile's own loads).
+  uint32_t part = 0;
+  if (fold)
+    for (uint32_t j = tid; j < blockIdx.x; j += SCAN_THREADS) part += tile_sums[j];
+  const uint64_t last_use = l2_policy_evict_first();
   uint32_t v[SCAN_ITEMS];
   bool full;
   uint64_t base;
-  load_items(data, n, blockIdx.x, v, full, base);
+  load_items(data, n, blockIdx.x, v, full, base, last_use);
   uint32_t sum = 0;
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; k++) sum += v[k];
   const uint32_t incl = warp_inclusive(sum, lane);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) part += __shfl_xor_sync(0xffffffffu, part, d);
   if (lane == 31) s_warp[warp] = incl;
+  if (lane == 0) s_part[warp] = part;
   __syncthreads();
-  uint32_t before = tile_prefix[blockIdx.x];
+  uint32_t before = 0;
+  if (fold) {
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; w++) before += s_part[w];
+  } else {
+    before = tile_sums[blockIdx.x];
+  }
 #pragma unroll
   for (int w = 0; w < SCAN_THREADS / 32; w++) before += w < warp ? s_warp[w] : 0u;
   uint32_t running = before + incl - sum;
@@ -231,10 +272,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_kernel(uint32_t* __re
     v[k] = running;
     running += x;
   }
+  if (fold && blockIdx.x == tiles - 1 && tid == SCAN_THREADS - 1) *total = running;
   if (full) {
     uint4* p = reinterpret_cast<uint4*>(data + base);
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS / 4; k++) p[k] = make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    for (int k = 0; k < SCAN_ITEMS / 4; k++)
+      st_u4_hinted(p + k, make_uint4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]), last_use);
   } else {
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++)
@@ -246,6 +289,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles_kernel(uint32_t* __re
 // values the single pass is faster (16 us against 21), at 12M the two-level one
 // (37 us against 49).
 constexpr uint32_t TWO_LEVEL_MIN = 1u << 21;
+// Up to this many tiles (16.7M values) each re-scanning CTA adds up the tile sums
+// before it itself (at most 16 L2 reads a thread).
+constexpr uint32_t FOLD_MAX_TILES = 4096;
 
 size_t single_pass_scratch_bytes(uint32_t capacity) {
   uint32_t tiles = std::max(1u, ceil_div(capacity, SCAN_TILE));
@@ -271,9 +317,10 @@ dg_status scan_launch(dg_context* ctx, uint32_t* data, uint32_t capacity, const 
     void* inner = static_cast<char*>(scratch) + (((size_t)tiles * 4 + 255) & ~(size_t)255);
     DG_LAUNCH(ctx, "scan_reduce",
               scan_reduce_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, sums));
-    DG_TRY(scan_launch(ctx, sums, tiles, nullptr, total, inner));  // tiles < TWO_LEVEL_MIN: single pass
+    const bool fold = tiles <= FOLD_MAX_TILES;
+    if (!fold) DG_TRY(scan_launch(ctx, sums, tiles, nullptr, total, inner));  // tiles < TWO_LEVEL_MIN: single pass
     DG_LAUNCH(ctx, "scan",
-              scan_tiles_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, sums));
+              scan_tiles_kernel<<<tiles, SCAN_THREADS, 0, ctx->stream>>>(data, capacity, count, sums, fold, total));
     return DG_OK;
   }
   auto* ticket = static_cast<uint32_t*>(scratch);

@@ -63,6 +63,28 @@ def test_prefix_sum_device_count(device):
     count.destroy()
 
 
+# Two-level scans (from 2^21 values): tile sums added up by each re-scanning CTA
+# (up to 4096 tiles) or scanned in between (past that), with device counts of
+# zero, a partial last tile and the full capacity.
+@pytest.mark.parametrize("capacity,n", [(3_000_000, 0), (3_000_000, 2_500_001), (3_000_000, 3_000_000),
+                                        (20_000_001, 17_000_000), (20_000_001, 20_000_001)])
+def test_prefix_sum_two_level_device_count(device, capacity, n):
+    rng = np.random.default_rng(capacity + n)
+    values = rng.integers(0, 1000, capacity).astype(np.uint32)
+    buf = device.upload(values)
+    count = device.upload(np.array([n], np.uint32))
+    scan = PrefixSum(device, buf, capacity, count)
+    scan.encode()
+    out = buf.read(np.uint32)
+    assert np.array_equal(out[:n], exclusive(values[:n]))
+    assert np.array_equal(out[n:], values[n:])  # past the count: untouched
+    assert int(scan.total.read(np.uint32)[0]) == int(values[:n].sum(dtype=np.uint64) & 0xFFFFFFFF)
+    assert device.check() == 0
+    scan.destroy()
+    buf.destroy()
+    count.destroy()
+
+
 @pytest.mark.parametrize("size", [1, 1000, 1024, 3840, 3841, 100_003])
 def test_radix_sort_32(device, size):
     keys = sort_keys(size)
