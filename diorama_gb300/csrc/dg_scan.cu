@@ -57,6 +57,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_kernel(uint32_t* __restrict
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t n = count_ptr ? min(*count_ptr, capacity) : capacity;
   uint32_t tiles = max(1u, (n + SCAN_TILE - 1) / SCAN_TILE);
+  // The grid covers the capacity; CTAs past this call's tiles leave at once, and
+  // the first `tiles` CTAs take the tickets 0..tiles-1, in arrival order.
+  if (blockIdx.x >= tiles) return;
   if (tid == 0) s_tile = atomicAdd(ticket, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;

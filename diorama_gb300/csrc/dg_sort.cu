@@ -177,6 +177,9 @@ __global__ void __launch_bounds__(SORT_THREADS, DG_SORT_MIN_BLOCKS)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t n = count ? min(*count, capacity) : capacity;
   const uint32_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+  // The grid covers the capacity; CTAs past the tiles of this call's keys leave at
+  // once. The first `tiles` CTAs take the tickets 0..tiles-1, in arrival order.
+  if (blockIdx.x >= tiles) return;
   if (tid == 0) s_tile = atomicAdd(ticket, 1u);
   for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) s_whist[i] = 0;
   __syncthreads();
