@@ -101,24 +101,39 @@ __global__ void __launch_bounds__(256) ssim_kernel(const float4* __restrict__ re
 #pragma unroll
   for (int k = 0; k < 6; k++) wp[k] = f2(win.w[k], win.w[k]);
   __syncthreads();
-  // Horizontal pass over every halo row, for the 16 output columns.
-  for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
-    const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    F2 a01 = f2(0.f, 0.f), a23 = f2(0.f, 0.f);
-    float a4 = 0.f;
+  // Horizontal pass over every halo row, for the 16 output columns, two adjacent
+  // columns per item: their 11-tap windows share 10 halo values, read (and
+  // squared) once. Each column's sums still run over its taps -5..5 in order.
+  for (int k = threadIdx.x; k < LS * (LT / 2) * 3; k += 256) {
+    const int ch = k % 3, col = 2 * ((k / 3) % (LT / 2)), row = k / (3 * (LT / 2));
+    F2 a01 = f2(0.f, 0.f), a23 = f2(0.f, 0.f), b01 = a01, b23 = a01;
+    float a4 = 0.f, b4 = 0.f;
     // Taps past the image read the halo's zeros and add exactly 0: the same sums
     // as skipping them, without a branch per tap.
 #pragma unroll
-    for (int t = -HALO; t <= HALO; t++) {
-      const int at = t < 0 ? -t : t;
+    for (int t = -HALO; t <= HALO + 1; t++) {  // halo column col + HALO + t
       const F2 xy = f2_load(&s_xy[row][col + HALO + t][ch]);
-      a01 = f2_fma(wp[at], xy, a01);                // x, y
-      a23 = f2_fma(wp[at], f2_mul(xy, xy), a23);    // x^2, y^2
-      a4 = fmaf(win.w[at], f2_lo(xy) * f2_hi(xy), a4);  // xy
+      const F2 sq = f2_mul(xy, xy);
+      const float pr = f2_lo(xy) * f2_hi(xy);
+      if (t <= HALO) {  // column col, tap t
+        const int at = t < 0 ? -t : t;
+        a01 = f2_fma(wp[at], xy, a01);  // x, y
+        a23 = f2_fma(wp[at], sq, a23);  // x^2, y^2
+        a4 = fmaf(win.w[at], pr, a4);   // xy
+      }
+      if (t > -HALO) {  // column col + 1, tap t - 1
+        const int at = t - 1 < 0 ? 1 - t : t - 1;
+        b01 = f2_fma(wp[at], xy, b01);
+        b23 = f2_fma(wp[at], sq, b23);
+        b4 = fmaf(win.w[at], pr, b4);
+      }
     }
     f2_store(&s_h01[row][col][ch], a01);
     f2_store(&s_h23[row][col][ch], a23);
     s_h4[row][col][ch] = a4;
+    f2_store(&s_h01[row][col + 1][ch], b01);
+    f2_store(&s_h23[row][col + 1][ch], b23);
+    s_h4[row][col + 1][ch] = b4;
   }
   __syncthreads();
   const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
@@ -221,18 +236,30 @@ __global__ void __launch_bounds__(256) gradient_kernel(const float4* __restrict_
 #pragma unroll
   for (int k = 0; k < 6; k++) wp[k] = f2(win.w[k], win.w[k]);
   __syncthreads();
-  for (int k = threadIdx.x; k < LS * LT * 3; k += 256) {
-    const int ch = k % 3, col = (k / 3) % LT, row = k / (3 * LT);
-    F2 a01 = f2(0.f, 0.f);
-    float a2 = 0.f;
+  // Two adjacent output columns per item, as in ssim_kernel.
+  for (int k = threadIdx.x; k < LS * (LT / 2) * 3; k += 256) {
+    const int ch = k % 3, col = 2 * ((k / 3) % (LT / 2)), row = k / (3 * (LT / 2));
+    F2 a01 = f2(0.f, 0.f), b01 = a01;
+    float a2 = 0.f, b2 = 0.f;
 #pragma unroll
-    for (int t = -HALO; t <= HALO; t++) {  // the halo holds zeros past the image
-      const int at = t < 0 ? -t : t;
-      a01 = f2_fma(wp[at], f2_load(&s_p01[row][col + HALO + t][ch]), a01);
-      a2 = fmaf(win.w[at], s_p2[row][col + HALO + t][ch], a2);
+    for (int t = -HALO; t <= HALO + 1; t++) {  // the halo holds zeros past the image
+      const F2 p01 = f2_load(&s_p01[row][col + HALO + t][ch]);
+      const float p2 = s_p2[row][col + HALO + t][ch];
+      if (t <= HALO) {  // column col, tap t
+        const int at = t < 0 ? -t : t;
+        a01 = f2_fma(wp[at], p01, a01);
+        a2 = fmaf(win.w[at], p2, a2);
+      }
+      if (t > -HALO) {  // column col + 1, tap t - 1
+        const int at = t - 1 < 0 ? 1 - t : t - 1;
+        b01 = f2_fma(wp[at], p01, b01);
+        b2 = fmaf(win.w[at], p2, b2);
+      }
     }
     f2_store(&s_h01[row][col][ch], a01);
     s_h2[row][col][ch] = a2;
+    f2_store(&s_h01[row][col + 1][ch], b01);
+    s_h2[row][col + 1][ch] = b2;
   }
   __syncthreads();
   const int lx = threadIdx.x % LT, ly = threadIdx.x / LT;
