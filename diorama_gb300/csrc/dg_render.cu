@@ -177,12 +177,12 @@ __global__ void __launch_bounds__(PRE_THREADS) preprocess_kernel(const Camera* _
 
 // CTAs of preprocess_kernel that fit on the device at once (its grid).
 uint32_t preprocess_grid(const dg_context* ctx, uint32_t count) {
-  static int per_sm = 0;
-  if (per_sm == 0) {
+  // Queried once per process (a function-local static initializes thread-safely).
+  static const int per_sm = [] {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, preprocess_kernel, PRE_THREADS, 0) != cudaSuccess) n = 1;
-    per_sm = std::max(1, n);
-  }
+    return std::max(1, n);
+  }();
   const uint32_t blocks = std::max(1u, ceil_div(count, PRE_THREADS));
   return std::min(blocks, (uint32_t)per_sm * (uint32_t)ctx->sm_count);
 }
