@@ -29,9 +29,12 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
-    # Every binding this package uses is declared in the header too.
+    # Every binding this package uses is declared in the header too, and every
+    # entry point the header declares has a ctypes signature here.
     undeclared = [n for n in _lib.SIGNATURES if n not in declared_functions()]
     assert not undeclared, undeclared
+    unbound = [n for n in declared_functions() if n != "dg_status" and n not in _lib.SIGNATURES]
+    assert not unbound, unbound
 
 
 def test_exports_have_c_linkage():
